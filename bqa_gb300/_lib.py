@@ -1,0 +1,93 @@
+"""ctypes binding of ``libbqa_gb300.so`` (the C ABI declared in ``include/bqa_gb300.h``).
+
+There is no fallback: if the library was not built, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
+ABI_VERSION = 1
+
+BQA_OK = 0
+BQA_STATUS_SVD_NOT_CONVERGED = 1
+
+
+class BqaClass(ctypes.Structure):
+    """Mirror of ``struct bqa_class``."""
+    _fields_ = [
+        ("degree", c_int32),
+        ("count", c_int32),
+        ("node_ids", c_void_p),
+        ("in_pos", c_void_p),
+        ("out_pos", c_void_p),
+        ("lmbd_pos", c_void_p),
+        ("edge_ampl", c_void_p),
+        ("node_ampl", c_void_p),
+        ("tensor", c_void_p),
+        ("tensor_out", c_void_p),
+    ]
+
+
+# name -> (restype, argtypes); every exported symbol of the header
+SIGNATURES = {
+    "bqa_abi_version": (c_int32, []),
+    "bqa_last_error": (ctypes.c_char_p, []),
+    "bqa_max_bond_dim": (c_int32, [c_int32]),
+    "bqa_bp_sweep": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bqa_bp_finalize": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_float, c_float, c_int32, c_void_p]),
+    "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),
+    "bqa_env_factor": (c_int32, [c_void_p, c_int32, c_int32, c_float, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bqa_bond_canon": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_float, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p]),
+    "bqa_apply_update": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32,
+                                   c_double, c_double, c_void_p]),
+    "bqa_msgs_from_lmbds": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_densities": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    "bqa_psplit": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    "bqa_edge_zz": (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_project_nodes": (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p]),
+}
+
+
+class BqaError(RuntimeError):
+    pass
+
+
+class Library:
+    """Loaded library with checked calls: ``lib.call("bqa_x", ...)`` raises on a bad status."""
+
+    def __init__(self, path: Path = LIB_PATH):
+        if not path.exists():
+            raise BqaError(f"{path} is missing: build the GB300 backend first "
+                           "(python -m bqa_gb300.build, or __graft_entry__.build())")
+        self.path = path
+        self.dll = ctypes.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(self.dll, name)
+            fn.restype = res
+            fn.argtypes = args
+        v = self.dll.bqa_abi_version()
+        if v != ABI_VERSION:
+            raise BqaError(f"{path} has ABI version {v}, expected {ABI_VERSION}: rebuild it")
+
+    def call(self, name: str, *args) -> None:
+        rc = getattr(self.dll, name)(*args)
+        if rc != BQA_OK:
+            msg = self.dll.bqa_last_error().decode(errors="replace")
+            raise BqaError(f"{name} failed with status {rc}: {msg}")
+
+    def max_bond_dim(self, degree: int) -> int:
+        return int(self.dll.bqa_max_bond_dim(degree))
+
+
+_LIB: Library | None = None
+
+
+def load() -> Library:
+    global _LIB
+    if _LIB is None:
+        _LIB = Library()
+    return _LIB

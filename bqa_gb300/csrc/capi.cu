@@ -1,0 +1,51 @@
+// Library-wide entry points of the C ABI: version, error text, size limits.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+
+#include "internal.h"
+#include "../../include/bqa_gb300.h"
+
+namespace bqa {
+
+static thread_local char g_last_error[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return BQA_OK;
+}
+
+int ensure_smem(const void* kernel, size_t bytes, const char* what) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, size_t> granted;
+    if (bytes <= 48 * 1024) return BQA_OK;
+    if (bytes > kMaxSmem) return set_error(BQA_ERR_UNSUPPORTED, "%s: needs %zu B of shared memory", what, bytes);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = granted.find(kernel);
+    if (it != granted.end() && it->second >= bytes) return BQA_OK;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "%s: cudaFuncSetAttribute: %s", what, cudaGetErrorString(e));
+    granted[kernel] = kMaxSmem;
+    return BQA_OK;
+}
+
+}  // namespace bqa
+
+extern "C" {
+
+int32_t bqa_abi_version(void) { return 1; }
+
+const char* bqa_last_error(void) { return bqa::g_last_error; }
+
+}  // extern "C"

@@ -1,0 +1,342 @@
+"""Device-resident annealing state and the per-step driver (the reference's state VM).
+
+``Annealer`` holds one job on one GPU: the degree-class index maps (int32), the node
+tensors of every class, the BP messages and the bond spectra, all resident in HBM, plus
+the scratch of the simple update.  Its methods mirror ``src/bqa/state.py``:
+
+============================  ==========================================  =====================
+reference (src/bqa/state.py)  here                                        C-ABI calls
+============================  ==========================================  =====================
+``_initialize_state`` :67     ``Annealer.__init__`` / ``reset``           msgs_from_lmbds
+``_simple_update`` :230       ``gate_layer``                              ext_msgs, env_factor,
+                                                                          bond_canon, apply_update
+``_apply_z/x_layer`` :142-156 fused into ``gate_layer``                   apply_update
+``_set_to_symmetric_gauge``   fused into ``gate_layer``                   apply_update, msgs_from_lmbds
+``_run_bp`` :97               ``run_bp``                                  bp_sweep, bp_finalize
+``run_layer`` :315            ``run_layer``
+``get_density_matrices`` :77  ``density_matrices``                        densities
+``measure`` :250              ``measure``                                 densities (+ host loop)
+(none)                        ``edge_zz`` / ``energy``                    psplit, edge_zz
+============================  ==========================================  =====================
+
+PyTorch only allocates device memory and supplies the stream; all arithmetic runs in
+``libbqa_gb300.so``.
+"""
+from __future__ import annotations
+
+import logging
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .layout import Context
+
+log = logging.getLogger(__name__)
+
+INIT_STATE = (np.sqrt(0.5), -np.sqrt(0.5))   # src/bqa/state.py:21
+
+
+def _ptr(t) -> int:
+    return t.data_ptr() if t is not None and t.numel() > 0 else 0
+
+
+@dataclass
+class _DeviceClass:
+    degree: int
+    count: int
+    node_ids: object
+    in_pos: object
+    out_pos: object
+    lmbd_pos: object
+    edge_ampl: object
+    node_ampl: object
+    tensors: list          # two ping-pong buffers, flat complex64
+
+
+class Annealer:
+    """One annealing job resident on one GPU."""
+
+    def __init__(self, ctx: Context, device=None, bp_check_every: int = 4):
+        import torch
+        self.torch = torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("the GB300 backend needs a CUDA device")
+        self.lib = _lib.load()
+        self.ctx = ctx
+        self.device = torch.device(device if device is not None else "cuda")
+        self.bp_check_every = max(1, int(bp_check_every))
+        E = ctx.edges_number
+        self.E = E
+        self.half = E // 2
+        chimax = ctx.max_bond_dim
+        for d in ctx.degree_to_layout:
+            lim = self.lib.max_bond_dim(d)
+            if chimax > lim:
+                raise NotImplementedError(
+                    f"max_bond_dim={chimax} with degree-{d} nodes is beyond what the GB300 kernels "
+                    f"hold on chip (max {lim} for this degree)")
+        dev = self.device
+        i32 = torch.int32
+        self.classes: list[_DeviceClass] = []
+        for d, L in ctx.degree_to_layout.items():
+            B = L.batch_size
+            size = B * 2 * chimax ** d
+            self.classes.append(_DeviceClass(
+                degree=d, count=B,
+                node_ids=torch.as_tensor(L.node_ids, dtype=i32, device=dev),
+                in_pos=torch.as_tensor(np.ascontiguousarray(L.input_msgs_position.T), dtype=i32, device=dev),
+                out_pos=torch.as_tensor(np.ascontiguousarray(L.output_msgs_position.T), dtype=i32, device=dev),
+                lmbd_pos=torch.as_tensor(np.ascontiguousarray(L.lmbds_position.T), dtype=i32, device=dev),
+                edge_ampl=torch.as_tensor(np.ascontiguousarray(np.asarray(L.edge_ampls, dtype=np.float64).T),
+                                          dtype=torch.float64, device=dev),
+                node_ampl=torch.as_tensor(L.node_ampls, dtype=torch.float64, device=dev),
+                tensors=[torch.empty(size, dtype=torch.complex64, device=dev) for _ in range(2)],
+            ))
+        nmax = 2 * chimax
+        c64 = torch.complex64
+        self.msgs = [torch.empty(E * chimax * chimax, dtype=c64, device=dev) for _ in range(2)]
+        # simple-update scratch: ext messages (later reused for canonicalisers), lu, ul
+        self.ext = torch.empty(E * nmax * nmax, dtype=c64, device=dev)
+        self.lu = torch.empty(E * nmax * nmax, dtype=c64, device=dev)
+        self.ul = torch.empty(E * nmax * nmax, dtype=c64, device=dev)
+        self.lmbds = torch.empty(self.half * nmax, dtype=torch.float32, device=dev)
+        self.colmax = torch.zeros(nmax, dtype=torch.int32, device=dev)
+        self.dist_parts = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.loop_state = torch.zeros(8, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.rho = torch.empty(ctx.nodes_number * 4, dtype=c64, device=dev)
+        self.zz = torch.empty(self.half, dtype=torch.float64, device=dev)
+        self.norm2 = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.rng = np.random.default_rng(ctx.seed)
+        self.stats: list[dict] = []
+        self.reset()
+
+    # ---- helpers -------------------------------------------------------------------------
+    @property
+    def stream(self) -> int:
+        return self.torch.cuda.current_stream(self.device).cuda_stream
+
+    def _class_array(self, out: bool = False):
+        arr = (_lib.BqaClass * len(self.classes))()
+        for i, c in enumerate(self.classes):
+            arr[i] = _lib.BqaClass(
+                c.degree, c.count, _ptr(c.node_ids), _ptr(c.in_pos), _ptr(c.out_pos), _ptr(c.lmbd_pos),
+                _ptr(c.edge_ampl), _ptr(c.node_ampl), _ptr(c.tensors[self.tcur]),
+                _ptr(c.tensors[1 - self.tcur]) if out else 0)
+        return arr
+
+    @property
+    def bond_dim(self) -> int:
+        return self.chi
+
+    def _msgs_cur(self):
+        return self.msgs[self.mcur]
+
+    # ---- state -----------------------------------------------------------------------------
+    def reset(self) -> None:
+        """Initial product state (src/bqa/state.py:41-74): every tensor [sqrt(.5), -sqrt(.5)],
+        bond dim 1, lambdas 1, messages diag(lambda)/tr."""
+        self.chi = 1
+        self.tcur = 0
+        self.mcur = 0
+        init = self.torch.tensor([complex(INIT_STATE[0]), complex(INIT_STATE[1])], dtype=self.torch.complex64,
+                                 device=self.device)
+        for c in self.classes:
+            c.tensors[0][: 2 * c.count].view(c.count, 2).copy_(init.expand(c.count, 2))
+        self.lam_stride = 1
+        self.lmbds[: self.half].fill_(1.0)
+        self.lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), 1, self.E, 1, _ptr(self._msgs_cur()), self.stream)
+
+    def set_state(self, degree_to_tensor: dict, msgs: np.ndarray, lmbds: np.ndarray | None = None) -> None:
+        """Load a state given as numpy arrays (tensors ``(B, 2, chi, ..)`` per degree, messages
+        ``(E, chi, chi)``, optional lambdas ``(E/2, chi)``); the bond dim is taken from msgs."""
+        torch = self.torch
+        chi = int(msgs.shape[-1])
+        if chi > self.ctx.max_bond_dim:
+            raise ValueError("state bond dim exceeds max_bond_dim")
+        self.chi, self.tcur, self.mcur = chi, 0, 0
+        for c in self.classes:
+            t = np.ascontiguousarray(degree_to_tensor[c.degree], dtype=np.complex64).reshape(-1)
+            c.tensors[0][: t.size].copy_(torch.from_numpy(t))
+        m = np.ascontiguousarray(msgs, dtype=np.complex64).reshape(-1)
+        self.msgs[0][: m.size].copy_(torch.from_numpy(m))
+        if lmbds is not None:
+            lam = np.ascontiguousarray(lmbds.real, dtype=np.float32)
+            self.lam_stride = lam.shape[1]
+            self.lmbds[: lam.size].copy_(torch.from_numpy(lam.reshape(-1)))
+
+    def get_state(self) -> tuple[dict, np.ndarray, np.ndarray]:
+        """Numpy copies of (tensors per degree, messages (E, chi, chi), lambdas (E/2, chi))."""
+        chi = self.chi
+        tens = {}
+        for c in self.classes:
+            shape = (c.count, 2) + (chi,) * c.degree
+            tens[c.degree] = c.tensors[self.tcur][: int(np.prod(shape))].cpu().numpy().reshape(shape)
+        msgs = self._msgs_cur()[: self.E * chi * chi].cpu().numpy().reshape(self.E, chi, chi)
+        lam = self.lmbds[: self.half * self.lam_stride].cpu().numpy().reshape(self.half, self.lam_stride)[:, :chi]
+        return tens, msgs, lam
+
+    # ---- annealing step --------------------------------------------------------------------
+    def gate_layer(self, xtime: float, ztime: float) -> tuple[int, float]:
+        """ZZ layer with BP-gauged truncation (``_simple_update``, src/bqa/state.py:230-247),
+        then the Rz and Rx layers and the symmetric gauge (state.py:142-156,219-227), fused:
+        extended messages -> environment factors -> bond canonicalisers and lambdas ->
+        global truncation dim (one small device-to-host read) -> tensor update ->
+        messages diag(lambda)/tr.  Returns (new bond dim, truncation error bound)."""
+        lib, st = self.lib, self.stream
+        ctx = self.ctx
+        chi = self.chi
+        n = 2 * chi
+        eps = float(ctx.pinv_eps)
+        cls = self._class_array()
+        lib.call("bqa_ext_msgs", cls, len(self.classes), chi, _ptr(self._msgs_cur()), _ptr(self.ext),
+                 float(ztime), st)
+        lib.call("bqa_env_factor", _ptr(self.ext), self.E, n, eps, _ptr(self.lu), _ptr(self.ul),
+                 _ptr(self.status), st)
+        self.colmax.zero_()
+        canon = self.ext  # the extended messages are consumed; reuse their storage
+        lib.call("bqa_bond_canon", _ptr(self.lu), _ptr(self.ul), self.E, n, eps, _ptr(canon),
+                 _ptr(self.lmbds), _ptr(self.colmax), _ptr(self.status), st)
+        # global truncation (src/bqa/backends.py:297-303)
+        max_l = self.colmax[:n].view(self.torch.float32).cpu().numpy().astype(np.float64)
+        rank = n - int(np.sum(max_l < eps))
+        dim = min(rank, ctx.max_bond_dim)
+        err = float(np.sqrt(np.sum(max_l[dim:] ** 2)))
+        log.info(f"Truncation performed, per edge error upper bound: {err}")
+        cls = self._class_array(out=True)
+        lib.call("bqa_apply_update", cls, len(self.classes), chi, dim, _ptr(canon), _ptr(self.lmbds), n,
+                 float(ztime), float(xtime), st)
+        self.tcur = 1 - self.tcur
+        self.chi = dim
+        self.lam_stride = n
+        lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), n, self.E, dim, _ptr(self._msgs_cur()), st)
+        return dim, err
+
+    def run_layer(self, xtime: float, ztime: float) -> dict:
+        """One annealing step (src/bqa/state.py:315-321)."""
+        dim, err = self.gate_layer(xtime, ztime)
+        sweeps = self.run_bp()
+        info = {"bond_dim": dim, "trunc_err": err, "sweeps": sweeps}
+        self.stats.append(info)
+        return info
+
+    def run_bp(self) -> int:
+        """Loopy BP to tolerance (src/bqa/state.py:97-124).  Sweeps are launched in groups of
+        ``bp_check_every`` between host checks; sweeps queued after convergence return at once
+        on the device.  Returns the number of sweeps run."""
+        ctx = self.ctx
+        if ctx.max_bp_iters_number < 1:
+            raise ValueError("max_bp_iter_number must be >= 1 to run belief propagation")
+        lib, st = self.lib, self.stream
+        cls = self._class_array()
+        a, b = self.msgs[self.mcur], self.msgs[1 - self.mcur]
+        self.loop_state.zero_()
+        self.dist_parts.zero_()
+        elems = self.E * self.chi * self.chi
+        launched = 0
+        eps, damp = float(ctx.bp_eps), float(ctx.damping)
+        while True:
+            for _ in range(min(self.bp_check_every, ctx.max_bp_iters_number - launched)):
+                lib.call("bqa_bp_sweep", cls, len(self.classes), self.chi, _ptr(a), _ptr(b),
+                         _ptr(self.dist_parts), _ptr(self.loop_state), st)
+                lib.call("bqa_bp_finalize", _ptr(a), _ptr(b), elems, _ptr(self.dist_parts),
+                         _ptr(self.loop_state), eps, damp, ctx.max_bp_iters_number, st)
+                launched += 1
+            ls = self.loop_state.cpu().numpy()
+            if ls[0]:
+                break
+            if launched >= ctx.max_bp_iters_number:
+                raise RuntimeError("BP loop state did not finish after the iteration cap")
+        if ls[2]:
+            self.mcur = 1 - self.mcur
+        if ls[3]:
+            best = np.array([ls[6]], dtype=np.int32).view(np.float32)[0]
+            log.warning(f"BP algorithm exceeds iterations limit set to {ctx.max_bp_iters_number}, "
+                        f"obtained bp_eps {best}")
+        return int(ls[1])
+
+    # ---- read-out ------------------------------------------------------------------------
+    def density_matrices(self) -> np.ndarray:
+        """(n, 2, 2) complex marginals (src/bqa/state.py:77-94)."""
+        self.lib.call("bqa_densities", self._class_array(), len(self.classes), self.chi,
+                      _ptr(self._msgs_cur()), _ptr(self.rho), self.stream)
+        return self.rho.view(-1, 2, 2).cpu().numpy().astype(np.complex128)
+
+    def bloch_vectors(self) -> np.ndarray:
+        rho = self.density_matrices()
+        x = (rho[:, 0, 1] + rho[:, 1, 0]).real
+        y = (rho[:, 1, 0] - rho[:, 0, 1]).imag
+        z = (rho[:, 0, 0] - rho[:, 1, 1]).real
+        return np.stack([x, y, z], axis=1)
+
+    def edge_zz(self) -> np.ndarray:
+        """BP two-site <Z_u Z_v> per undirected edge (oracle ``edge_zz``)."""
+        pm = self.lu   # scratch of the simple update, idle between steps
+        self.lib.call("bqa_psplit", self._class_array(), len(self.classes), self.chi, _ptr(self._msgs_cur()),
+                      _ptr(pm), self.stream)
+        self.lib.call("bqa_edge_zz", _ptr(pm), self.E, self.chi, _ptr(self.zz), self.stream)
+        return self.zz.cpu().numpy()
+
+    def energy(self, zz: np.ndarray | None = None, z: np.ndarray | None = None) -> float:
+        ctx = self.ctx
+        zz = self.edge_zz() if zz is None else zz
+        z = self.bloch_vectors()[:, 2] if z is None else z
+        return float(np.dot(ctx.edge_ampl, zz) + np.dot(ctx.node_ampl, z))
+
+    def spin_readout(self, z: np.ndarray | None = None) -> np.ndarray:
+        """Deterministic read-out sign(<Z_i>) -> +1 / -1 (z > 0 -> +1)."""
+        z = self.bloch_vectors()[:, 2] if z is None else z
+        return np.where(z > 0, 1, -1)
+
+    def spin_energy(self, spins: np.ndarray) -> float:
+        ctx = self.ctx
+        return float(np.dot(ctx.edge_ampl, spins[ctx.edge_src] * spins[ctx.edge_dst]) + np.dot(ctx.node_ampl, spins))
+
+    # ---- measurement -----------------------------------------------------------------------
+    def _project(self, nodes, outcomes) -> None:
+        """Project nodes onto outcomes (0: |0>, 1: |1>), then renormalise each touched class."""
+        ctx = self.ctx
+        nodes = np.asarray(nodes, dtype=np.int64)
+        outcomes = np.asarray(outcomes, dtype=np.int64)
+        deg = ctx.node_degree[nodes]
+        for i, c in enumerate(self.classes):
+            sel = deg == c.degree
+            if not np.any(sel):
+                continue
+            pos = self.torch.as_tensor(ctx.node_position[nodes[sel]].astype(np.int32), device=self.device)
+            out = self.torch.as_tensor(outcomes[sel].astype(np.int32), device=self.device)
+            self.lib.call("bqa_project_nodes", _ptr(c.tensors[self.tcur]), c.count, 2 * self.chi ** c.degree,
+                          _ptr(pos), _ptr(out), int(pos.numel()), _ptr(self.norm2), self.stream)
+
+    def measure(self) -> list:
+        """Sequential most-polarised-first sampling (src/bqa/state.py:250-312) with the same
+        host generator (numpy default_rng(seed).uniform) and the same order of draws."""
+        ctx = self.ctx
+        n = ctx.nodes_number
+        thr = ctx.measurement_threshold
+        result = np.zeros(n, dtype=np.int64)
+        measured = np.zeros(n, dtype=bool)
+        while not measured.all():
+            probs = self.density_matrices()[:, 0, 0].real
+            free = np.flatnonzero(~measured)
+            node = int(free[np.argmax(np.abs(2.0 * probs[free] - 1.0))])
+            prob = float(probs[node])
+            outcome = 0 if prob > self.rng.uniform(0.0, 1.0) else 1
+            self._project([node], [outcome])
+            measured[node] = True
+            result[node] = 1 - 2 * outcome
+            self.run_bp()
+            probs = self.density_matrices()[:, 0, 0].real
+            free = np.flatnonzero(~measured)
+            up = free[probs[free] > thr]
+            down = free[probs[free] < 1.0 - thr]
+            batch = np.concatenate([up, down])
+            if batch.size:
+                self._project(batch, np.concatenate([np.zeros(up.size, np.int64), np.ones(down.size, np.int64)]))
+                measured[batch] = True
+                result[up] = 1
+                result[down] = -1
+            self.run_bp()
+        log.info("Measurement outcomes sampling completed")
+        return [int(x) for x in result]

@@ -1,0 +1,179 @@
+"""Kernel-level parity of the CUDA path against the FP64 oracle, on identical seeded inputs.
+
+Each test loads one random state (complex tensors at a fixed bond dim, random PSD
+trace-normalised messages) into the device engine, runs one C-ABI entry point and compares
+with the oracle function the kernel restates.  Tolerances are for complex64 arithmetic:
+deterministic outputs (messages, extended messages, updated tensors, densities) to 2e-5
+relative to their largest entry; gauge-dependent outputs only through gauge-invariant
+combinations.
+"""
+import numpy as np
+import pytest
+
+from tests import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from bqa_gb300 import _lib  # noqa: E402
+from bqa_gb300.engine import Annealer, _ptr  # noqa: E402
+from bqa_gb300.layout import build_context  # noqa: E402
+from oracle import bqa_oracle as orc  # noqa: E402
+
+CASES = [("rr3_n16_chi4", 4), ("rr3_n24_chi8", 8), ("mixed_n18_chi3", 3), ("rr4_n20_chi4", 4),
+         ("rr3_n16_chi4", 16), ("grid3x4_chi4_damped", 5), ("tree9", 2)]
+RTOL = 2e-5
+
+
+def random_state(name, chi, seed=0):
+    conf = gc.config(name)
+    conf["max_bond_dim"] = chi
+    octx = orc.make_context(conf)
+    rng = np.random.default_rng(seed)
+    tens = {}
+    for d, L in octx.degree_to_layout.items():
+        shape = (L.node_ids.shape[0], 2) + (chi,) * d
+        t = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        t /= np.linalg.norm(t.reshape(shape[0], -1), axis=1).reshape((-1,) + (1,) * (t.ndim - 1))
+        tens[d] = t
+    a = rng.normal(size=(octx.edges_number, chi, chi)) + 1j * rng.normal(size=(octx.edges_number, chi, chi))
+    m = a @ np.conj(np.swapaxes(a, 1, 2)) + 0.1 * np.eye(chi)
+    m /= np.trace(m, axis1=1, axis2=2)[:, None, None]
+    lam = np.sort(rng.uniform(0.05, 1.0, size=(octx.edges_number // 2, chi)), axis=1)[:, ::-1]
+    lam /= np.linalg.norm(lam, axis=1, keepdims=True)
+    # round to complex64 so both sides see the same inputs
+    tens = {d: t.astype(np.complex64).astype(np.complex128) for d, t in tens.items()}
+    m = m.astype(np.complex64).astype(np.complex128)
+    st = orc.OracleState(np.random.default_rng(0), tens, m, lam.astype(np.complex128))
+    job = Annealer(build_context(conf))
+    job.set_state(tens, m, lam)
+    return octx, st, job
+
+
+def rel_err(got, want):
+    return float(np.abs(got - want).max() / max(np.abs(want).max(), 1e-30))
+
+
+@pytest.mark.parametrize("name,chi", CASES)
+def test_bp_sweep_matches_oracle(name, chi):
+    octx, st, job = random_state(name, chi)
+    want = np.empty_like(st.msgs)
+    for d, t in st.degree_to_tensor.items():
+        L = octx.degree_to_layout[d]
+        for mm, p in zip(orc.pass_msgs(t, [st.msgs[p] for p in L.input_msgs_position]), L.output_msgs_position):
+            want[p] = mm
+    job.dist_parts.zero_()
+    job.lib.call("bqa_bp_sweep", job._class_array(), len(job.classes), chi, _ptr(job.msgs[0]), _ptr(job.msgs[1]),
+                 _ptr(job.dist_parts), None, job.stream)
+    got = job.msgs[1][: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, want) < RTOL
+    num, den = job.dist_parts.view(torch.float32).cpu().numpy()
+    d_want = orc.get_dist(want, st.msgs)
+    assert abs(np.sqrt(num) / np.sqrt(den) - d_want) < 1e-5 * max(1.0, d_want)
+
+
+@pytest.mark.parametrize("name,chi", CASES)
+def test_ext_msgs_match_oracle(name, chi):
+    octx, st, job = random_state(name, chi, seed=1)
+    ztime = 0.37
+    want = orc.get_extended_msgs(octx, ztime, st)
+    job.lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, _ptr(job.msgs[0]), _ptr(job.ext),
+                 ztime, job.stream)
+    got = job.ext[: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, want) < RTOL
+
+
+@pytest.mark.parametrize("name,chi", CASES)
+def test_canonicalisers_match_oracle(name, chi):
+    octx, st, job = random_state(name, chi, seed=2)
+    ext = orc.get_extended_msgs(octx, 0.21, st).astype(np.complex64).astype(np.complex128)
+    eps = octx.pinv_eps
+    lam_w, can_w = orc.get_canonicalizers(ext, eps)
+    E, n = ext.shape[0], ext.shape[1]
+    job.ext[: ext.size].copy_(torch.from_numpy(ext.astype(np.complex64).reshape(-1)))
+    job.status.zero_()
+    job.colmax.zero_()
+    job.lib.call("bqa_env_factor", _ptr(job.ext), E, n, eps, _ptr(job.lu), _ptr(job.ul), _ptr(job.status), job.stream)
+    job.lib.call("bqa_bond_canon", _ptr(job.lu), _ptr(job.ul), E, n, eps, _ptr(job.ext), _ptr(job.lmbds),
+                 _ptr(job.colmax), _ptr(job.status), job.stream)
+    assert int(job.status.item()) == 0
+    lam = job.lmbds[: E // 2 * n].cpu().numpy().reshape(E // 2, n)
+    can = job.ext[: E * n * n].cpu().numpy().reshape(E, n, n)
+    big = lam_w.real > 1e-3
+    assert np.abs(lam - lam_w.real)[big].max() < 2e-5
+    colmax = job.colmax[:n].view(torch.float32).cpu().numpy()
+    assert np.allclose(colmax, lam.max(axis=0))
+    # gauge-invariant bond operator  can[p+h] diag(lam) can[p]^T  (= P_fwd P_bwd^T, projectors)
+    h = E // 2
+    keep = (lam_w.real > 1e-3).astype(float)
+    g_w = np.einsum("pic,pc,pjc->pij", can_w[h:], lam_w.real * keep, can_w[:h])
+    g = np.einsum("pic,pc,pjc->pij", can[h:], lam * keep, can[:h])
+    assert rel_err(g, g_w) < 5e-4
+
+
+@pytest.mark.parametrize("name,chi,dim", [("rr3_n16_chi4", 2, 4), ("rr3_n24_chi8", 8, 8), ("mixed_n18_chi3", 3, 5),
+                                          ("rr4_n20_chi4", 4, 3), ("rr3_n16_chi4", 16, 16)])
+def test_apply_update_matches_oracle(name, chi, dim):
+    octx, st, job = random_state(name, max(chi, dim), seed=3)
+    # re-draw a state at bond chi, and canonicalisers with n = 2 chi, dim columns
+    rng = np.random.default_rng(4)
+    tens = {}
+    for d, L in octx.degree_to_layout.items():
+        shape = (L.node_ids.shape[0], 2) + (chi,) * d
+        tens[d] = (rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(np.complex64).astype(np.complex128)
+    E, n = octx.edges_number, 2 * chi
+    can = (rng.normal(size=(E, n, n)) + 1j * rng.normal(size=(E, n, n))).astype(np.complex64).astype(np.complex128)
+    lam = np.sort(rng.uniform(0.05, 1.0, size=(E // 2, n)), axis=1)[:, ::-1].astype(np.float32)
+    ztime, xtime = 0.13, 0.41
+    ost = orc.OracleState(np.random.default_rng(0), {d: t.copy() for d, t in tens.items()},
+                          np.zeros((E, dim, dim), complex), lam[:, :dim].astype(np.complex128))
+    for d, L in octx.degree_to_layout.items():
+        aligned = [can[p][:, :, :dim] for p in L.input_msgs_position]
+        ost.degree_to_tensor[d] = orc.apply_canonicalizers_with_extensions(
+            ost.degree_to_tensor[d], aligned, [a * ztime for a in L.edge_ampls])
+    orc.apply_z_layer(octx, ztime, ost)
+    orc.apply_x_layer(xtime, ost)
+    orc.set_to_symmetric_gauge(octx, ost)
+    job.set_state(tens, np.zeros((E, chi, chi), np.complex64))
+    job.ext[: can.size].copy_(torch.from_numpy(can.astype(np.complex64).reshape(-1)))
+    job.lmbds[: lam.size].copy_(torch.from_numpy(lam.reshape(-1)))
+    job.lib.call("bqa_apply_update", job._class_array(out=True), len(job.classes), chi, dim, _ptr(job.ext),
+                 _ptr(job.lmbds), n, ztime, xtime, job.stream)
+    job.tcur = 1
+    job.chi = dim
+    for c in job.classes:
+        shape = (c.count, 2) + (dim,) * c.degree
+        got = c.tensors[1][: int(np.prod(shape))].cpu().numpy().reshape(shape)
+        assert rel_err(got, ost.degree_to_tensor[c.degree]) < RTOL
+    job.lib.call("bqa_msgs_from_lmbds", _ptr(job.lmbds), n, E, dim, _ptr(job.msgs[0]), job.stream)
+    got_m = job.msgs[0][: E * dim * dim].cpu().numpy().reshape(E, dim, dim)
+    assert rel_err(got_m, ost.msgs) < 1e-6
+
+
+@pytest.mark.parametrize("name,chi", CASES)
+def test_densities_and_zz_match_oracle(name, chi):
+    octx, st, job = random_state(name, chi, seed=5)
+    rho_w = orc.get_density_matrices(octx, st)
+    rho = job.density_matrices()
+    assert np.abs(rho - rho_w).max() < 2e-5
+    zz_w = orc.edge_zz(octx, st)
+    assert np.abs(job.edge_zz() - zz_w).max() < 2e-5
+
+
+@pytest.mark.parametrize("name,chi", [("rr3_n16_chi4", 4), ("mixed_n18_chi3", 3), ("grid3x4_chi4_damped", 4)])
+def test_bp_loop_matches_oracle(name, chi):
+    octx, st, job = random_state(name, chi, seed=6)
+    octx.bp_eps = 1e-6
+    job.ctx.bp_eps = 1e-6
+    orc.run_bp(octx, st)
+    job.run_bp()
+    _, msgs, _ = job.get_state()
+    assert np.abs(msgs - st.msgs).max() < 2e-5
+
+
+def test_library_reports_limits():
+    lib = _lib.load()
+    assert lib.max_bond_dim(3) == 16
+    assert lib.max_bond_dim(4) == 8
+    assert lib.max_bond_dim(2) == 16
