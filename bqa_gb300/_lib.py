@@ -9,7 +9,9 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 1
+ABI_VERSION = 2
+BQA_C64 = 0
+BQA_C128 = 1
 
 BQA_OK = 0
 BQA_STATUS_SVD_NOT_CONVERGED = 1
@@ -35,20 +37,24 @@ class BqaClass(ctypes.Structure):
 SIGNATURES = {
     "bqa_abi_version": (c_int32, []),
     "bqa_last_error": (ctypes.c_char_p, []),
-    "bqa_max_bond_dim": (c_int32, [c_int32]),
-    "bqa_bp_sweep": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
-    "bqa_bp_finalize": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_float, c_float, c_int32, c_void_p]),
-    "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),
-    "bqa_env_factor": (c_int32, [c_void_p, c_int32, c_int32, c_float, c_void_p, c_void_p, c_void_p, c_void_p]),
-    "bqa_bond_canon": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_float, c_void_p, c_void_p, c_void_p,
-                                 c_void_p, c_void_p]),
-    "bqa_apply_update": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32,
+    "bqa_max_bond_dim": (c_int32, [c_int32, c_int32]),
+    "bqa_bp_sweep": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
+                               c_void_p]),
+    "bqa_bp_finalize": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_double, c_double,
+                                  c_int32, c_void_p]),
+    "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),
+    "bqa_env_factor": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p, c_void_p,
+                                 c_void_p]),
+    "bqa_bond_canon": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,
+                                 c_void_p, c_void_p, c_void_p]),
+    "bqa_apply_update": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32,
                                    c_double, c_double, c_void_p]),
-    "bqa_msgs_from_lmbds": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p]),
-    "bqa_densities": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
-    "bqa_psplit": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
-    "bqa_edge_zz": (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p]),
-    "bqa_project_nodes": (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p]),
+    "bqa_msgs_from_lmbds": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_densities": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    "bqa_psplit": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    "bqa_edge_zz": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_project_nodes": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p,
+                                    c_void_p]),
 }
 
 
@@ -79,8 +85,8 @@ class Library:
             msg = self.dll.bqa_last_error().decode(errors="replace")
             raise BqaError(f"{name} failed with status {rc}: {msg}")
 
-    def max_bond_dim(self, degree: int) -> int:
-        return int(self.dll.bqa_max_bond_dim(degree))
+    def max_bond_dim(self, degree: int, dtype: int = BQA_C64) -> int:
+        return int(self.dll.bqa_max_bond_dim(degree, dtype))
 
 
 _LIB: Library | None = None

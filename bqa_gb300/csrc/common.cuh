@@ -1,5 +1,6 @@
-// Shared device helpers of the GB300 annealing kernels: complex64 arithmetic on float2,
-// block/warp reductions, and the half-ZZ-gate bond coefficients.
+// Shared device helpers of the GB300 annealing kernels: complex arithmetic on float2
+// (complex64) and double2 (complex128), block/warp reductions, and the half-ZZ-gate bond
+// coefficients.  Kernels are templated on the real type R (float or double).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -11,62 +12,67 @@
 
 namespace bqa {
 
-// ---- complex64 on float2 -----------------------------------------------------------------
+template <typename R> struct Cx;
+template <> struct Cx<float> { using T = float2; using Bits = uint32_t; };
+template <> struct Cx<double> { using T = double2; using Bits = unsigned long long; };
 
-__device__ __forceinline__ float2 c_zero() { return make_float2(0.f, 0.f); }
-__device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-__device__ __forceinline__ float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
-__device__ __forceinline__ float c_abs2(float2 a) { return fmaf(a.x, a.x, a.y * a.y); }
+// ---- complex arithmetic ----------------------------------------------------------------------
 
-__device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
-    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+__device__ __forceinline__ float2 c_make(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ double2 c_make(double x, double y) { return make_double2(x, y); }
+
+template <typename C> __device__ __forceinline__ C c_zero();
+template <> __device__ __forceinline__ float2 c_zero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double2 c_zero<double2>() { return make_double2(0.0, 0.0); }
+
+template <typename C> __device__ __forceinline__ C c_add(C a, C b) { return c_make(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C c_sub(C a, C b) { return c_make(a.x - b.x, a.y - b.y); }
+template <typename C, typename R> __device__ __forceinline__ C c_scale(C a, R s) { return c_make(a.x * s, a.y * s); }
+template <typename C> __device__ __forceinline__ C c_conj(C a) { return c_make(a.x, -a.y); }
+template <typename C> __device__ __forceinline__ auto c_abs2(C a) -> decltype(a.x) { return fma(a.x, a.x, a.y * a.y); }
+
+template <typename C> __device__ __forceinline__ C c_mul(C a, C b) {
+    return c_make(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 // acc + a*b
-__device__ __forceinline__ float2 c_fma(float2 a, float2 b, float2 acc) {
-    acc.x = fmaf(a.x, b.x, acc.x);
-    acc.x = fmaf(-a.y, b.y, acc.x);
-    acc.y = fmaf(a.x, b.y, acc.y);
-    acc.y = fmaf(a.y, b.x, acc.y);
+template <typename C> __device__ __forceinline__ C c_fma(C a, C b, C acc) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
     return acc;
 }
 // acc + conj(a)*b
-__device__ __forceinline__ float2 c_fma_conj(float2 a, float2 b, float2 acc) {
-    acc.x = fmaf(a.x, b.x, acc.x);
-    acc.x = fmaf(a.y, b.y, acc.x);
-    acc.y = fmaf(a.x, b.y, acc.y);
-    acc.y = fmaf(-a.y, b.x, acc.y);
+template <typename C> __device__ __forceinline__ C c_fma_conj(C a, C b, C acc) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
     return acc;
 }
 // a / b
-__device__ __forceinline__ float2 c_div(float2 a, float2 b) {
-    const float inv = 1.0f / c_abs2(b);
-    return make_float2((a.x * b.x + a.y * b.y) * inv, (a.y * b.x - a.x * b.y) * inv);
+template <typename C> __device__ __forceinline__ C c_div(C a, C b) {
+    const auto inv = decltype(a.x)(1) / c_abs2(b);
+    return c_make((a.x * b.x + a.y * b.y) * inv, (a.y * b.x - a.x * b.y) * inv);
 }
 
 // ---- reductions ----------------------------------------------------------------------------
 
-__device__ __forceinline__ float warp_max(float v) {
+template <typename R> __device__ __forceinline__ R warp_max(R v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(BQA_FULL_MASK, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(BQA_FULL_MASK, v, o));
     return v;
 }
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(BQA_FULL_MASK, v, o);
-    return v;
-}
-__device__ __forceinline__ double warp_sum_d(double v) {
+template <typename R> __device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(BQA_FULL_MASK, v, o);
     return v;
 }
 
-// Block-wide sum of `cnt` floats per thread (cnt <= 8); every thread gets the totals.
-// `scratch` needs cnt * 32 floats of shared memory.  Must be called by the whole block.
-template <int CNT>
-__device__ __forceinline__ void block_sum(float (&v)[CNT], float* scratch) {
+// Block-wide sum of CNT values per thread; every thread gets the totals.  `scratch` needs
+// CNT * 32 values of shared memory.  Must be called by the whole block.
+template <int CNT, typename R>
+__device__ __forceinline__ void block_sum(R (&v)[CNT], R* scratch) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
     for (int c = 0; c < CNT; ++c) v[c] = warp_sum(v[c]);
@@ -78,28 +84,34 @@ __device__ __forceinline__ void block_sum(float (&v)[CNT], float* scratch) {
     __syncthreads();
 #pragma unroll
     for (int c = 0; c < CNT; ++c) {
-        float t = lane < nw ? scratch[c * 32 + lane] : 0.f;
+        R t = lane < nw ? scratch[c * 32 + lane] : R(0);
         v[c] = warp_sum(t);
     }
     __syncthreads();
 }
 
-__device__ __forceinline__ float block_max(float v, float* scratch) {
+template <typename R>
+__device__ __forceinline__ R block_max(R v, R* scratch) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     v = warp_max(v);
     __syncthreads();
     if (lane == 0) scratch[warp] = v;
     __syncthreads();
-    float t = lane < nw ? scratch[lane] : 0.f;
+    R t = lane < nw ? scratch[lane] : R(0);
     v = warp_max(t);
     __syncthreads();
     return v;
 }
 
-// max of non-negative floats through their bit patterns (monotone for x >= 0)
+// max of non-negative reals through their bit patterns (monotone for x >= 0)
 __device__ __forceinline__ void atomic_max_nonneg(uint32_t* addr, float v) {
     atomicMax(addr, __float_as_uint(fmaxf(v, 0.f)));
 }
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+    atomicMax(addr, (unsigned long long)__double_as_longlong(fmax(v, 0.0)));
+}
+__device__ __forceinline__ float bits_to_real(uint32_t b) { return __uint_as_float(b); }
+__device__ __forceinline__ double bits_to_real(unsigned long long b) { return __longlong_as_double((long long)b); }
 
 // ---- half of exp(-i c Z Z) on one bond -------------------------------------------------------
 // The bond of a node is doubled to (e, j), e in {0,1}: block e = 0 carries a0 * I and block
@@ -107,12 +119,14 @@ __device__ __forceinline__ void atomic_max_nonneg(uint32_t* addr, float v) {
 // so a0^2 = cos c and a1^2 = -i sin c (src/bqa/backends.py:20-22,519-526).  The square roots
 // are numpy's principal complex square roots of the complex-typed cos/sin, whose zero
 // imaginary part carries a sign (-sin(c)*0 for cos, cos(c)*0 for sin); that sign picks the
-// branch for a negative argument.  Computed in double, rounded once.
+// branch for a negative argument.  Computed in double, rounded once to R.
+template <typename R>
 struct HalfZZ {
-    float2 a0, a1;
+    typename Cx<R>::T a0, a1;
 };
 
-__device__ __forceinline__ HalfZZ half_zz(double c) {
+template <typename R>
+__device__ __forceinline__ HalfZZ<R> half_zz(double c) {
     double sc, cc;
     sincos(c, &sc, &cc);
     double r0, i0, r1, i1;
@@ -122,9 +136,9 @@ __device__ __forceinline__ HalfZZ half_zz(double c) {
     else { r1 = 0.0; i1 = (cc >= 0.0) ? sqrt(-sc) : -sqrt(-sc); }
     // a1 = (1 - i)/sqrt(2) * (r1 + i i1)
     const double h = 0.70710678118654752440;
-    HalfZZ out;
-    out.a0 = make_float2((float)r0, (float)i0);
-    out.a1 = make_float2((float)(h * (r1 + i1)), (float)(h * (i1 - r1)));
+    HalfZZ<R> out;
+    out.a0 = c_make((R)r0, (R)i0);
+    out.a1 = c_make((R)(h * (r1 + i1)), (R)(h * (i1 - r1)));
     return out;
 }
 

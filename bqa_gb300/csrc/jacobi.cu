@@ -19,66 +19,72 @@ namespace bqa {
 
 constexpr int kMaxSweeps = 40;
 
-template <int W>
-__device__ __forceinline__ bool jacobi_columns(float2 (&a)[W], float2 (&v)[W], int lane) {
-    const float tol = (float)W * 1.2e-7f;
-    bool any_rot = true;
+template <typename R> __device__ __forceinline__ R jacobi_eps();
+template <> __device__ __forceinline__ float jacobi_eps<float>() { return 1.2e-7f; }
+template <> __device__ __forceinline__ double jacobi_eps<double>() { return 2.3e-16; }
+
+template <typename C>
+__device__ __forceinline__ C shfl_xor_c(C v, int r, int w) {
+    v.x = __shfl_xor_sync(BQA_FULL_MASK, v.x, r, w);
+    v.y = __shfl_xor_sync(BQA_FULL_MASK, v.y, r, w);
+    return v;
+}
+
+template <int W, typename R>
+__device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typename Cx<R>::T (&v)[W], int lane) {
+    using C = typename Cx<R>::T;
+    const R tol = (R)W * jacobi_eps<R>();
+    const R tiny = sizeof(R) == 4 ? R(1e-30) : R(1e-280);
     for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
         int rotated = 0;
 #pragma unroll 1
         for (int r = 1; r < W; ++r) {
             const bool low = lane < (lane ^ r);
-            float2 o[W];
-            float alpha = 0.f, beta = 0.f;
-            float2 g = c_zero();
+            R alpha = 0, beta = 0;
+            C g = c_zero<C>();
 #pragma unroll
             for (int i = 0; i < W; ++i) {
-                o[i].x = __shfl_xor_sync(BQA_FULL_MASK, a[i].x, r, W);
-                o[i].y = __shfl_xor_sync(BQA_FULL_MASK, a[i].y, r, W);
-                const float2 p = low ? a[i] : o[i];
-                const float2 q = low ? o[i] : a[i];
-                alpha = fmaf(p.x, p.x, fmaf(p.y, p.y, alpha));
-                beta = fmaf(q.x, q.x, fmaf(q.y, q.y, beta));
+                const C o = shfl_xor_c(a[i], r, W);
+                const C p = low ? a[i] : o;
+                const C q = low ? o : a[i];
+                alpha = fma(p.x, p.x, fma(p.y, p.y, alpha));
+                beta = fma(q.x, q.x, fma(q.y, q.y, beta));
                 g = c_fma_conj(p, q, g);
             }
-            const float gabs = sqrtf(c_abs2(g));
-            const bool rot = alpha > 1e-30f && beta > 1e-30f && gabs > tol * sqrtf(alpha) * sqrtf(beta);
-            float c = 1.f, s = 0.f;
-            float2 eb = make_float2(1.f, 0.f);  // conj(e)
+            const R gabs = sqrt(c_abs2(g));
+            const bool rot = alpha > tiny && beta > tiny && gabs > tol * sqrt(alpha) * sqrt(beta);
+            R c = 1, s = 0;
+            C eb = c_make(R(1), R(0));  // conj(e)
             if (rot) {
-                const float zeta = (beta - alpha) / (2.f * gabs);
-                const float t = copysignf(1.f, zeta) / (fabsf(zeta) + hypotf(1.f, zeta));
-                c = rsqrtf(fmaf(t, t, 1.f));
+                const R zeta = (beta - alpha) / (R(2) * gabs);
+                const R t = copysign(R(1), zeta) / (fabs(zeta) + hypot(R(1), zeta));
+                c = R(1) / sqrt(fma(t, t, R(1)));
                 s = c * t;
-                eb = make_float2(g.x / gabs, -g.y / gabs);
+                eb = c_make(g.x / gabs, -g.y / gabs);
                 rotated = 1;
             }
 #pragma unroll
             for (int i = 0; i < W; ++i) {
-                const float2 p = low ? a[i] : o[i];
-                const float2 q = c_mul(eb, low ? o[i] : a[i]);
-                a[i] = low ? make_float2(c * p.x - s * q.x, c * p.y - s * q.y)
-                           : make_float2(s * p.x + c * q.x, s * p.y + c * q.y);
+                const C o = shfl_xor_c(a[i], r, W);
+                const C p = low ? a[i] : o;
+                const C q = c_mul(eb, low ? o : a[i]);
+                a[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
             }
 #pragma unroll
             for (int i = 0; i < W; ++i) {
-                float2 ov;
-                ov.x = __shfl_xor_sync(BQA_FULL_MASK, v[i].x, r, W);
-                ov.y = __shfl_xor_sync(BQA_FULL_MASK, v[i].y, r, W);
-                const float2 p = low ? v[i] : ov;
-                const float2 q = c_mul(eb, low ? ov : v[i]);
-                v[i] = low ? make_float2(c * p.x - s * q.x, c * p.y - s * q.y)
-                           : make_float2(s * p.x + c * q.x, s * p.y + c * q.y);
+                const C o = shfl_xor_c(v[i], r, W);
+                const C p = low ? v[i] : o;
+                const C q = c_mul(eb, low ? o : v[i]);
+                v[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
             }
         }
-        any_rot = __any_sync(BQA_FULL_MASK, rotated) != 0;
-        if (!any_rot) return true;
+        if (!__any_sync(BQA_FULL_MASK, rotated)) return true;
     }
     return false;
 }
 
-template <int W>
-__device__ __forceinline__ float seg_sum(float x) {
+template <int W, typename R>
+__device__ __forceinline__ R seg_sum(R x) {
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) x += __shfl_xor_sync(BQA_FULL_MASK, x, o, W);
     return x;
@@ -86,36 +92,37 @@ __device__ __forceinline__ float seg_sum(float x) {
 
 // m = U S Vh per matrix (masked at eps) -> lu = sqrt(S) Vh, ul = U pinv(sqrt(S))
 // (src/bqa/backends.py:483-490,709-727).
-template <int W>
-__global__ void __launch_bounds__(128) env_factor_kernel(const float2* __restrict__ mats, int count, int n,
-                                                         float eps, float2* __restrict__ lu,
-                                                         float2* __restrict__ ul, int32_t* status) {
+template <int W, typename R>
+__global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
+                                                         R eps, typename Cx<R>::T* __restrict__ lu,
+                                                         typename Cx<R>::T* __restrict__ ul, int32_t* status) {
+    using C = typename Cx<R>::T;
     const int lane = threadIdx.x & (W - 1);
     const int mat = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = mat < count;
     const size_t base = (size_t)(live ? mat : 0) * n * n;
-    float2 a[W], v[W];
+    C a[W], v[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) {
-        a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero();
-        v[i] = make_float2(i == lane ? 1.f : 0.f, 0.f);
+        a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
+        v[i] = c_make(i == lane ? R(1) : R(0), R(0));
     }
-    const bool ok = jacobi_columns<W>(a, v, lane);
+    const bool ok = jacobi_columns<W, R>(a, v, lane);
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
-    float nrm2 = 0.f;
+    R nrm2 = 0;
 #pragma unroll
     for (int i = 0; i < W; ++i) nrm2 += c_abs2(a[i]);
-    const float sig = sqrtf(nrm2);
+    const R sig = sqrt(nrm2);
     const bool keep = sig > eps;
-    const float sq = sqrtf(sig);
+    const R sq = sqrt(sig);
     if (!live || lane >= n) return;
     // row `lane` of lu = sqrt(sigma) * conj(v)^T ; column `lane` of ul = a / (sigma sqrt(sigma))
-    const float inv = keep ? 1.f / (sig * sq) : 0.f;
-    const float sqk = keep ? sq : 0.f;
+    const R inv = keep ? R(1) / (sig * sq) : R(0);
+    const R sqk = keep ? sq : R(0);
 #pragma unroll
     for (int k = 0; k < W; ++k) {
         if (k < n) {
-            lu[base + (size_t)lane * n + k] = make_float2(sqk * v[k].x, -sqk * v[k].y);
+            lu[base + (size_t)lane * n + k] = c_make(sqk * v[k].x, -sqk * v[k].y);
             ul[base + (size_t)k * n + lane] = c_scale(a[k], inv);
         }
     }
@@ -123,66 +130,71 @@ __global__ void __launch_bounds__(128) env_factor_kernel(const float2* __restric
 
 // Per undirected edge p: ker = lu[p] lu[p+h]^T = us s vhs; lambdas; canonicalisers
 // (src/bqa/state.py:171-200).
-template <int W>
-__global__ void __launch_bounds__(128) bond_canon_kernel(const float2* __restrict__ lu, const float2* __restrict__ ul,
-                                                         int edges, int n, float eps, float2* __restrict__ canon,
-                                                         float* __restrict__ lmbds, uint32_t* colmax,
+template <int W, typename R>
+__global__ void __launch_bounds__(128) bond_canon_kernel(const typename Cx<R>::T* __restrict__ lu,
+                                                         const typename Cx<R>::T* __restrict__ ul, int edges, int n,
+                                                         R eps, typename Cx<R>::T* __restrict__ canon,
+                                                         R* __restrict__ lmbds, typename Cx<R>::Bits* colmax,
                                                          int32_t* status) {
-    extern __shared__ float4 smem_raw[];
+    using C = typename Cx<R>::T;
+    extern __shared__ double4 smem_raw[];
     const int lane = threadIdx.x & (W - 1);
     const int seg = threadIdx.x / W;
-    float2* sm = reinterpret_cast<float2*>(smem_raw) + (size_t)seg * W * W;
+    C* sm = reinterpret_cast<C*>(smem_raw) + (size_t)seg * W * W;
     const int half = edges / 2;
     const int p = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = p < half;
     const int pf = live ? p : 0, pb = pf + half;
     const size_t nn = (size_t)n * n;
     // stage lu_f, then ker[:, lane] = lu_f . lu_b[lane, :]^T
-    for (int i = lane; i < n * n; i += W) sm[i] = live ? lu[(size_t)pf * nn + i] : c_zero();
+    for (int i = lane; i < n * n; i += W) sm[i] = live ? lu[(size_t)pf * nn + i] : c_zero<C>();
     __syncwarp();
-    float2 brow[W];
+    C a[W], v[W];
+    {
+        C brow[W];
 #pragma unroll
-    for (int k = 0; k < W; ++k) brow[k] = (live && lane < n && k < n) ? lu[(size_t)pb * nn + (size_t)lane * n + k] : c_zero();
-    float2 a[W], v[W];
+        for (int k = 0; k < W; ++k)
+            brow[k] = (live && lane < n && k < n) ? lu[(size_t)pb * nn + (size_t)lane * n + k] : c_zero<C>();
 #pragma unroll
-    for (int i = 0; i < W; ++i) {
-        float2 acc = c_zero();
-        if (i < n) {
+        for (int i = 0; i < W; ++i) {
+            C acc = c_zero<C>();
+            if (i < n) {
 #pragma unroll
-            for (int k = 0; k < W; ++k)
-                if (k < n) acc = c_fma(sm[i * n + k], brow[k], acc);
+                for (int k = 0; k < W; ++k)
+                    if (k < n) acc = c_fma(sm[i * n + k], brow[k], acc);
+            }
+            a[i] = acc;
+            v[i] = c_make(i == lane ? R(1) : R(0), R(0));
         }
-        a[i] = acc;
-        v[i] = make_float2(i == lane ? 1.f : 0.f, 0.f);
     }
-    const bool ok = jacobi_columns<W>(a, v, lane);
+    const bool ok = jacobi_columns<W, R>(a, v, lane);
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
-    float nrm2 = 0.f;
+    R nrm2 = 0;
 #pragma unroll
     for (int i = 0; i < W; ++i) nrm2 += c_abs2(a[i]);
-    const float sig = sqrtf(nrm2);
-    const float sk = (lane < n && sig > eps) ? sig : 0.f;
+    const R sig = sqrt(nrm2);
+    const R sk = (lane < n && sig > eps) ? sig : R(0);
     // descending rank among the segment's columns, ties by column index
     int rank = 0;
 #pragma unroll
     for (int k = 0; k < W; ++k) {
-        const float o = __shfl_sync(BQA_FULL_MASK, sk, k, W);
+        const R o = __shfl_sync(BQA_FULL_MASK, sk, k, W);
         rank += (o > sk) || (o == sk && k < lane);
     }
-    const float norm = sqrtf(seg_sum<W>(sk * sk));
+    const R norm = sqrt(seg_sum<W>(sk * sk));
     if (live && lane < n) {
-        lmbds[(size_t)pf * n + rank] = norm > 0.f ? sk / norm : 0.f;
-        if (norm > 0.f) atomic_max_nonneg(colmax + rank, sk / norm);
+        lmbds[(size_t)pf * n + rank] = norm > R(0) ? sk / norm : R(0);
+        if (norm > R(0)) atomic_max_nonneg(colmax + rank, sk / norm);
     }
-    const float uinv = sk > 0.f ? 1.f / sig : 0.f;
+    const R uinv = sk > R(0) ? R(1) / sig : R(0);
     // fwd canonicaliser column rank: ul[p] . (a / sigma) -> canon[p + half]
     __syncwarp();
-    for (int i = lane; i < n * n; i += W) sm[i] = live ? ul[(size_t)pf * nn + i] : c_zero();
+    for (int i = lane; i < n * n; i += W) sm[i] = live ? ul[(size_t)pf * nn + i] : c_zero<C>();
     __syncwarp();
     if (live && lane < n) {
-        float2* out = canon + (size_t)pb * nn + rank;
+        C* out = canon + (size_t)pb * nn + rank;
         for (int i = 0; i < n; ++i) {
-            float2 acc = c_zero();
+            C acc = c_zero<C>();
 #pragma unroll
             for (int k = 0; k < W; ++k)
                 if (k < n) acc = c_fma(sm[i * n + k], a[k], acc);
@@ -191,13 +203,13 @@ __global__ void __launch_bounds__(128) bond_canon_kernel(const float2* __restric
     }
     // bwd canonicaliser column rank: ul[p + half] . conj(v)  (vs = vhs^T) -> canon[p]
     __syncwarp();
-    for (int i = lane; i < n * n; i += W) sm[i] = live ? ul[(size_t)pb * nn + i] : c_zero();
+    for (int i = lane; i < n * n; i += W) sm[i] = live ? ul[(size_t)pb * nn + i] : c_zero<C>();
     __syncwarp();
     if (live && lane < n) {
-        const float keep = sk > 0.f ? 1.f : 0.f;
-        float2* out = canon + (size_t)pf * nn + rank;
+        const R keep = sk > R(0) ? R(1) : R(0);
+        C* out = canon + (size_t)pf * nn + rank;
         for (int i = 0; i < n; ++i) {
-            float2 acc = c_zero();
+            C acc = c_zero<C>();
 #pragma unroll
             for (int k = 0; k < W; ++k)
                 if (k < n) acc = c_fma(sm[i * n + k], c_conj(v[k]), acc);
@@ -206,26 +218,48 @@ __global__ void __launch_bounds__(128) bond_canon_kernel(const float2* __restric
     }
 }
 
-template <int W>
-static int launch_env(const float2* m, int count, int n, float eps, float2* lu, float2* ul, int32_t* status,
-                      cudaStream_t st) {
+template <int W, typename R>
+static int launch_env(const void* m, int count, int n, double eps, void* lu, void* ul, int32_t* status, cudaStream_t st) {
+    using C = typename Cx<R>::T;
     const int per_block = 128 / W;
     const int blocks = (count + per_block - 1) / per_block;
-    env_factor_kernel<W><<<blocks, 128, 0, st>>>(m, count, n, eps, lu, ul, status);
+    env_factor_kernel<W, R><<<blocks, 128, 0, st>>>(static_cast<const C*>(m), count, n, (R)eps, static_cast<C*>(lu),
+                                                    static_cast<C*>(ul), status);
     return check_launch("env_factor");
 }
 
-template <int W>
-static int launch_canon(const float2* lu, const float2* ul, int edges, int n, float eps, float2* canon,
-                        float* lmbds, uint32_t* colmax, int32_t* status, cudaStream_t st) {
+template <int W, typename R>
+static int launch_canon(const void* lu, const void* ul, int edges, int n, double eps, void* canon, void* lmbds,
+                        void* colmax, int32_t* status, cudaStream_t st) {
+    using C = typename Cx<R>::T;
     const int per_block = 128 / W;
     const int half = edges / 2;
     const int blocks = (half + per_block - 1) / per_block;
-    const size_t smem = (size_t)128 * W * sizeof(float2);
-    int rc = ensure_smem((const void*)bond_canon_kernel<W>, smem, "bond_canon");
+    const size_t smem = (size_t)128 * W * sizeof(C);
+    int rc = ensure_smem((const void*)bond_canon_kernel<W, R>, smem, "bond_canon");
     if (rc) return rc;
-    bond_canon_kernel<W><<<blocks, 128, smem, st>>>(lu, ul, edges, n, eps, canon, lmbds, colmax, status);
+    bond_canon_kernel<W, R><<<blocks, 128, smem, st>>>(static_cast<const C*>(lu), static_cast<const C*>(ul), edges, n,
+                                                       (R)eps, static_cast<C*>(canon), static_cast<R*>(lmbds),
+                                                       static_cast<typename Cx<R>::Bits*>(colmax), status);
     return check_launch("bond_canon");
+}
+
+template <typename R>
+static int env_dispatch(const void* m, int count, int n, double eps, void* lu, void* ul, int32_t* status,
+                        cudaStream_t st) {
+    if (n <= 8) return launch_env<8, R>(m, count, n, eps, lu, ul, status, st);
+    if (n <= 16) return launch_env<16, R>(m, count, n, eps, lu, ul, status, st);
+    if (n <= 32) return launch_env<32, R>(m, count, n, eps, lu, ul, status, st);
+    return set_error(BQA_ERR_UNSUPPORTED, "bqa_env_factor: matrix size %d > 32", n);
+}
+
+template <typename R>
+static int canon_dispatch(const void* lu, const void* ul, int edges, int n, double eps, void* canon, void* lmbds,
+                          void* colmax, int32_t* status, cudaStream_t st) {
+    if (n <= 8) return launch_canon<8, R>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    if (n <= 16) return launch_canon<16, R>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    if (n <= 32) return launch_canon<32, R>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    return set_error(BQA_ERR_UNSUPPORTED, "bqa_bond_canon: matrix size %d > 32", n);
 }
 
 }  // namespace bqa
@@ -234,32 +268,24 @@ using namespace bqa;
 
 extern "C" {
 
-int32_t bqa_env_factor(const void* mats, int32_t count, int32_t n, float eps, void* lu, void* ul, int32_t* status,
-                       void* stream) {
+int32_t bqa_env_factor(const void* mats, int32_t count, int32_t n, int32_t dtype, double eps, void* lu, void* ul,
+                       int32_t* status, void* stream) {
     if (!mats || !lu || !ul || !status || count < 0 || n < 1) return set_error(BQA_ERR_ARG, "bqa_env_factor: bad argument");
     if (count == 0) return BQA_OK;
-    auto m = static_cast<const float2*>(mats);
-    auto l = static_cast<float2*>(lu);
-    auto u = static_cast<float2*>(ul);
     cudaStream_t st = as_stream(stream);
-    if (n <= 8) return launch_env<8>(m, count, n, eps, l, u, status, st);
-    if (n <= 16) return launch_env<16>(m, count, n, eps, l, u, status, st);
-    if (n <= 32) return launch_env<32>(m, count, n, eps, l, u, status, st);
-    return set_error(BQA_ERR_UNSUPPORTED, "bqa_env_factor: matrix size %d > 32", n);
+    if (dtype == BQA_C64) return env_dispatch<float>(mats, count, n, eps, lu, ul, status, st);
+    if (dtype == BQA_C128) return env_dispatch<double>(mats, count, n, eps, lu, ul, status, st);
+    return set_error(BQA_ERR_ARG, "bqa_env_factor: unknown dtype %d", dtype);
 }
 
-int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n, float eps, void* canon,
-                       float* lmbds, uint32_t* colmax, int32_t* status, void* stream) {
+int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n, int32_t dtype, double eps, void* canon,
+                       void* lmbds, void* colmax, int32_t* status, void* stream) {
     if (!lu || !ul || !canon || !lmbds || !colmax || !status || edges < 2 || n < 1)
         return set_error(BQA_ERR_ARG, "bqa_bond_canon: bad argument");
-    auto l = static_cast<const float2*>(lu);
-    auto u = static_cast<const float2*>(ul);
-    auto c = static_cast<float2*>(canon);
     cudaStream_t st = as_stream(stream);
-    if (n <= 8) return launch_canon<8>(l, u, edges, n, eps, c, lmbds, colmax, status, st);
-    if (n <= 16) return launch_canon<16>(l, u, edges, n, eps, c, lmbds, colmax, status, st);
-    if (n <= 32) return launch_canon<32>(l, u, edges, n, eps, c, lmbds, colmax, status, st);
-    return set_error(BQA_ERR_UNSUPPORTED, "bqa_bond_canon: matrix size %d > 32", n);
+    if (dtype == BQA_C64) return canon_dispatch<float>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    if (dtype == BQA_C128) return canon_dispatch<double>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    return set_error(BQA_ERR_ARG, "bqa_bond_canon: unknown dtype %d", dtype);
 }
 
 }  // extern "C"

@@ -37,6 +37,19 @@ log = logging.getLogger(__name__)
 INIT_STATE = (np.sqrt(0.5), -np.sqrt(0.5))   # src/bqa/state.py:21
 
 
+def resolve_precision(precision: str | None = None) -> str:
+    """Arithmetic of a job: "single" (complex64, this backend's default) or "double" (complex128).
+
+    Without an explicit argument the reference's switch is honoured: the environment
+    variable BQA_PRECISION (src/bqa/utils.py:10-21); unset means "single" here, because
+    the FP32 path is this backend's production path."""
+    import os
+    p = (precision or os.environ.get("BQA_PRECISION") or "single").lower()
+    if p not in ("single", "double"):
+        raise ValueError(f"Unknown value of BQA_PRECISION environment variable {p}")
+    return p
+
+
 def _ptr(t) -> int:
     return t.data_ptr() if t is not None and t.numel() > 0 else 0
 
@@ -51,18 +64,23 @@ class _DeviceClass:
     lmbd_pos: object
     edge_ampl: object
     node_ampl: object
-    tensors: list          # two ping-pong buffers, flat complex64
+    tensors: list          # two ping-pong buffers, flat complex
 
 
 class Annealer:
     """One annealing job resident on one GPU."""
 
-    def __init__(self, ctx: Context, device=None, bp_check_every: int = 4):
+    def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4):
         import torch
         self.torch = torch
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 backend needs a CUDA device")
         self.lib = _lib.load()
+        self.precision = resolve_precision(precision)
+        self.dtype = _lib.BQA_C64 if self.precision == "single" else _lib.BQA_C128
+        cplx = torch.complex64 if self.precision == "single" else torch.complex128
+        real = torch.float32 if self.precision == "single" else torch.float64
+        self.real_np = np.float32 if self.precision == "single" else np.float64
         self.ctx = ctx
         self.device = torch.device(device if device is not None else "cuda")
         self.bp_check_every = max(1, int(bp_check_every))
@@ -71,11 +89,11 @@ class Annealer:
         self.half = E // 2
         chimax = ctx.max_bond_dim
         for d in ctx.degree_to_layout:
-            lim = self.lib.max_bond_dim(d)
+            lim = self.lib.max_bond_dim(d, self.dtype)
             if chimax > lim:
                 raise NotImplementedError(
                     f"max_bond_dim={chimax} with degree-{d} nodes is beyond what the GB300 kernels "
-                    f"hold on chip (max {lim} for this degree)")
+                    f"hold on chip at {self.precision} precision (max {lim} for this degree)")
         dev = self.device
         i32 = torch.int32
         self.classes: list[_DeviceClass] = []
@@ -91,21 +109,21 @@ class Annealer:
                 edge_ampl=torch.as_tensor(np.ascontiguousarray(np.asarray(L.edge_ampls, dtype=np.float64).T),
                                           dtype=torch.float64, device=dev),
                 node_ampl=torch.as_tensor(L.node_ampls, dtype=torch.float64, device=dev),
-                tensors=[torch.empty(size, dtype=torch.complex64, device=dev) for _ in range(2)],
+                tensors=[torch.empty(size, dtype=cplx, device=dev) for _ in range(2)],
             ))
         nmax = 2 * chimax
-        c64 = torch.complex64
-        self.msgs = [torch.empty(E * chimax * chimax, dtype=c64, device=dev) for _ in range(2)]
+        self.msgs = [torch.empty(E * chimax * chimax, dtype=cplx, device=dev) for _ in range(2)]
         # simple-update scratch: ext messages (later reused for canonicalisers), lu, ul
-        self.ext = torch.empty(E * nmax * nmax, dtype=c64, device=dev)
-        self.lu = torch.empty(E * nmax * nmax, dtype=c64, device=dev)
-        self.ul = torch.empty(E * nmax * nmax, dtype=c64, device=dev)
-        self.lmbds = torch.empty(self.half * nmax, dtype=torch.float32, device=dev)
-        self.colmax = torch.zeros(nmax, dtype=torch.int32, device=dev)
-        self.dist_parts = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.ext = torch.empty(E * nmax * nmax, dtype=cplx, device=dev)
+        self.lu = torch.empty(E * nmax * nmax, dtype=cplx, device=dev)
+        self.ul = torch.empty(E * nmax * nmax, dtype=cplx, device=dev)
+        self.lmbds = torch.empty(self.half * nmax, dtype=real, device=dev)
+        # max over edges of each lambda column, as the real's bit pattern
+        self.colmax = torch.zeros(nmax, dtype=torch.int32 if self.precision == "single" else torch.int64, device=dev)
+        self.dist_parts = torch.zeros(2, dtype=torch.int64, device=dev)
         self.loop_state = torch.zeros(8, dtype=torch.int32, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.rho = torch.empty(ctx.nodes_number * 4, dtype=c64, device=dev)
+        self.rho = torch.empty(ctx.nodes_number * 4, dtype=cplx, device=dev)
         self.zz = torch.empty(self.half, dtype=torch.float64, device=dev)
         self.norm2 = torch.zeros(1, dtype=torch.float64, device=dev)
         self.rng = np.random.default_rng(ctx.seed)
@@ -127,6 +145,10 @@ class Annealer:
         return arr
 
     @property
+    def _np_cplx(self):
+        return np.complex64 if self.precision == "single" else np.complex128
+
+    @property
     def bond_dim(self) -> int:
         return self.chi
 
@@ -140,13 +162,14 @@ class Annealer:
         self.chi = 1
         self.tcur = 0
         self.mcur = 0
-        init = self.torch.tensor([complex(INIT_STATE[0]), complex(INIT_STATE[1])], dtype=self.torch.complex64,
+        init = self.torch.tensor([complex(INIT_STATE[0]), complex(INIT_STATE[1])], dtype=self.msgs[0].dtype,
                                  device=self.device)
         for c in self.classes:
             c.tensors[0][: 2 * c.count].view(c.count, 2).copy_(init.expand(c.count, 2))
         self.lam_stride = 1
         self.lmbds[: self.half].fill_(1.0)
-        self.lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), 1, self.E, 1, _ptr(self._msgs_cur()), self.stream)
+        self.lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), 1, self.E, 1, self.dtype, _ptr(self._msgs_cur()),
+                      self.stream)
 
     def set_state(self, degree_to_tensor: dict, msgs: np.ndarray, lmbds: np.ndarray | None = None) -> None:
         """Load a state given as numpy arrays (tensors ``(B, 2, chi, ..)`` per degree, messages
@@ -157,12 +180,12 @@ class Annealer:
             raise ValueError("state bond dim exceeds max_bond_dim")
         self.chi, self.tcur, self.mcur = chi, 0, 0
         for c in self.classes:
-            t = np.ascontiguousarray(degree_to_tensor[c.degree], dtype=np.complex64).reshape(-1)
+            t = np.ascontiguousarray(degree_to_tensor[c.degree], dtype=self._np_cplx).reshape(-1)
             c.tensors[0][: t.size].copy_(torch.from_numpy(t))
-        m = np.ascontiguousarray(msgs, dtype=np.complex64).reshape(-1)
+        m = np.ascontiguousarray(msgs, dtype=self._np_cplx).reshape(-1)
         self.msgs[0][: m.size].copy_(torch.from_numpy(m))
         if lmbds is not None:
-            lam = np.ascontiguousarray(lmbds.real, dtype=np.float32)
+            lam = np.ascontiguousarray(lmbds.real, dtype=self.real_np)
             self.lam_stride = lam.shape[1]
             self.lmbds[: lam.size].copy_(torch.from_numpy(lam.reshape(-1)))
 
@@ -190,27 +213,28 @@ class Annealer:
         n = 2 * chi
         eps = float(ctx.pinv_eps)
         cls = self._class_array()
-        lib.call("bqa_ext_msgs", cls, len(self.classes), chi, _ptr(self._msgs_cur()), _ptr(self.ext),
+        dt = self.dtype
+        lib.call("bqa_ext_msgs", cls, len(self.classes), chi, dt, _ptr(self._msgs_cur()), _ptr(self.ext),
                  float(ztime), st)
-        lib.call("bqa_env_factor", _ptr(self.ext), self.E, n, eps, _ptr(self.lu), _ptr(self.ul),
+        lib.call("bqa_env_factor", _ptr(self.ext), self.E, n, dt, eps, _ptr(self.lu), _ptr(self.ul),
                  _ptr(self.status), st)
         self.colmax.zero_()
         canon = self.ext  # the extended messages are consumed; reuse their storage
-        lib.call("bqa_bond_canon", _ptr(self.lu), _ptr(self.ul), self.E, n, eps, _ptr(canon),
+        lib.call("bqa_bond_canon", _ptr(self.lu), _ptr(self.ul), self.E, n, dt, eps, _ptr(canon),
                  _ptr(self.lmbds), _ptr(self.colmax), _ptr(self.status), st)
         # global truncation (src/bqa/backends.py:297-303)
-        max_l = self.colmax[:n].view(self.torch.float32).cpu().numpy().astype(np.float64)
+        max_l = self.colmax[:n].view(self.lmbds.dtype).cpu().numpy().astype(np.float64)
         rank = n - int(np.sum(max_l < eps))
         dim = min(rank, ctx.max_bond_dim)
         err = float(np.sqrt(np.sum(max_l[dim:] ** 2)))
         log.info(f"Truncation performed, per edge error upper bound: {err}")
         cls = self._class_array(out=True)
-        lib.call("bqa_apply_update", cls, len(self.classes), chi, dim, _ptr(canon), _ptr(self.lmbds), n,
+        lib.call("bqa_apply_update", cls, len(self.classes), chi, dim, dt, _ptr(canon), _ptr(self.lmbds), n,
                  float(ztime), float(xtime), st)
         self.tcur = 1 - self.tcur
         self.chi = dim
         self.lam_stride = n
-        lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), n, self.E, dim, _ptr(self._msgs_cur()), st)
+        lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), n, self.E, dim, dt, _ptr(self._msgs_cur()), st)
         return dim, err
 
     def run_layer(self, xtime: float, ztime: float) -> dict:
@@ -238,9 +262,9 @@ class Annealer:
         eps, damp = float(ctx.bp_eps), float(ctx.damping)
         while True:
             for _ in range(min(self.bp_check_every, ctx.max_bp_iters_number - launched)):
-                lib.call("bqa_bp_sweep", cls, len(self.classes), self.chi, _ptr(a), _ptr(b),
+                lib.call("bqa_bp_sweep", cls, len(self.classes), self.chi, self.dtype, _ptr(a), _ptr(b),
                          _ptr(self.dist_parts), _ptr(self.loop_state), st)
-                lib.call("bqa_bp_finalize", _ptr(a), _ptr(b), elems, _ptr(self.dist_parts),
+                lib.call("bqa_bp_finalize", _ptr(a), _ptr(b), elems, self.dtype, _ptr(self.dist_parts),
                          _ptr(self.loop_state), eps, damp, ctx.max_bp_iters_number, st)
                 launched += 1
             ls = self.loop_state.cpu().numpy()
@@ -259,7 +283,7 @@ class Annealer:
     # ---- read-out ------------------------------------------------------------------------
     def density_matrices(self) -> np.ndarray:
         """(n, 2, 2) complex marginals (src/bqa/state.py:77-94)."""
-        self.lib.call("bqa_densities", self._class_array(), len(self.classes), self.chi,
+        self.lib.call("bqa_densities", self._class_array(), len(self.classes), self.chi, self.dtype,
                       _ptr(self._msgs_cur()), _ptr(self.rho), self.stream)
         return self.rho.view(-1, 2, 2).cpu().numpy().astype(np.complex128)
 
@@ -273,9 +297,9 @@ class Annealer:
     def edge_zz(self) -> np.ndarray:
         """BP two-site <Z_u Z_v> per undirected edge (oracle ``edge_zz``)."""
         pm = self.lu   # scratch of the simple update, idle between steps
-        self.lib.call("bqa_psplit", self._class_array(), len(self.classes), self.chi, _ptr(self._msgs_cur()),
-                      _ptr(pm), self.stream)
-        self.lib.call("bqa_edge_zz", _ptr(pm), self.E, self.chi, _ptr(self.zz), self.stream)
+        self.lib.call("bqa_psplit", self._class_array(), len(self.classes), self.chi, self.dtype,
+                      _ptr(self._msgs_cur()), _ptr(pm), self.stream)
+        self.lib.call("bqa_edge_zz", _ptr(pm), self.E, self.chi, self.dtype, _ptr(self.zz), self.stream)
         return self.zz.cpu().numpy()
 
     def energy(self, zz: np.ndarray | None = None, z: np.ndarray | None = None) -> float:
@@ -307,7 +331,7 @@ class Annealer:
             pos = self.torch.as_tensor(ctx.node_position[nodes[sel]].astype(np.int32), device=self.device)
             out = self.torch.as_tensor(outcomes[sel].astype(np.int32), device=self.device)
             self.lib.call("bqa_project_nodes", _ptr(c.tensors[self.tcur]), c.count, 2 * self.chi ** c.degree,
-                          _ptr(pos), _ptr(out), int(pos.numel()), _ptr(self.norm2), self.stream)
+                          self.dtype, _ptr(pos), _ptr(out), int(pos.numel()), _ptr(self.norm2), self.stream)
 
     def measure(self) -> list:
         """Sequential most-polarised-first sampling (src/bqa/state.py:250-312) with the same

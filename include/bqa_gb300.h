@@ -8,10 +8,13 @@
  * cites the reference code it replaces.
  *
  * Conventions
- *  - All pointers are DEVICE pointers unless a parameter says "host".  Complex numbers
- *    are complex64 stored as interleaved (re, im) float pairs, i.e. ``float2``.
+ *  - All pointers are DEVICE pointers unless a parameter says "host".
+ *  - ``dtype`` selects the arithmetic: BQA_C64 = complex64 stored as interleaved float
+ *    pairs (``float2``), real side buffers float; BQA_C128 = complex128 (``double2``),
+ *    real side buffers double -- the reference's BQA_PRECISION=single / double
+ *    (src/bqa/utils.py:10-30).
  *  - Index maps are int32, node-major: ``in_pos[i*d + k]`` is the message slot of the
- *    edge nbr_k -> node i of the class (reference layout keeps the same values k-major,
+ *    edge nbr_k -> node i of the class (the reference keeps the same values k-major,
  *    src/bqa/config/config_canonicalization.py:62-131).
  *  - A node tensor of degree d at bond dim chi is ``[2][chi]...[chi]`` (last bond
  *    fastest); a class stores its B tensors back to back.  Messages are ``[E][chi][chi]``.
@@ -39,6 +42,8 @@ enum {
     BQA_ERR_CUDA = 3          /* a CUDA runtime call failed; see bqa_last_error() */
 };
 
+enum { BQA_C64 = 0, BQA_C128 = 1 };
+
 /* device status word bits (written by kernels into a caller int32) */
 enum {
     BQA_STATUS_SVD_NOT_CONVERGED = 1  /* a Jacobi SVD hit its sweep cap */
@@ -55,8 +60,8 @@ typedef struct bqa_class {
     const int32_t* lmbd_pos;   /* [B][d] lambda slot of the edge (= out_pos % (E/2)) */
     const double* edge_ampl;   /* [B][d] coupling J of the edge */
     const double* node_ampl;   /* [B]    field h of the node */
-    void* tensor;              /* [B][2][chi^d] complex64, current tensors */
-    void* tensor_out;          /* [B][2][dim^d] complex64, written by bqa_apply_update */
+    void* tensor;              /* [B][2][chi^d] complex, current tensors */
+    void* tensor_out;          /* [B][2][dim^d] complex, written by bqa_apply_update */
 } bqa_class;
 
 /* ABI version of this header (bumped on any signature change). */
@@ -65,38 +70,37 @@ int32_t bqa_abi_version(void);
 /* Text of the last error raised on the calling host thread (static storage). */
 const char* bqa_last_error(void);
 
-/* Largest bond dimension the message kernels accept for degree d (0: degree unsupported). */
-int32_t bqa_max_bond_dim(int32_t degree);
+/* Largest bond dimension the kernels accept for degree d at dtype (0: unsupported). */
+int32_t bqa_max_bond_dim(int32_t degree, int32_t dtype);
 
 /*
  * One BP sweep over all classes (src/bqa/state.py:105-113 with
  * Tensor.pass_msgs, src/bqa/backends.py:381-408): for every node and bond k, the message
  * node -> nbr_k is the trace-normalised contraction of conj(T) with T after every other
  * incoming message has been applied.  Every message slot of the output buffer is written,
- * and max|new-old|^2, max|new+old|^2 are folded into dist_parts[0..1] (float bits; zero
- * them before the first sweep, bqa_bp_finalize re-zeroes them).
+ * and max|new-old|^2, max|new+old|^2 are folded into dist_parts (2 reals as unsigned bits:
+ * uint32[2] for BQA_C64, uint64[2] for BQA_C128; zero them before the first sweep,
+ * bqa_bp_finalize re-zeroes them).
  * With loop_state == NULL the sweep reads msgs_a and writes msgs_b.  Otherwise
  * (device-driven loop, see bqa_bp_finalize) it returns at once when loop_state[0] (done)
  * is set, and reads buffer loop_state[2] (0: msgs_a, 1: msgs_b) and writes the other.
  */
-int32_t bqa_bp_sweep(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi,
-                     void* msgs_a, void* msgs_b, uint32_t* dist_parts,
-                     const int32_t* loop_state, void* stream);
+int32_t bqa_bp_sweep(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi, int32_t dtype,
+                     void* msgs_a, void* msgs_b, void* dist_parts, const int32_t* loop_state, void* stream);
 
 /*
  * BP convergence decision and damping after one sweep (src/bqa/state.py:113-124,
  * Tensor.get_dist src/bqa/backends.py:492-495, damping src/bqa/backends.py:761-764).
- * loop_state is int32[8] = {done, sweeps, cur, exhausted, damp_pending, dist bits,
- * best dist bits, unused}; zero it (and dist_parts) before the first sweep of a BP run.
- * When dist < eps the run is done and the current buffer (the sweep's INPUT) is kept;
- * otherwise the current buffer becomes damping*current + (1-damping)*new (a buffer flip
- * when damping == 0).  After sweep max_iters without convergence the run is done with
- * ``exhausted`` set and ``cur`` pointing at the raw output of the last sweep (the
+ * loop_state is int32[8] = {done, sweeps, cur, exhausted, damp_pending, dist (float bits),
+ * best dist (float bits), unused}; zero it (and dist_parts) before the first sweep of a
+ * BP run.  When dist < eps the run is done and the current buffer (the sweep's INPUT) is
+ * kept; otherwise the current buffer becomes damping*current + (1-damping)*new (a buffer
+ * flip when damping == 0).  After sweep max_iters without convergence the run is done
+ * with ``exhausted`` set and ``cur`` pointing at the raw output of the last sweep (the
  * reference keeps that buffer too).  Does nothing once done is set.
  */
-int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, uint32_t* dist_parts,
-                        int32_t* loop_state, float eps, float damping, int32_t max_iters,
-                        void* stream);
+int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, int32_t dtype, void* dist_parts,
+                        int32_t* loop_state, double eps, double damping, int32_t max_iters, void* stream);
 
 /*
  * Extended messages of the ZZ-gate layer (src/bqa/state.py:127-139 with the conditional-Z
@@ -104,27 +108,28 @@ int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, uint32_t*
  * 2chi x 2chi message of the tensor whose bond k carries half of exp(-i J_k ztime Z Z).
  * Writes ext_out[E][2chi][2chi].
  */
-int32_t bqa_ext_msgs(const bqa_class* classes, int32_t n_classes, int32_t chi,
-                     const void* msgs, void* ext_out, double ztime, void* stream);
+int32_t bqa_ext_msgs(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, const void* msgs,
+                     void* ext_out, double ztime, void* stream);
 
 /*
  * Environment factors of every (extended) message m = U S Vh, singular values <= eps
  * dropped (src/bqa/backends.py:483-490,709-727): lu = sqrt(S) Vh and ul = U pinv(sqrt(S)),
- * both [E][n][n].  One-sided Jacobi SVD per matrix, FP32; a matrix that hits the sweep cap
- * sets BQA_STATUS_SVD_NOT_CONVERGED in *status.
+ * both [count][n][n], n <= 32.  One-sided Jacobi SVD per matrix in the dtype's precision;
+ * a matrix that hits the sweep cap sets BQA_STATUS_SVD_NOT_CONVERGED in *status.
  */
-int32_t bqa_env_factor(const void* mats, int32_t count, int32_t n, float eps,
-                       void* lu, void* ul, int32_t* status, void* stream);
+int32_t bqa_env_factor(const void* mats, int32_t count, int32_t n, int32_t dtype, double eps, void* lu, void* ul,
+                       int32_t* status, void* stream);
 
 /*
  * Bond canonicalisation (src/bqa/state.py:171-200): for every undirected edge p < E/2,
  * ker = lu[p] lu[p+E/2]^T = us s vhs (masked at eps), lambdas = s/|s| (descending) into
- * lmbds[p][0..n-1], canonicalisers ul[p+E/2] us -> canon[p+E/2] and ul[p] vhs^T ->
- * canon[p], and max over edges of each lambda column folded into colmax[0..n-1]
- * (float bits, caller zeroes; src/bqa/backends.py:297-303).
+ * lmbds[p][0..n-1] (real), canonicalisers ul[p] us -> canon[p+E/2] and ul[p+E/2] vhs^T ->
+ * canon[p], and the max over edges of each lambda column folded into colmax[0..n-1]
+ * (real bits, uint32 for BQA_C64, uint64 for BQA_C128; caller zeroes;
+ * src/bqa/backends.py:297-303).
  */
-int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n, float eps,
-                       void* canon, float* lmbds, uint32_t* colmax, int32_t* status, void* stream);
+int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n, int32_t dtype, double eps, void* canon,
+                       void* lmbds, void* colmax, int32_t* status, void* stream);
 
 /*
  * Tensor update of one annealing step after truncation to bond dim ``dim``: per node,
@@ -132,41 +137,41 @@ int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n,
  * canon[in_pos[k]], src/bqa/backends.py:416-432), then Rz(h ztime) and Rx(xtime)
  * (src/bqa/state.py:142-156), sqrt(lambda) on every bond and per-node L2 normalisation
  * (symmetric gauge, src/bqa/state.py:219-227).  Reads tensor, writes tensor_out.
- * lmbds is [E/2][lam_stride] with the kept values in the first dim columns.
+ * lmbds is real [E/2][lam_stride] with the kept values in the first dim columns.
  */
-int32_t bqa_apply_update(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dim,
-                         const void* canon, const float* lmbds, int32_t lam_stride,
-                         double ztime, double xtime, void* stream);
+int32_t bqa_apply_update(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dim, int32_t dtype,
+                         const void* canon, const void* lmbds, int32_t lam_stride, double ztime, double xtime,
+                         void* stream);
 
 /* msgs[e] = diag(lmbds[e % (E/2)][0..dim-1]) / trace (src/bqa/state.py:56-57). */
-int32_t bqa_msgs_from_lmbds(const float* lmbds, int32_t lam_stride, int32_t edges, int32_t dim,
+int32_t bqa_msgs_from_lmbds(const void* lmbds, int32_t lam_stride, int32_t edges, int32_t dim, int32_t dtype,
                             void* msgs, void* stream);
 
 /*
  * Per-node 2x2 marginals (src/bqa/state.py:77-94, src/bqa/backends.py:440-448), written
- * to rho[node_id][2][2] (complex64).  Degree-0 nodes get psi psi^dagger.
+ * to rho[node_id][2][2].  Degree-0 nodes get psi psi^dagger.
  */
-int32_t bqa_densities(const bqa_class* classes, int32_t n_classes, int32_t chi,
-                      const void* msgs, void* rho, void* stream);
+int32_t bqa_densities(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, const void* msgs,
+                      void* rho, void* stream);
 
 /*
  * Phys-resolved open-bond blocks P_s of every directed edge slot (unnormalised), written
  * to pm[E][2][chi][chi]; input of bqa_edge_zz.  No reference counterpart (the reference
- * computes no two-site quantity); definition in oracle/bqa_oracle.py:psplit_msgs.
+ * computes no two-site quantity); the definition is oracle/bqa_oracle.py:psplit_msgs.
  */
-int32_t bqa_psplit(const bqa_class* classes, int32_t n_classes, int32_t chi,
-                   const void* msgs, void* pm, void* stream);
+int32_t bqa_psplit(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, const void* msgs, void* pm,
+                   void* stream);
 
 /* BP two-site <Z_u Z_v> of every undirected edge p < E/2 from pm, into zz[p] (float64). */
-int32_t bqa_edge_zz(const void* pm, int32_t edges, int32_t chi, double* zz, void* stream);
+int32_t bqa_edge_zz(const void* pm, int32_t edges, int32_t chi, int32_t dtype, double* zz, void* stream);
 
 /*
  * Projective measurement of m nodes of one class (src/bqa/backends.py:730-734): for each
  * j < m, the outcome-(1 - outcomes[j]) half of node positions[j] is zeroed; then the
- * whole class buffer (count * node_elems complex64) is divided by its L2 norm.
+ * whole class buffer (count * node_elems complex) is divided by its L2 norm.
  * positions/outcomes are device int32[m]; norm2_scratch is a device double.
  */
-int32_t bqa_project_nodes(void* tensors, int32_t count, int32_t node_elems, const int32_t* positions,
+int32_t bqa_project_nodes(void* tensors, int32_t count, int32_t node_elems, int32_t dtype, const int32_t* positions,
                           const int32_t* outcomes, int32_t m, double* norm2_scratch, void* stream);
 
 #ifdef __cplusplus

@@ -38,11 +38,13 @@ def test_abi_version_and_limits(lib):
     assert lib.max_bond_dim(3) == 16
     assert lib.max_bond_dim(4) == 8
     assert lib.max_bond_dim(-1) == 0
+    assert lib.max_bond_dim(3, _lib.BQA_C128) == 13
+    assert lib.max_bond_dim(3, 7) == 0
 
 
 def test_bad_arguments_are_reported_not_crashing(lib):
-    rc = lib.dll.bqa_env_factor(None, 4, 8, ctypes.c_float(1e-6), None, None, None, None)
+    rc = lib.dll.bqa_env_factor(None, 4, 8, 0, 1e-6, None, None, None, None)
     assert rc == 1
     assert b"bqa_env_factor" in lib.dll.bqa_last_error()
     with pytest.raises(_lib.BqaError):
-        lib.call("bqa_edge_zz", None, 4, 2, None, None)
+        lib.call("bqa_edge_zz", None, 4, 2, 0, None, None)

@@ -26,7 +26,7 @@ CASES = [("rr3_n16_chi4", 4), ("rr3_n24_chi8", 8), ("mixed_n18_chi3", 3), ("rr4_
 RTOL = 2e-5
 
 
-def random_state(name, chi, seed=0):
+def random_state(name, chi, seed=0, precision="single"):
     conf = gc.config(name)
     conf["max_bond_dim"] = chi
     octx = orc.make_context(conf)
@@ -46,7 +46,7 @@ def random_state(name, chi, seed=0):
     tens = {d: t.astype(np.complex64).astype(np.complex128) for d, t in tens.items()}
     m = m.astype(np.complex64).astype(np.complex128)
     st = orc.OracleState(np.random.default_rng(0), tens, m, lam.astype(np.complex128))
-    job = Annealer(build_context(conf))
+    job = Annealer(build_context(conf), precision=precision)
     job.set_state(tens, m, lam)
     return octx, st, job
 
@@ -64,11 +64,11 @@ def test_bp_sweep_matches_oracle(name, chi):
         for mm, p in zip(orc.pass_msgs(t, [st.msgs[p] for p in L.input_msgs_position]), L.output_msgs_position):
             want[p] = mm
     job.dist_parts.zero_()
-    job.lib.call("bqa_bp_sweep", job._class_array(), len(job.classes), chi, _ptr(job.msgs[0]), _ptr(job.msgs[1]),
-                 _ptr(job.dist_parts), None, job.stream)
+    job.lib.call("bqa_bp_sweep", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.msgs[1]), _ptr(job.dist_parts), None, job.stream)
     got = job.msgs[1][: want.size].cpu().numpy().reshape(want.shape)
     assert rel_err(got, want) < RTOL
-    num, den = job.dist_parts.view(torch.float32).cpu().numpy()
+    num, den = job.dist_parts.view(torch.int32)[:2].view(torch.float32).cpu().numpy()
     d_want = orc.get_dist(want, st.msgs)
     assert abs(np.sqrt(num) / np.sqrt(den) - d_want) < 1e-5 * max(1.0, d_want)
 
@@ -78,8 +78,8 @@ def test_ext_msgs_match_oracle(name, chi):
     octx, st, job = random_state(name, chi, seed=1)
     ztime = 0.37
     want = orc.get_extended_msgs(octx, ztime, st)
-    job.lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, _ptr(job.msgs[0]), _ptr(job.ext),
-                 ztime, job.stream)
+    job.lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.ext), ztime, job.stream)
     got = job.ext[: want.size].cpu().numpy().reshape(want.shape)
     assert rel_err(got, want) < RTOL
 
@@ -94,8 +94,9 @@ def test_canonicalisers_match_oracle(name, chi):
     job.ext[: ext.size].copy_(torch.from_numpy(ext.astype(np.complex64).reshape(-1)))
     job.status.zero_()
     job.colmax.zero_()
-    job.lib.call("bqa_env_factor", _ptr(job.ext), E, n, eps, _ptr(job.lu), _ptr(job.ul), _ptr(job.status), job.stream)
-    job.lib.call("bqa_bond_canon", _ptr(job.lu), _ptr(job.ul), E, n, eps, _ptr(job.ext), _ptr(job.lmbds),
+    job.lib.call("bqa_env_factor", _ptr(job.ext), E, n, job.dtype, eps, _ptr(job.lu), _ptr(job.ul), _ptr(job.status),
+                 job.stream)
+    job.lib.call("bqa_bond_canon", _ptr(job.lu), _ptr(job.ul), E, n, job.dtype, eps, _ptr(job.ext), _ptr(job.lmbds),
                  _ptr(job.colmax), _ptr(job.status), job.stream)
     assert int(job.status.item()) == 0
     lam = job.lmbds[: E // 2 * n].cpu().numpy().reshape(E // 2, n)
@@ -112,7 +113,7 @@ def test_canonicalisers_match_oracle(name, chi):
     assert rel_err(g, g_w) < 5e-4
 
 
-@pytest.mark.parametrize("name,chi,dim", [("rr3_n16_chi4", 2, 4), ("rr3_n24_chi8", 8, 8), ("mixed_n18_chi3", 3, 5),
+@pytest.mark.parametrize("name,chi,dim", [("rr3_n16_chi4", 2, 4), ("rr3_n24_chi8", 8, 8), ("grid3x4_chi4_damped", 3, 5),
                                           ("rr4_n20_chi4", 4, 3), ("rr3_n16_chi4", 16, 16)])
 def test_apply_update_matches_oracle(name, chi, dim):
     octx, st, job = random_state(name, max(chi, dim), seed=3)
@@ -138,15 +139,15 @@ def test_apply_update_matches_oracle(name, chi, dim):
     job.set_state(tens, np.zeros((E, chi, chi), np.complex64))
     job.ext[: can.size].copy_(torch.from_numpy(can.astype(np.complex64).reshape(-1)))
     job.lmbds[: lam.size].copy_(torch.from_numpy(lam.reshape(-1)))
-    job.lib.call("bqa_apply_update", job._class_array(out=True), len(job.classes), chi, dim, _ptr(job.ext),
-                 _ptr(job.lmbds), n, ztime, xtime, job.stream)
+    job.lib.call("bqa_apply_update", job._class_array(out=True), len(job.classes), chi, dim, job.dtype,
+                 _ptr(job.ext), _ptr(job.lmbds), n, ztime, xtime, job.stream)
     job.tcur = 1
     job.chi = dim
     for c in job.classes:
         shape = (c.count, 2) + (dim,) * c.degree
         got = c.tensors[1][: int(np.prod(shape))].cpu().numpy().reshape(shape)
         assert rel_err(got, ost.degree_to_tensor[c.degree]) < RTOL
-    job.lib.call("bqa_msgs_from_lmbds", _ptr(job.lmbds), n, E, dim, _ptr(job.msgs[0]), job.stream)
+    job.lib.call("bqa_msgs_from_lmbds", _ptr(job.lmbds), n, E, dim, job.dtype, _ptr(job.msgs[0]), job.stream)
     got_m = job.msgs[0][: E * dim * dim].cpu().numpy().reshape(E, dim, dim)
     assert rel_err(got_m, ost.msgs) < 1e-6
 
@@ -172,8 +173,22 @@ def test_bp_loop_matches_oracle(name, chi):
     assert np.abs(msgs - st.msgs).max() < 2e-5
 
 
-def test_library_reports_limits():
-    lib = _lib.load()
-    assert lib.max_bond_dim(3) == 16
-    assert lib.max_bond_dim(4) == 8
-    assert lib.max_bond_dim(2) == 16
+@pytest.mark.parametrize("name,chi", [("rr3_n16_chi4", 4), ("mixed_n18_chi3", 3), ("tree9", 2)])
+def test_double_precision_kernels_match_oracle_to_roundoff(name, chi):
+    """The complex128 build of the same kernels agrees with the FP64 oracle to ~1e-12."""
+    octx, st, job = random_state(name, chi, seed=7, precision="double")
+    want = np.empty_like(st.msgs)
+    for d, t in st.degree_to_tensor.items():
+        L = octx.degree_to_layout[d]
+        for mm, p in zip(orc.pass_msgs(t, [st.msgs[p] for p in L.input_msgs_position]), L.output_msgs_position):
+            want[p] = mm
+    job.dist_parts.zero_()
+    job.lib.call("bqa_bp_sweep", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.msgs[1]), _ptr(job.dist_parts), None, job.stream)
+    got = job.msgs[1][: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, want) < 1e-12
+    ext_w = orc.get_extended_msgs(octx, 0.3, st)
+    job.lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.ext), 0.3, job.stream)
+    assert rel_err(job.ext[: ext_w.size].cpu().numpy().reshape(ext_w.shape), ext_w) < 1e-12
+    assert np.abs(job.density_matrices() - orc.get_density_matrices(octx, st)).max() < 1e-12
