@@ -128,7 +128,45 @@ class Annealer:
         self.norm2 = torch.zeros(1, dtype=torch.float64, device=dev)
         self.rng = np.random.default_rng(ctx.seed)
         self.stats: list[dict] = []
+        self._events: list | None = None
         self.reset()
+
+    # ---- kernel timing (CUDA events on the launch stream) ----------------------------------
+    def enable_kernel_timing(self, on: bool = True) -> None:
+        """Record a CUDA event pair around every C-ABI launch group (bench instrumentation)."""
+        self._events = [] if on else None
+
+    def _launch(self, name: str, flops: float, nbytes: float, fn, *args) -> None:
+        if self._events is None:
+            fn(*args)
+            return
+        ev0 = self.torch.cuda.Event(enable_timing=True)
+        ev1 = self.torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        fn(*args)
+        ev1.record()
+        self._events.append([name, ev0, ev1, flops, nbytes])
+
+    def kernel_times(self) -> list[tuple[str, float, float, float]]:
+        """(name, milliseconds, algorithmic flops, algorithmic bytes) of every timed launch
+        group since timing was enabled; synchronises the device."""
+        if not self._events:
+            return []
+        self.torch.cuda.synchronize(self.device)
+        return [(n, a.elapsed_time(b), f, by) for n, a, b, f, by in self._events]
+
+    def bp_sweep_cost(self) -> tuple[float, float]:
+        """Algorithmic (flops, bytes) of one BP sweep at the current bond dim: per node of degree
+        d, 2 d^2 chi^(d+1) complex MACs (d messages, each d-1 mode products and one closing
+        contraction), and the tensor read once plus d messages read and d written."""
+        chi, el = self.chi, (8 if self.precision == "single" else 16)
+        f = b = 0.0
+        for c in self.classes:
+            if c.degree == 0:
+                continue
+            f += c.count * 8.0 * 2 * c.degree ** 2 * chi ** (c.degree + 1)
+            b += c.count * el * (2.0 * chi ** c.degree + 2.0 * c.degree * chi * chi)
+        return f, b
 
     # ---- helpers -------------------------------------------------------------------------
     @property
@@ -214,14 +252,14 @@ class Annealer:
         eps = float(ctx.pinv_eps)
         cls = self._class_array()
         dt = self.dtype
-        lib.call("bqa_ext_msgs", cls, len(self.classes), chi, dt, _ptr(self._msgs_cur()), _ptr(self.ext),
-                 float(ztime), st)
-        lib.call("bqa_env_factor", _ptr(self.ext), self.E, n, dt, eps, _ptr(self.lu), _ptr(self.ul),
-                 _ptr(self.status), st)
+        self._launch("ext_msgs", 0.0, 0.0, lib.call, "bqa_ext_msgs", cls, len(self.classes), chi, dt,
+                     _ptr(self._msgs_cur()), _ptr(self.ext), float(ztime), st)
+        self._launch("env_factor", 0.0, 0.0, lib.call, "bqa_env_factor", _ptr(self.ext), self.E, n, dt, eps,
+                     _ptr(self.lu), _ptr(self.ul), _ptr(self.status), st)
         self.colmax.zero_()
         canon = self.ext  # the extended messages are consumed; reuse their storage
-        lib.call("bqa_bond_canon", _ptr(self.lu), _ptr(self.ul), self.E, n, dt, eps, _ptr(canon),
-                 _ptr(self.lmbds), _ptr(self.colmax), _ptr(self.status), st)
+        self._launch("bond_canon", 0.0, 0.0, lib.call, "bqa_bond_canon", _ptr(self.lu), _ptr(self.ul), self.E, n,
+                     dt, eps, _ptr(canon), _ptr(self.lmbds), _ptr(self.colmax), _ptr(self.status), st)
         # global truncation (src/bqa/backends.py:297-303)
         max_l = self.colmax[:n].view(self.lmbds.dtype).cpu().numpy().astype(np.float64)
         rank = n - int(np.sum(max_l < eps))
@@ -229,8 +267,8 @@ class Annealer:
         err = float(np.sqrt(np.sum(max_l[dim:] ** 2)))
         log.info(f"Truncation performed, per edge error upper bound: {err}")
         cls = self._class_array(out=True)
-        lib.call("bqa_apply_update", cls, len(self.classes), chi, dim, dt, _ptr(canon), _ptr(self.lmbds), n,
-                 float(ztime), float(xtime), st)
+        self._launch("apply_update", 0.0, 0.0, lib.call, "bqa_apply_update", cls, len(self.classes), chi, dim, dt,
+                     _ptr(canon), _ptr(self.lmbds), n, float(ztime), float(xtime), st)
         self.tcur = 1 - self.tcur
         self.chi = dim
         self.lam_stride = n
@@ -260,10 +298,12 @@ class Annealer:
         elems = self.E * self.chi * self.chi
         launched = 0
         eps, damp = float(ctx.bp_eps), float(ctx.damping)
+        flops, nbytes = self.bp_sweep_cost()
+        first = len(self._events) if self._events is not None else 0
         while True:
             for _ in range(min(self.bp_check_every, ctx.max_bp_iters_number - launched)):
-                lib.call("bqa_bp_sweep", cls, len(self.classes), self.chi, self.dtype, _ptr(a), _ptr(b),
-                         _ptr(self.dist_parts), _ptr(self.loop_state), st)
+                self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep", cls, len(self.classes), self.chi,
+                             self.dtype, _ptr(a), _ptr(b), _ptr(self.dist_parts), _ptr(self.loop_state), st)
                 lib.call("bqa_bp_finalize", _ptr(a), _ptr(b), elems, self.dtype, _ptr(self.dist_parts),
                          _ptr(self.loop_state), eps, damp, ctx.max_bp_iters_number, st)
                 launched += 1
@@ -272,6 +312,11 @@ class Annealer:
                 break
             if launched >= ctx.max_bp_iters_number:
                 raise RuntimeError("BP loop state did not finish after the iteration cap")
+        if self._events is not None:
+            # sweeps queued after convergence returned at once: they did no algorithmic work
+            sw = [e for e in self._events[first:] if e[0] == "bp_sweep"]
+            for e in sw[int(ls[1]):]:
+                e[0] = "bp_sweep_skipped"
         if ls[2]:
             self.mcur = 1 - self.mcur
         if ls[3]:
