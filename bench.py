@@ -300,6 +300,51 @@ def run_gpu_arm(args) -> None:
         dist.destroy_process_group()
 
 
+def run_sweep_mode(args) -> None:
+    """Time the dominant kernel alone: one BP sweep over all nodes at a fixed bond dim, on
+    random normalised node tensors with maximally mixed messages (a launch of the
+    message kernel does the same work whatever the values).  Prints one JSON line."""
+    import torch
+    from bqa_gb300 import instances
+    from bqa_gb300.engine import Annealer, _ptr
+    from bqa_gb300.layout import build_context
+    conf = instances.headline_gpu_job(n=args.n, seed=0, chi=args.chi)
+    ctx = build_context(conf)
+    job = Annealer(ctx, precision=args.precision)
+    chi = args.chi
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    for c in job.classes:
+        size = c.count * 2 * chi ** c.degree
+        t = torch.randn(size, dtype=job.msgs[0].dtype, device="cuda", generator=gen).view(c.count, -1)
+        c.tensors[0][:size].copy_((t / t.norm(dim=1, keepdim=True)).view(-1))
+    eye = torch.eye(chi, dtype=job.msgs[0].dtype, device="cuda") / chi
+    job.msgs[0][: ctx.edges_number * chi * chi].copy_(eye.expand(ctx.edges_number, chi, chi).reshape(-1))
+    job.chi, job.tcur, job.mcur = chi, 0, 0
+    cls = job._class_array()
+    flops, nbytes = job.bp_sweep_cost()
+
+    def sweep():
+        job.lib.call("bqa_bp_sweep", cls, len(job.classes), chi, job.dtype, _ptr(job.msgs[0]), _ptr(job.msgs[1]),
+                     _ptr(job.dist_parts), None, job.stream)
+
+    for _ in range(args.warmup):
+        sweep()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in evs:
+        a.record()
+        sweep()
+        b.record()
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    mean = float(np.mean(ms))
+    print(json.dumps({"mode": "sweep", "n": args.n, "chi": chi, "precision": args.precision, "sweeps": args.steps,
+                      "ms_per_sweep": mean, "ms_min": float(np.min(ms)),
+                      "tflops": flops / (mean / 1000) / 1e12, "algorithmic_gbs": nbytes / (mean / 1000) / 1e9,
+                      "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": nbytes,
+                      "msg_updates_per_s": ctx.edges_number / (mean / 1000)}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -309,11 +354,15 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep"])
+    ap.add_argument("--precision", default="single", choices=["single", "double"])
     args = ap.parse_args()
     logging.basicConfig(level=logging.ERROR)
     logging.getLogger("bqa_gb300").setLevel(logging.ERROR)
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.mode == "sweep":
+        run_sweep_mode(args)
     else:
         run_gpu_arm(args)
 
