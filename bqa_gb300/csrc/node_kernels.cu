@@ -11,12 +11,23 @@
 //   <Z_u Z_v> input (no reference counterpart):     P_0, P_1 themselves.
 // All kernels are templated on the real type R: float (complex64 path) or double
 // (complex128 path, the reference's BQA_PRECISION=double arithmetic).
+#include <cstdlib>
+
 #include "common.cuh"
 #include "internal.h"
+#include "tiled_node.cuh"
 
 namespace bqa {
 
 enum NodeMode { MODE_BP = 0, MODE_EXT = 1, MODE_PSPLIT = 2, MODE_DENS = 3 };
+
+// The register-tiled kernels serve the (degree, chi) pairs they are built for unless the
+// environment variable BQA_GB300_TILED=0 is set when the library loads (then every launch
+// takes the generic kernel, which tests use to cross-check the two).
+static const bool g_use_tiled = [] {
+    const char* v = getenv("BQA_GB300_TILED");
+    return !(v && v[0] == '0');
+}();
 
 template <typename R>
 struct NodeArgs {
@@ -88,6 +99,50 @@ __device__ __forceinline__ void close_psplit(const C* __restrict__ T, const C* _
 __host__ __device__ inline size_t node_smem_elems(int d, int chi) {
     const size_t NT = 2 * (size_t)ipow(chi, d);
     return 3 * NT + (size_t)(d + 4) * chi * chi + 128;  // + block-reduction scratch
+}
+
+// Outputs of one (node, bond idx) from its open-bond blocks sP = [P_0; P_1]: the BP message
+// (plus the dist maxima), the extended message, or the blocks themselves.
+template <int MODE, typename R>
+__device__ __forceinline__ void write_outputs(const NodeArgs<R>& a, int node, int idx, const typename Cx<R>::T* sP,
+                                              const typename Cx<R>::T* msgs_in, typename Cx<R>::T* msgs_out,
+                                              R& num2, R& den2) {
+    using C = typename Cx<R>::T;
+    const int d = a.d, chi = a.chi, n2 = chi * chi;
+    const int slot = a.out_pos[node * d + idx];
+    if (MODE == MODE_PSPLIT) {
+        C* og = a.out + (size_t)slot * 2 * n2;
+        for (int i = threadIdx.x; i < 2 * n2; i += blockDim.x) og[i] = sP[i];
+    } else {
+        C tr = c_zero<C>();
+        for (int q = 0; q < chi; ++q) tr = c_add(tr, c_add(sP[q * chi + q], sP[n2 + q * chi + q]));
+        if (MODE == MODE_BP) {
+            const C* old = msgs_in + (size_t)slot * n2;
+            C* og = msgs_out + (size_t)slot * n2;
+            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                const C m = c_div(c_add(sP[i], sP[n2 + i]), tr);
+                const C o = old[i];
+                og[i] = m;
+                num2 = fmax(num2, c_abs2(c_sub(m, o)));
+                den2 = fmax(den2, c_abs2(c_add(m, o)));
+            }
+        } else {  // MODE_EXT
+            const HalfZZ<R> h = half_zz<R>(a.edge_ampl[node * d + idx] * a.ztime);
+            const R scale = c_abs2(h.a0) + c_abs2(h.a1);
+            const C trx = c_scale(tr, scale);
+            const int n = 2 * chi;
+            C* og = a.out + (size_t)slot * n * n;
+            for (int o = threadIdx.x; o < n * n; o += blockDim.x) {
+                const int row = o / n, col = o - row * n;
+                const int e = row >= chi, f = col >= chi;
+                const int ia = row - e * chi, ib = col - f * chi;
+                const C p0 = sP[ia * chi + ib], p1 = sP[n2 + ia * chi + ib];
+                const C pe = ((e + f) & 1) ? c_sub(p0, p1) : c_add(p0, p1);
+                const C coef = c_mul(c_conj(e ? h.a1 : h.a0), f ? h.a1 : h.a0);
+                og[o] = c_div(c_mul(coef, pe), trx);
+            }
+        }
+    }
 }
 
 template <int CM, int MODE, typename R>
@@ -163,41 +218,7 @@ __global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
         close_psplit(sT, cur, sP, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
         __syncthreads();
 
-        const int slot = a.out_pos[node * d + idx];
-        if (MODE == MODE_PSPLIT) {
-            C* og = a.out + (size_t)slot * 2 * n2;
-            for (int i = threadIdx.x; i < 2 * n2; i += blockDim.x) og[i] = sP[i];
-        } else {
-            C tr = c_zero<C>();
-            for (int q = 0; q < chi; ++q) tr = c_add(tr, c_add(sP[q * chi + q], sP[n2 + q * chi + q]));
-            if (MODE == MODE_BP) {
-                const C* old = msgs_in + (size_t)slot * n2;
-                C* og = msgs_out + (size_t)slot * n2;
-                for (int i = threadIdx.x; i < n2; i += blockDim.x) {
-                    const C m = c_div(c_add(sP[i], sP[n2 + i]), tr);
-                    const C o = old[i];
-                    og[i] = m;
-                    num2 = fmax(num2, c_abs2(c_sub(m, o)));
-                    den2 = fmax(den2, c_abs2(c_add(m, o)));
-                }
-            } else {  // MODE_EXT
-                const HalfZZ<R> h = half_zz<R>(a.edge_ampl[node * d + idx] * a.ztime);
-                const C ae[2] = {h.a0, h.a1};
-                const R scale = c_abs2(h.a0) + c_abs2(h.a1);
-                const C trx = c_scale(tr, scale);
-                const int n = 2 * chi;
-                C* og = a.out + (size_t)slot * n * n;
-                for (int o = threadIdx.x; o < n * n; o += blockDim.x) {
-                    const int row = o / n, col = o - row * n;
-                    const int e = row >= chi, f = col >= chi;
-                    const int ia = row - e * chi, ib = col - f * chi;
-                    const C p0 = sP[ia * chi + ib], p1 = sP[n2 + ia * chi + ib];
-                    const C pe = ((e + f) & 1) ? c_sub(p0, p1) : c_add(p0, p1);
-                    const C coef = c_mul(c_conj(ae[e]), ae[f]);
-                    og[o] = c_div(c_mul(coef, pe), trx);
-                }
-            }
-        }
+        write_outputs<MODE, R>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
         __syncthreads();
     }
     if (MODE == MODE_BP) {
@@ -210,9 +231,106 @@ __global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
     }
 }
 
+
+// Register-tiled complex64 kernel for compile-time (D, CHI), BP and extended messages.
+template <int D, int CHI, int MODE>
+__global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kernel(NodeArgs<float> a) {
+    using S = tiled::Shape<D, CHI>;
+    static_assert(CHI % 4 == 0, "tiled kernel needs chi % 4 == 0");
+    static_assert(S::CLOSE_TILES <= S::THREADS, "close tiles exceed the block");
+    constexpr int NT = S::NT, N2 = S::N2, PER_S = S::PER_S, TH = S::THREADS;
+    extern __shared__ double4 smem_raw[];
+    float2* sT = reinterpret_cast<float2*>(smem_raw);
+    float2* sA = sT + NT;
+    float2* sB = sA + NT;
+    float2* sMt = sB + NT;
+    float2* sP = sMt + D * N2;
+    float* sRed = reinterpret_cast<float*>(sP + 2 * N2);
+
+    const float2* msgs_in = a.msgs_a;
+    float2* msgs_out = a.msgs_b;
+    if (MODE == MODE_BP && a.loop_state != nullptr) {
+        if (a.loop_state[0]) return;
+        if (a.loop_state[2]) { msgs_in = a.msgs_b; msgs_out = const_cast<float2*>(a.msgs_a); }
+    }
+    const int node = blockIdx.x;
+    {
+        const float4* tg = reinterpret_cast<const float4*>(a.tensors + (size_t)node * NT);
+        float4* st = reinterpret_cast<float4*>(sT);
+        for (int i = threadIdx.x; i < NT / 2; i += TH) st[i] = tg[i];
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
+        for (int o = threadIdx.x; o < N2; o += TH) {
+            const int i = o / CHI, j = o - i * CHI;
+            sMt[k * N2 + j * CHI + i] = mg[o];
+        }
+    }
+    __syncthreads();
+
+    float num2 = 0.f, den2 = 0.f;
+#pragma unroll 1
+    for (int idx = 0; idx < D; ++idx) {
+        const float2* cur = sT;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            if (k == idx) continue;
+            float2* nxt = (cur == sA) ? sB : sA;
+            if (k == D - 1)
+                tiled::product_last<CHI, TH>(cur, nxt, sMt + k * N2, 2 * tiled::cpow(CHI, D - 1));
+            else
+                tiled::product_inner<CHI, TH>(cur, nxt, sMt + k * N2, 2 * ipow(CHI, k), ipow(CHI, D - 1 - k));
+            __syncthreads();
+            cur = nxt;
+        }
+        tiled::close_tiled<CHI, TH, S::KS, PER_S>(sT, cur, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
+        __syncthreads();
+        write_outputs<MODE, float>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
+        __syncthreads();
+    }
+    if (MODE == MODE_BP) {
+        num2 = block_max(num2, sRed);
+        den2 = block_max(den2, sRed);
+        if (threadIdx.x == 0) {
+            atomic_max_nonneg(a.dist_parts, num2);
+            atomic_max_nonneg(a.dist_parts + 1, den2);
+        }
+    }
+}
+
+template <int D, int CHI, int MODE>
+static int launch_tiled(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    using S = tiled::Shape<D, CHI>;
+    const size_t smem = (size_t)S::SMEM_ELEMS * sizeof(float2);
+    int rc = ensure_smem((const void*)tiled_node_kernel<D, CHI, MODE>, smem, "tiled node kernel");
+    if (rc) return rc;
+    tiled_node_kernel<D, CHI, MODE><<<count, S::THREADS, smem, st>>>(args);
+    return check_launch("tiled node kernel");
+}
+
+// (degree, chi) pairs with a register-tiled complex64 kernel; 1 if launched, 0 if not covered
+template <int MODE>
+static int try_tiled(const NodeArgs<float>& a, int count, cudaStream_t st, int* rc) {
+    const int d = a.d, chi = a.chi;
+#define BQA_TILED(DD, CC) \
+    if (d == DD && chi == CC) { *rc = launch_tiled<DD, CC, MODE>(a, count, st); return 1; }
+    BQA_TILED(2, 8) BQA_TILED(2, 12) BQA_TILED(2, 16)
+    BQA_TILED(3, 4) BQA_TILED(3, 8) BQA_TILED(3, 12) BQA_TILED(3, 16)
+    BQA_TILED(4, 4) BQA_TILED(4, 8)
+#undef BQA_TILED
+    return 0;
+}
+
 template <int MODE, typename R>
 static int launch_node_mode(const NodeArgs<R>& args, int count, cudaStream_t st) {
     const int chi = args.chi, d = args.d;
+    if constexpr (sizeof(R) == 4 && (MODE == MODE_BP || MODE == MODE_EXT)) {
+        if (g_use_tiled) {
+            int rc = BQA_OK;
+            if (try_tiled<MODE>(args, count, st, &rc)) return rc;
+        }
+    }
     const size_t smem = node_smem_elems(d, chi) * sizeof(typename Cx<R>::T);
     const int fib = 2 * ipow(chi, d > 0 ? d - 1 : 0);
     int threads = ((max(fib, 2 * chi * chi) + 31) / 32) * 32;

@@ -1,0 +1,208 @@
+// Register-tiled complex64 node contraction for compile-time (degree D, bond dim CHI),
+// CHI a multiple of 4.  Same mathematics as node_kernel (node_kernels.cu), organised as
+// small GEMMs on shared-memory operands:
+//
+//   bond product on bond k:   Y[a][i][b] = sum_j M[i][j] X[a][j][b]
+//       A = 2 CHI^k rows (s included), B = CHI^(D-1-k) columns.  A thread owns a 4x4 tile of
+//       complex accumulators: 4 values of i times 4 of b (B >= 4), or 4 of a times 4 of i on
+//       the last bond (B = 1).  Operands come in as 128-bit loads (two complex values) from
+//       the tensor and from the transposed message Mt[j][i] = M[i][j].
+//   closing contraction for bond idx:
+//       P_s[a][b] = sum_{x,y} conj(T[s][x][a][y]) R[s][x][b][y]
+//       a thread owns a 4x4 tile of (a, b) for one K-slice; the KS slices of a tile sit in
+//       adjacent lanes and are summed with xor-shuffles.
+//
+// Per node and sweep that is d^2 units of 2 CHI^(d+1) complex MACs (d-1 bond products and
+// one closing contraction per outgoing message), as in the reference order of operations.
+#pragma once
+
+#include "common.cuh"
+
+namespace bqa {
+namespace tiled {
+
+__host__ __device__ constexpr int cpow(int b, int e) { return e == 0 ? 1 : b * cpow(b, e - 1); }
+
+template <int D, int CHI>
+struct Shape {
+    static constexpr int PER_S = cpow(CHI, D);
+    static constexpr int NT = 2 * PER_S;
+    static constexpr int N2 = CHI * CHI;
+    static constexpr int PROD_TILES = 2 * (CHI / 4) * (cpow(CHI, D - 1) / 4 > 0 ? cpow(CHI, D - 1) / 4 : 1);
+    static constexpr int THREADS = ((PROD_TILES + 31) / 32) * 32 > 256 ? 256 : ((PROD_TILES + 31) / 32) * 32;
+    static constexpr int CLOSE_TILES = 2 * (CHI / 4) * (CHI / 4);
+    static constexpr int KS_RAW = THREADS / CLOSE_TILES;
+    static constexpr int KS = KS_RAW >= 32 ? 32 : (KS_RAW >= 16 ? 16 : (KS_RAW >= 8 ? 8 : (KS_RAW >= 4 ? 4 : (KS_RAW >= 2 ? 2 : 1))));
+    // shared memory (float2 elements): T, two buffers, D transposed messages, P (2 blocks), scratch
+    static constexpr int SMEM_ELEMS = 3 * NT + D * N2 + 2 * N2 + 128;
+};
+
+__device__ __forceinline__ void ld2(const float2* p, float2& a, float2& b) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a = make_float2(v.x, v.y);
+    b = make_float2(v.z, v.w);
+}
+__device__ __forceinline__ void st2(float2* p, float2 a, float2 b) {
+    *reinterpret_cast<float4*>(p) = make_float4(a.x, a.y, b.x, b.y);
+}
+
+// Y[a][i][b] = sum_j Mt[j][i] X[a][j][b], B >= 4 (B a multiple of 4)
+template <int CHI, int THREADS>
+__device__ __forceinline__ void product_inner(const float2* __restrict__ X, float2* __restrict__ Y,
+                                              const float2* __restrict__ Mt, int A, int B) {
+    constexpr int NIG = CHI / 4;
+    const int nbg = B >> 2;
+    const int tiles = A * NIG * nbg;
+    for (int t = threadIdx.x; t < tiles; t += THREADS) {
+        const int bg = t % nbg;
+        const int rest = t / nbg;
+        const int ig = rest % NIG;
+        const int a = rest / NIG;
+        float2 acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+        const float2* xp = X + (size_t)a * CHI * B + bg * 4;
+        const float2* mp = Mt + ig * 4;
+#pragma unroll 4
+        for (int j = 0; j < CHI; ++j) {
+            float2 x[4], m[4];
+            ld2(xp + (size_t)j * B, x[0], x[1]);
+            ld2(xp + (size_t)j * B + 2, x[2], x[3]);
+            ld2(mp + j * CHI, m[0], m[1]);
+            ld2(mp + j * CHI + 2, m[2], m[3]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = c_fma(m[u], x[v], acc[u][v]);
+        }
+        float2* yp = Y + ((size_t)a * CHI + ig * 4) * B + bg * 4;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            st2(yp + (size_t)u * B, acc[u][0], acc[u][1]);
+            st2(yp + (size_t)u * B + 2, acc[u][2], acc[u][3]);
+        }
+    }
+}
+
+// Y[a][i] = sum_j X[a][j] Mt[j][i]  (product on the last bond, B = 1)
+template <int CHI, int THREADS>
+__device__ __forceinline__ void product_last(const float2* __restrict__ X, float2* __restrict__ Y,
+                                             const float2* __restrict__ Mt, int A) {
+    constexpr int NIG = CHI / 4;
+    const int tiles = (A >> 2) * NIG;
+    for (int t = threadIdx.x; t < tiles; t += THREADS) {
+        const int ig = t % NIG;
+        const int a0 = (t / NIG) * 4;
+        float2 acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+        const float2* xp = X + (size_t)a0 * CHI;
+        const float2* mp = Mt + ig * 4;
+#pragma unroll 2
+        for (int j = 0; j < CHI; j += 2) {
+            float2 x[4][2], m0[4], m1[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) ld2(xp + u * CHI + j, x[u][0], x[u][1]);
+            ld2(mp + j * CHI, m0[0], m0[1]);
+            ld2(mp + j * CHI + 2, m0[2], m0[3]);
+            ld2(mp + (j + 1) * CHI, m1[0], m1[1]);
+            ld2(mp + (j + 1) * CHI + 2, m1[2], m1[3]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    acc[u][v] = c_fma(x[u][0], m0[v], acc[u][v]);
+                    acc[u][v] = c_fma(x[u][1], m1[v], acc[u][v]);
+                }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            float2* yp = Y + (size_t)(a0 + u) * CHI + ig * 4;
+            st2(yp, acc[u][0], acc[u][1]);
+            st2(yp + 2, acc[u][2], acc[u][3]);
+        }
+    }
+}
+
+// P[s][a][b] = sum_{x<Ax, y<B} conj(T[s][x][a][y]) R[s][x][b][y]; per s the operands are
+// [Ax][CHI][B] with Ax * CHI * B = PER_S.  Result written to P[2][CHI][CHI].
+template <int CHI, int THREADS, int KS, int PER_S>
+__device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const float2* __restrict__ Rt,
+                                            float2* __restrict__ P, int Ax, int B) {
+    constexpr int NG = CHI / 4;
+    constexpr int TILES = 2 * NG * NG;
+    const int t = threadIdx.x;
+    const int ks = t % KS;
+    const int tile = t / KS;
+    const bool active = tile < TILES;
+    const int s = active ? tile / (NG * NG) : 0;
+    const int ag = (tile / NG) % NG, bg = tile % NG;
+    float2 acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+    const float2* tb = T + (size_t)s * PER_S + ag * 4 * B;
+    const float2* rb = Rt + (size_t)s * PER_S + bg * 4 * B;
+    if (active) {
+        if (B >= 2) {
+            // K runs over (x, y) in pairs of y
+            const int hb = B >> 1;
+            const int K2 = Ax * hb;
+            for (int p = ks; p < K2; p += KS) {
+                const int x = p / hb, y = (p - x * hb) * 2;
+                const size_t off = (size_t)x * CHI * B + y;
+                float2 tv[4][2], rv[4][2];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) ld2(tb + off + (size_t)u * B, tv[u][0], tv[u][1]);
+#pragma unroll
+                for (int v = 0; v < 4; ++v) ld2(rb + off + (size_t)v * B, rv[v][0], rv[v][1]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        acc[u][v] = c_fma_conj(tv[u][0], rv[v][0], acc[u][v]);
+                        acc[u][v] = c_fma_conj(tv[u][1], rv[v][1], acc[u][v]);
+                    }
+            }
+        } else {
+            // last bond: operands [Ax][CHI]; rows x, 4 consecutive a / b per thread
+            for (int x = ks; x < Ax; x += KS) {
+                float2 tv[4], rv[4];
+                ld2(tb + (size_t)x * CHI, tv[0], tv[1]);
+                ld2(tb + (size_t)x * CHI + 2, tv[2], tv[3]);
+                ld2(rb + (size_t)x * CHI, rv[0], rv[1]);
+                ld2(rb + (size_t)x * CHI + 2, rv[2], rv[3]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) acc[u][v] = c_fma_conj(tv[u], rv[v], acc[u][v]);
+            }
+        }
+    }
+    // sum the KS slices (adjacent lanes)
+#pragma unroll
+    for (int off = KS / 2; off > 0; off >>= 1) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                acc[u][v].x += __shfl_xor_sync(BQA_FULL_MASK, acc[u][v].x, off);
+                acc[u][v].y += __shfl_xor_sync(BQA_FULL_MASK, acc[u][v].y, off);
+            }
+    }
+    if (active && ks == 0) {
+        float2* pp = P + (size_t)s * CHI * CHI;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) pp[(ag * 4 + u) * CHI + bg * 4 + v] = acc[u][v];
+    }
+}
+
+}  // namespace tiled
+}  // namespace bqa

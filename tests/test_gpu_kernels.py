@@ -21,8 +21,11 @@ from bqa_gb300.engine import Annealer, _ptr  # noqa: E402
 from bqa_gb300.layout import build_context  # noqa: E402
 from oracle import bqa_oracle as orc  # noqa: E402
 
+# (case, bond dim): register-tiled kernels for (d, chi) in {2,3,4} x {4,8,12,16} (chi % 4 == 0
+# where built), the generic kernel elsewhere (mixed degrees up to 7, odd chi, degree 1)
 CASES = [("rr3_n16_chi4", 4), ("rr3_n24_chi8", 8), ("mixed_n18_chi3", 3), ("rr4_n20_chi4", 4),
-         ("rr3_n16_chi4", 16), ("grid3x4_chi4_damped", 5), ("tree9", 2)]
+         ("rr3_n16_chi4", 16), ("grid3x4_chi4_damped", 5), ("tree9", 2), ("grid3x4_chi4_damped", 8),
+         ("rr3_n24_chi8", 12), ("grid3x4_chi4_damped", 4)]
 RTOL = 2e-5
 
 
