@@ -10,8 +10,12 @@
 // with t = sign(zeta)/(|zeta| + sqrt(1+zeta^2)), zeta = (beta-alpha)/(2|gamma|),
 // c = 1/sqrt(1+t^2), s = c t, makes the pair orthogonal (the complex form of Hestenes'
 // method, Demmel & Veselic 1992).  At convergence A V = U Sigma with sigma_j = |a_j|.
-// A pair is rotated only if |gamma| > tol sqrt(alpha beta); sweeps stop when a whole sweep
-// rotates nothing in the warp, or at the sweep cap (then a status bit is set).
+// A pair is rotated only if |gamma| > tol sqrt(alpha beta) and |gamma| > eps |A|_F^2: the
+// second (absolute) test stops columns whose norm is below the precision of the matrix --
+// pure rounding noise, which would never pass the relative test -- from rotating forever;
+// it keeps the absolute accuracy eps |A| of the singular values, as LAPACK's.  Sweeps stop
+// when a whole sweep rotates nothing in the warp, or at the sweep cap (then a status bit is
+// set).
 #include "common.cuh"
 #include "internal.h"
 
@@ -34,6 +38,12 @@ template <int W, typename R>
 __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typename Cx<R>::T (&v)[W], int lane) {
     using C = typename Cx<R>::T;
     const R tol = (R)W * jacobi_eps<R>();
+    R fro2 = 0;
+#pragma unroll
+    for (int i = 0; i < W; ++i) fro2 += c_abs2(a[i]);
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) fro2 += __shfl_xor_sync(BQA_FULL_MASK, fro2, o, W);
+    const R floor_abs = jacobi_eps<R>() * fro2;
     const R tiny = sizeof(R) == 4 ? R(1e-30) : R(1e-280);
     for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
         int rotated = 0;
@@ -52,7 +62,7 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                 g = c_fma_conj(p, q, g);
             }
             const R gabs = sqrt(c_abs2(g));
-            const bool rot = alpha > tiny && beta > tiny && gabs > tol * sqrt(alpha) * sqrt(beta);
+            const bool rot = alpha > tiny && beta > tiny && gabs > tol * sqrt(alpha) * sqrt(beta) && gabs > floor_abs;
             R c = 1, s = 0;
             C eb = c_make(R(1), R(0));  // conj(e)
             if (rot) {

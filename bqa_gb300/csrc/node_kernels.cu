@@ -237,8 +237,9 @@ template <int D, int CHI, int MODE>
 __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kernel(NodeArgs<float> a) {
     using S = tiled::Shape<D, CHI>;
     static_assert(CHI % 4 == 0, "tiled kernel needs chi % 4 == 0");
+    static_assert(D >= 2 && D <= 4, "tiled kernel schedules cover degrees 2..4");
     static_assert(S::CLOSE_TILES <= S::THREADS, "close tiles exceed the block");
-    constexpr int NT = S::NT, N2 = S::N2, PER_S = S::PER_S, TH = S::THREADS;
+    constexpr int NT = S::NT, N2 = S::N2, PER_S = S::PER_S, TH = S::THREADS, SW = S::SW;
     extern __shared__ double4 smem_raw[];
     float2* sT = reinterpret_cast<float2*>(smem_raw);
     float2* sA = sT + NT;
@@ -256,8 +257,8 @@ __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kern
     const int node = blockIdx.x;
     {
         const float4* tg = reinterpret_cast<const float4*>(a.tensors + (size_t)node * NT);
-        float4* st = reinterpret_cast<float4*>(sT);
-        for (int i = threadIdx.x; i < NT / 2; i += TH) st[i] = tg[i];
+        for (int i = threadIdx.x; i < NT / 2; i += TH)
+            *reinterpret_cast<float4*>(sT + tiled::swz<SW>(2 * i)) = tg[i];
     }
 #pragma unroll
     for (int k = 0; k < D; ++k) {
@@ -270,24 +271,32 @@ __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kern
     __syncthreads();
 
     float num2 = 0.f, den2 = 0.f;
-#pragma unroll 1
-    for (int idx = 0; idx < D; ++idx) {
-        const float2* cur = sT;
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            if (k == idx) continue;
-            float2* nxt = (cur == sA) ? sB : sA;
-            if (k == D - 1)
-                tiled::product_last<CHI, TH>(cur, nxt, sMt + k * N2, 2 * tiled::cpow(CHI, D - 1));
-            else
-                tiled::product_inner<CHI, TH>(cur, nxt, sMt + k * N2, 2 * ipow(CHI, k), ipow(CHI, D - 1 - k));
-            __syncthreads();
-            cur = nxt;
-        }
-        tiled::close_tiled<CHI, TH, S::KS, PER_S>(sT, cur, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
+    auto prod = [&](const float2* X, float2* Y, int k) {
+        tiled::product<D, CHI, TH, SW>(X, Y, sMt + k * N2, k);
+        __syncthreads();
+    };
+    auto emit = [&](int idx, const float2* R) {
+        tiled::close_tiled<CHI, TH, S::KS, PER_S, SW>(sT, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
         __syncthreads();
         write_outputs<MODE, float>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
         __syncthreads();
+    };
+    if (D == 2) {
+        prod(sT, sA, 1); emit(0, sA);
+        prod(sT, sA, 0); emit(1, sA);
+    } else if (D == 3) {
+        prod(sT, sA, 0);                    // U = T x0
+        prod(sA, sB, 1); emit(2, sB);       // U x1
+        prod(sA, sB, 2); emit(1, sB);       // U x2
+        prod(sT, sA, 1);                    // T x1
+        prod(sA, sB, 2); emit(0, sB);       // (T x1) x2
+    } else {
+        prod(sT, sB, 0); prod(sB, sA, 1);   // U = T x0 x1
+        prod(sA, sB, 2); emit(3, sB);
+        prod(sA, sB, 3); emit(2, sB);
+        prod(sT, sB, 2); prod(sB, sA, 3);   // V = T x2 x3
+        prod(sA, sB, 0); emit(1, sB);
+        prod(sA, sB, 1); emit(0, sB);
     }
     if (MODE == MODE_BP) {
         num2 = block_max(num2, sRed);

@@ -12,8 +12,15 @@
 //       a thread owns a 4x4 tile of (a, b) for one K-slice; the KS slices of a tile sit in
 //       adjacent lanes and are summed with xor-shuffles.
 //
-// Per node and sweep that is d^2 units of 2 CHI^(d+1) complex MACs (d-1 bond products and
-// one closing contraction per outgoing message), as in the reference order of operations.
+// Tensor buffers in shared memory are XOR-swizzled in 16-byte chunks: element e lives at
+// e ^ (((e >> 4) & SW) << 1), SW = 7 for CHI = 16 and 3 for CHI = 8.  A 16-element row is
+// 128 bytes, so without the swizzle the same column of consecutive rows falls in one bank
+// group; with it, 8 consecutive rows hit 8 distinct groups, and every aligned pair of
+// complex values stays contiguous (bit 0 is untouched).
+//
+// The outgoing messages share bond products: with U = T x_0 M_0, the messages of bonds 2 and
+// 1 (D = 3) close U x_1 M_1 and U x_2 M_2, and bond 0 closes (T x_1 M_1) x_2 M_2: 5 products
+// and 3 closing contractions instead of 6 + 3 (D = 4: 8 + 4 instead of 12 + 4).
 #pragma once
 
 #include "common.cuh"
@@ -29,13 +36,18 @@ struct Shape {
     static constexpr int NT = 2 * PER_S;
     static constexpr int N2 = CHI * CHI;
     static constexpr int PROD_TILES = 2 * (CHI / 4) * (cpow(CHI, D - 1) / 4 > 0 ? cpow(CHI, D - 1) / 4 : 1);
-    static constexpr int THREADS = ((PROD_TILES + 31) / 32) * 32 > 256 ? 256 : ((PROD_TILES + 31) / 32) * 32;
+    static constexpr int R32 = ((PROD_TILES + 31) / 32) * 32;
+    static constexpr int THREADS = R32 > 512 ? 512 : R32;
     static constexpr int CLOSE_TILES = 2 * (CHI / 4) * (CHI / 4);
     static constexpr int KS_RAW = THREADS / CLOSE_TILES;
     static constexpr int KS = KS_RAW >= 32 ? 32 : (KS_RAW >= 16 ? 16 : (KS_RAW >= 8 ? 8 : (KS_RAW >= 4 ? 4 : (KS_RAW >= 2 ? 2 : 1))));
+    static constexpr int SW = CHI == 16 ? 7 : (CHI == 8 ? 3 : 0);
     // shared memory (float2 elements): T, two buffers, D transposed messages, P (2 blocks), scratch
     static constexpr int SMEM_ELEMS = 3 * NT + D * N2 + 2 * N2 + 128;
 };
+
+template <int SW>
+__device__ __forceinline__ int swz(int e) { return SW ? (e ^ (((e >> 4) & SW) << 1)) : e; }
 
 __device__ __forceinline__ void ld2(const float2* p, float2& a, float2& b) {
     const float4 v = *reinterpret_cast<const float4*>(p);
@@ -47,7 +59,7 @@ __device__ __forceinline__ void st2(float2* p, float2 a, float2 b) {
 }
 
 // Y[a][i][b] = sum_j Mt[j][i] X[a][j][b], B >= 4 (B a multiple of 4)
-template <int CHI, int THREADS>
+template <int CHI, int THREADS, int SW>
 __device__ __forceinline__ void product_inner(const float2* __restrict__ X, float2* __restrict__ Y,
                                               const float2* __restrict__ Mt, int A, int B) {
     constexpr int NIG = CHI / 4;
@@ -63,13 +75,14 @@ __device__ __forceinline__ void product_inner(const float2* __restrict__ X, floa
         for (int u = 0; u < 4; ++u)
 #pragma unroll
             for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
-        const float2* xp = X + (size_t)a * CHI * B + bg * 4;
+        const int xb = a * CHI * B + bg * 4;
         const float2* mp = Mt + ig * 4;
 #pragma unroll 4
         for (int j = 0; j < CHI; ++j) {
             float2 x[4], m[4];
-            ld2(xp + (size_t)j * B, x[0], x[1]);
-            ld2(xp + (size_t)j * B + 2, x[2], x[3]);
+            const int e = xb + j * B;
+            ld2(X + swz<SW>(e), x[0], x[1]);
+            ld2(X + swz<SW>(e + 2), x[2], x[3]);
             ld2(mp + j * CHI, m[0], m[1]);
             ld2(mp + j * CHI + 2, m[2], m[3]);
 #pragma unroll
@@ -77,17 +90,17 @@ __device__ __forceinline__ void product_inner(const float2* __restrict__ X, floa
 #pragma unroll
                 for (int v = 0; v < 4; ++v) acc[u][v] = c_fma(m[u], x[v], acc[u][v]);
         }
-        float2* yp = Y + ((size_t)a * CHI + ig * 4) * B + bg * 4;
+        const int yb = (a * CHI + ig * 4) * B + bg * 4;
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            st2(yp + (size_t)u * B, acc[u][0], acc[u][1]);
-            st2(yp + (size_t)u * B + 2, acc[u][2], acc[u][3]);
+            st2(Y + swz<SW>(yb + u * B), acc[u][0], acc[u][1]);
+            st2(Y + swz<SW>(yb + u * B + 2), acc[u][2], acc[u][3]);
         }
     }
 }
 
 // Y[a][i] = sum_j X[a][j] Mt[j][i]  (product on the last bond, B = 1)
-template <int CHI, int THREADS>
+template <int CHI, int THREADS, int SW>
 __device__ __forceinline__ void product_last(const float2* __restrict__ X, float2* __restrict__ Y,
                                              const float2* __restrict__ Mt, int A) {
     constexpr int NIG = CHI / 4;
@@ -100,13 +113,12 @@ __device__ __forceinline__ void product_last(const float2* __restrict__ X, float
         for (int u = 0; u < 4; ++u)
 #pragma unroll
             for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
-        const float2* xp = X + (size_t)a0 * CHI;
         const float2* mp = Mt + ig * 4;
 #pragma unroll 2
         for (int j = 0; j < CHI; j += 2) {
             float2 x[4][2], m0[4], m1[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) ld2(xp + u * CHI + j, x[u][0], x[u][1]);
+            for (int u = 0; u < 4; ++u) ld2(X + swz<SW>((a0 + u) * CHI + j), x[u][0], x[u][1]);
             ld2(mp + j * CHI, m0[0], m0[1]);
             ld2(mp + j * CHI + 2, m0[2], m0[3]);
             ld2(mp + (j + 1) * CHI, m1[0], m1[1]);
@@ -121,16 +133,25 @@ __device__ __forceinline__ void product_last(const float2* __restrict__ X, float
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            float2* yp = Y + (size_t)(a0 + u) * CHI + ig * 4;
-            st2(yp, acc[u][0], acc[u][1]);
-            st2(yp + 2, acc[u][2], acc[u][3]);
+            const int yb = (a0 + u) * CHI + ig * 4;
+            st2(Y + swz<SW>(yb), acc[u][0], acc[u][1]);
+            st2(Y + swz<SW>(yb + 2), acc[u][2], acc[u][3]);
         }
     }
 }
 
+// Bond product on bond k of a [2][CHI]^D buffer.
+template <int D, int CHI, int THREADS, int SW>
+__device__ __forceinline__ void product(const float2* X, float2* Y, const float2* Mt, int k) {
+    if (k == D - 1)
+        product_last<CHI, THREADS, SW>(X, Y, Mt, 2 * cpow(CHI, D - 1));
+    else
+        product_inner<CHI, THREADS, SW>(X, Y, Mt, 2 * ipow(CHI, k), ipow(CHI, D - 1 - k));
+}
+
 // P[s][a][b] = sum_{x<Ax, y<B} conj(T[s][x][a][y]) R[s][x][b][y]; per s the operands are
 // [Ax][CHI][B] with Ax * CHI * B = PER_S.  Result written to P[2][CHI][CHI].
-template <int CHI, int THREADS, int KS, int PER_S>
+template <int CHI, int THREADS, int KS, int PER_S, int SW>
 __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const float2* __restrict__ Rt,
                                             float2* __restrict__ P, int Ax, int B) {
     constexpr int NG = CHI / 4;
@@ -146,8 +167,8 @@ __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const 
     for (int u = 0; u < 4; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
-    const float2* tb = T + (size_t)s * PER_S + ag * 4 * B;
-    const float2* rb = Rt + (size_t)s * PER_S + bg * 4 * B;
+    const int tb = s * PER_S + ag * 4 * B;
+    const int rb = s * PER_S + bg * 4 * B;
     if (active) {
         if (B >= 2) {
             // K runs over (x, y) in pairs of y
@@ -155,12 +176,12 @@ __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const 
             const int K2 = Ax * hb;
             for (int p = ks; p < K2; p += KS) {
                 const int x = p / hb, y = (p - x * hb) * 2;
-                const size_t off = (size_t)x * CHI * B + y;
+                const int off = x * CHI * B + y;
                 float2 tv[4][2], rv[4][2];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) ld2(tb + off + (size_t)u * B, tv[u][0], tv[u][1]);
+                for (int u = 0; u < 4; ++u) ld2(T + swz<SW>(tb + off + u * B), tv[u][0], tv[u][1]);
 #pragma unroll
-                for (int v = 0; v < 4; ++v) ld2(rb + off + (size_t)v * B, rv[v][0], rv[v][1]);
+                for (int v = 0; v < 4; ++v) ld2(Rt + swz<SW>(rb + off + v * B), rv[v][0], rv[v][1]);
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -173,10 +194,10 @@ __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const 
             // last bond: operands [Ax][CHI]; rows x, 4 consecutive a / b per thread
             for (int x = ks; x < Ax; x += KS) {
                 float2 tv[4], rv[4];
-                ld2(tb + (size_t)x * CHI, tv[0], tv[1]);
-                ld2(tb + (size_t)x * CHI + 2, tv[2], tv[3]);
-                ld2(rb + (size_t)x * CHI, rv[0], rv[1]);
-                ld2(rb + (size_t)x * CHI + 2, rv[2], rv[3]);
+                ld2(T + swz<SW>(tb + x * CHI), tv[0], tv[1]);
+                ld2(T + swz<SW>(tb + x * CHI + 2), tv[2], tv[3]);
+                ld2(Rt + swz<SW>(rb + x * CHI), rv[0], rv[1]);
+                ld2(Rt + swz<SW>(rb + x * CHI + 2), rv[2], rv[3]);
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
 #pragma unroll

@@ -262,6 +262,9 @@ class Annealer:
                      dt, eps, _ptr(canon), _ptr(self.lmbds), _ptr(self.colmax), _ptr(self.status), st)
         # global truncation (src/bqa/backends.py:297-303)
         max_l = self.colmax[:n].view(self.lmbds.dtype).cpu().numpy().astype(np.float64)
+        if int(self.status.item()):
+            log.warning("a Jacobi SVD of the truncation step hit its sweep cap")
+            self.status.zero_()
         rank = n - int(np.sum(max_l < eps))
         dim = min(rank, ctx.max_bond_dim)
         err = float(np.sqrt(np.sum(max_l[dim:] ** 2)))
