@@ -10,12 +10,14 @@
 // with t = sign(zeta)/(|zeta| + sqrt(1+zeta^2)), zeta = (beta-alpha)/(2|gamma|),
 // c = 1/sqrt(1+t^2), s = c t, makes the pair orthogonal (the complex form of Hestenes'
 // method, Demmel & Veselic 1992).  At convergence A V = U Sigma with sigma_j = |a_j|.
-// A pair is rotated only if |gamma| > tol sqrt(alpha beta) and |gamma| > eps |A|_F^2: the
-// second (absolute) test stops columns whose norm is below the precision of the matrix --
-// pure rounding noise, which would never pass the relative test -- from rotating forever;
-// it keeps the absolute accuracy eps |A| of the singular values, as LAPACK's.  Sweeps stop
-// when a whole sweep rotates nothing in the warp, or at the sweep cap (then a status bit is
-// set).
+// A pair is rotated only if |gamma| > tol sqrt(alpha beta) and both columns are above the
+// noise level of the matrix, |a|^2 > W eps^2 |A|_F^2.  Columns below it are rounding noise
+// (the remains of dependent columns); their mutual products never pass the relative test,
+// so without the freeze they would rotate among themselves until the sweep cap.  A frozen
+// column has sigma < sqrt(W) eps |A|_F, below every threshold the callers apply to these
+// matrices (pinv_eps on trace-normalised messages, 1e-6 on normalised bond spectra), so no
+// keep/drop decision changes.  Sweeps stop when a whole sweep rotates nothing in the warp,
+// or at the sweep cap (then a status bit is set).
 #include "common.cuh"
 #include "internal.h"
 
@@ -43,8 +45,7 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
     for (int i = 0; i < W; ++i) fro2 += c_abs2(a[i]);
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) fro2 += __shfl_xor_sync(BQA_FULL_MASK, fro2, o, W);
-    const R floor_abs = jacobi_eps<R>() * fro2;
-    const R tiny = sizeof(R) == 4 ? R(1e-30) : R(1e-280);
+    const R col_floor = fmax((R)W * jacobi_eps<R>() * jacobi_eps<R>() * fro2, sizeof(R) == 4 ? R(1e-30) : R(1e-280));
     for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
         int rotated = 0;
 #pragma unroll 1
@@ -62,7 +63,7 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                 g = c_fma_conj(p, q, g);
             }
             const R gabs = sqrt(c_abs2(g));
-            const bool rot = alpha > tiny && beta > tiny && gabs > tol * sqrt(alpha) * sqrt(beta) && gabs > floor_abs;
+            const bool rot = alpha > col_floor && beta > col_floor && gabs > tol * sqrt(alpha) * sqrt(beta);
             R c = 1, s = 0;
             C eb = c_make(R(1), R(0));  // conj(e)
             if (rot) {
