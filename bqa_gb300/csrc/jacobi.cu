@@ -10,14 +10,13 @@
 // with t = sign(zeta)/(|zeta| + sqrt(1+zeta^2)), zeta = (beta-alpha)/(2|gamma|),
 // c = 1/sqrt(1+t^2), s = c t, makes the pair orthogonal (the complex form of Hestenes'
 // method, Demmel & Veselic 1992).  At convergence A V = U Sigma with sigma_j = |a_j|.
-// A pair is rotated only if |gamma| > tol sqrt(alpha beta) and both columns are above the
-// noise level of the matrix, |a|^2 > W eps^2 |A|_F^2.  Columns below it are rounding noise
-// (the remains of dependent columns); their mutual products never pass the relative test,
-// so without the freeze they would rotate among themselves until the sweep cap.  A frozen
-// column has sigma < sqrt(W) eps |A|_F, below every threshold the callers apply to these
-// matrices (pinv_eps on trace-normalised messages, 1e-6 on normalised bond spectra), so no
-// keep/drop decision changes.  Sweeps stop when a whole sweep rotates nothing in the warp,
-// or at the sweep cap (then a status bit is set).
+// A pair is rotated if |gamma| > tol sqrt(alpha beta).  Sweeps stop when a whole sweep
+// rotates no pair of SIGNIFICANT columns in the warp (both above the noise level of the
+// matrix, |a|^2 > W eps^2 |A|_F^2), or at the sweep cap (then a status bit is set).
+// Columns below that level are rounding noise (the remains of dependent columns): their
+// mutual products never pass the relative test, so they would keep the loop going until
+// the cap; they are still rotated like every other pair while the loop runs, so the
+// orthogonalisation of the significant columns against them is untouched.
 #include "common.cuh"
 #include "internal.h"
 
@@ -36,7 +35,7 @@ __device__ __forceinline__ C shfl_xor_c(C v, int r, int w) {
     return v;
 }
 
-template <int W, typename R>
+template <int W, typename R, bool WITH_V>
 __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typename Cx<R>::T (&v)[W], int lane) {
     using C = typename Cx<R>::T;
     const R tol = (R)W * jacobi_eps<R>();
@@ -63,7 +62,7 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                 g = c_fma_conj(p, q, g);
             }
             const R gabs = sqrt(c_abs2(g));
-            const bool rot = alpha > col_floor && beta > col_floor && gabs > tol * sqrt(alpha) * sqrt(beta);
+            const bool rot = alpha > R(0) && beta > R(0) && gabs > tol * sqrt(alpha) * sqrt(beta);
             R c = 1, s = 0;
             C eb = c_make(R(1), R(0));  // conj(e)
             if (rot) {
@@ -72,7 +71,7 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                 c = R(1) / sqrt(fma(t, t, R(1)));
                 s = c * t;
                 eb = c_make(g.x / gabs, -g.y / gabs);
-                rotated = 1;
+                rotated |= (alpha > col_floor && beta > col_floor);
             }
 #pragma unroll
             for (int i = 0; i < W; ++i) {
@@ -81,12 +80,14 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                 const C q = c_mul(eb, low ? o : a[i]);
                 a[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
             }
+            if (WITH_V) {
 #pragma unroll
-            for (int i = 0; i < W; ++i) {
-                const C o = shfl_xor_c(v[i], r, W);
-                const C p = low ? v[i] : o;
-                const C q = c_mul(eb, low ? o : v[i]);
-                v[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
+                for (int i = 0; i < W; ++i) {
+                    const C o = shfl_xor_c(v[i], r, W);
+                    const C p = low ? v[i] : o;
+                    const C q = c_mul(eb, low ? o : v[i]);
+                    v[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
+                }
             }
         }
         if (!__any_sync(BQA_FULL_MASK, rotated)) return true;
@@ -102,7 +103,9 @@ __device__ __forceinline__ R seg_sum(R x) {
 }
 
 // m = U S Vh per matrix (masked at eps) -> lu = sqrt(S) Vh, ul = U pinv(sqrt(S))
-// (src/bqa/backends.py:483-490,709-727).
+// (src/bqa/backends.py:483-490,709-727).  The messages are Hermitian positive semidefinite,
+// so V = U on every singular value above the noise level (the rest are masked): the right
+// vectors are not accumulated, and u_j = a_j / sigma_j gives both factors.
 template <int W, typename R>
 __global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ lu,
@@ -112,13 +115,10 @@ __global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T
     const int mat = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = mat < count;
     const size_t base = (size_t)(live ? mat : 0) * n * n;
-    C a[W], v[W];
+    C a[W], v[1 > W ? 1 : W];
 #pragma unroll
-    for (int i = 0; i < W; ++i) {
-        a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
-        v[i] = c_make(i == lane ? R(1) : R(0), R(0));
-    }
-    const bool ok = jacobi_columns<W, R>(a, v, lane);
+    for (int i = 0; i < W; ++i) a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
+    const bool ok = jacobi_columns<W, R, false>(a, v, lane);
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
     R nrm2 = 0;
 #pragma unroll
@@ -127,13 +127,14 @@ __global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T
     const bool keep = sig > eps;
     const R sq = sqrt(sig);
     if (!live || lane >= n) return;
-    // row `lane` of lu = sqrt(sigma) * conj(v)^T ; column `lane` of ul = a / (sigma sqrt(sigma))
+    // u = a / sigma; row `lane` of lu = sqrt(sigma) conj(u)^T = conj(a) / sqrt(sigma);
+    // column `lane` of ul = u / sqrt(sigma) = a / (sigma sqrt(sigma))
     const R inv = keep ? R(1) / (sig * sq) : R(0);
-    const R sqk = keep ? sq : R(0);
+    const R linv = keep ? R(1) / sq : R(0);
 #pragma unroll
     for (int k = 0; k < W; ++k) {
         if (k < n) {
-            lu[base + (size_t)lane * n + k] = c_make(sqk * v[k].x, -sqk * v[k].y);
+            lu[base + (size_t)lane * n + k] = c_make(linv * a[k].x, -linv * a[k].y);
             ul[base + (size_t)k * n + lane] = c_scale(a[k], inv);
         }
     }
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(128) bond_canon_kernel(const typename Cx<R>::T
             v[i] = c_make(i == lane ? R(1) : R(0), R(0));
         }
     }
-    const bool ok = jacobi_columns<W, R>(a, v, lane);
+    const bool ok = jacobi_columns<W, R, true>(a, v, lane);
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
     R nrm2 = 0;
 #pragma unroll
