@@ -104,8 +104,9 @@ __device__ __forceinline__ R seg_sum(R x) {
 
 // m = U S Vh per matrix (masked at eps) -> lu = sqrt(S) Vh, ul = U pinv(sqrt(S))
 // (src/bqa/backends.py:483-490,709-727).  The messages are Hermitian positive semidefinite,
-// so V = U on every singular value above the noise level (the rest are masked): the right
-// vectors are not accumulated, and u_j = a_j / sigma_j gives both factors.
+// so U = V on every singular value above the noise level (the rest are masked); both factors
+// are built from the accumulated V, which stays unitary to working precision, while
+// a_j / sigma_j carries a relative error eps |m| / sigma_j for small sigma_j.
 template <int W, typename R>
 __global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ lu,
@@ -115,10 +116,13 @@ __global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T
     const int mat = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = mat < count;
     const size_t base = (size_t)(live ? mat : 0) * n * n;
-    C a[W], v[1 > W ? 1 : W];
+    C a[W], v[W];
 #pragma unroll
-    for (int i = 0; i < W; ++i) a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
-    const bool ok = jacobi_columns<W, R, false>(a, v, lane);
+    for (int i = 0; i < W; ++i) {
+        a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
+        v[i] = c_make(i == lane ? R(1) : R(0), R(0));
+    }
+    const bool ok = jacobi_columns<W, R, true>(a, v, lane);
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
     R nrm2 = 0;
 #pragma unroll
@@ -127,15 +131,14 @@ __global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T
     const bool keep = sig > eps;
     const R sq = sqrt(sig);
     if (!live || lane >= n) return;
-    // u = a / sigma; row `lane` of lu = sqrt(sigma) conj(u)^T = conj(a) / sqrt(sigma);
-    // column `lane` of ul = u / sqrt(sigma) = a / (sigma sqrt(sigma))
-    const R inv = keep ? R(1) / (sig * sq) : R(0);
-    const R linv = keep ? R(1) / sq : R(0);
+    // row `lane` of lu = sqrt(sigma) conj(v)^T ; column `lane` of ul = v / sqrt(sigma)
+    const R sqk = keep ? sq : R(0);
+    const R inv = keep ? R(1) / sq : R(0);
 #pragma unroll
     for (int k = 0; k < W; ++k) {
         if (k < n) {
-            lu[base + (size_t)lane * n + k] = c_make(linv * a[k].x, -linv * a[k].y);
-            ul[base + (size_t)k * n + lane] = c_scale(a[k], inv);
+            lu[base + (size_t)lane * n + k] = c_make(sqk * v[k].x, -sqk * v[k].y);
+            ul[base + (size_t)k * n + lane] = c_scale(v[k], inv);
         }
     }
 }
