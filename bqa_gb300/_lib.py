@@ -55,6 +55,8 @@ SIGNATURES = {
     "bqa_edge_zz": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p]),
     "bqa_project_nodes": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p,
                                     c_void_p]),
+    "bqa_canonicalize_noalloc": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,
+                                           c_void_p, c_void_p, c_void_p]),
 }
 
 

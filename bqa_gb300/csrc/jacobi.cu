@@ -17,6 +17,8 @@
 // mutual products never pass the relative test, so they would keep the loop going until
 // the cap; they are still rotated like every other pair while the loop runs, so the
 // orthogonalisation of the significant columns against them is untouched.
+#include <mutex>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -301,6 +303,89 @@ int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n,
     if (dtype == BQA_C64) return canon_dispatch<float>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
     if (dtype == BQA_C128) return canon_dispatch<double>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
     return set_error(BQA_ERR_ARG, "bqa_bond_canon: unknown dtype %d", dtype);
+}
+
+}  // extern "C"
+
+// ---- canonicalisation without caller scratch ------------------------------------------------
+//
+// bqa_canonicalize_noalloc runs the two kernels above (environment factors, then bond
+// canonicalisation) with the intermediate factors lu and ul placed in one file-scope device
+// array instead of caller-provided buffers.  It exists for callers that cannot allocate
+// device memory: host programs whose device heap belongs to an external pool allocator
+// (serving runtimes that reserve all free HBM at start-up), and pipelines that must not call
+// cudaMalloc/cudaFree because those synchronise the device.  Such a caller passes only the
+// inputs and outputs; the factors live in kNoAllocScratchBytes of device memory that every
+// GPU which loads this library holds until the process exits.
+//
+// The array's device address is looked up once per device, on the first call made with that
+// device current (cudaGetSymbolAddress; the host-side name of a __device__ array is not a
+// device address).  That first call therefore should come before any stream capture.  All
+// calls share the array and it keeps the previous call's contents; every element the kernels
+// read is written earlier in the same call, and nothing in it must start at zero.  Calls that
+// overlap on the GPU (different streams, or different host threads) race on the array.
+
+namespace bqa {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;   // 64 MiB: lu + ul
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static void* noalloc_scratch_address(int* rc) {
+    static std::mutex mu;
+    static void* addr[64] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { *rc = set_error(BQA_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); return nullptr; }
+    if (dev < 0 || dev >= 64) { *rc = set_error(BQA_ERR_UNSUPPORTED, "device ordinal %d >= 64", dev); return nullptr; }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            *rc = set_error(BQA_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+            return nullptr;
+        }
+        addr[dev] = p;
+    }
+    *rc = BQA_OK;
+    return addr[dev];
+}
+
+}  // namespace bqa
+
+extern "C" {
+
+int32_t bqa_canonicalize_noalloc(const void* ext_msgs, int32_t edges, int32_t n, int32_t dtype, double eps,
+                                 void* canon, void* lmbds, void* colmax, int32_t* status, void* stream) {
+    if (!ext_msgs || !canon || !lmbds || !colmax || !status || edges < 2 || n < 1)
+        return set_error(BQA_ERR_ARG, "bqa_canonicalize_noalloc: bad argument");
+    if (dtype != BQA_C64 && dtype != BQA_C128)
+        return set_error(BQA_ERR_ARG, "bqa_canonicalize_noalloc: unknown dtype %d", dtype);
+    if (n > 32) return set_error(BQA_ERR_UNSUPPORTED, "bqa_canonicalize_noalloc: matrix size %d > 32", n);
+    const size_t el = dtype == BQA_C64 ? 8 : 16;
+    const size_t one = (size_t)edges * n * n * el;
+    if (2 * one > kNoAllocScratchBytes)
+        return set_error(BQA_ERR_UNSUPPORTED,
+                         "bqa_canonicalize_noalloc: %d edges at n=%d need %zu bytes of factors, above the "
+                         "%zu-byte static scratch; use bqa_env_factor + bqa_bond_canon with caller buffers",
+                         edges, n, 2 * one, kNoAllocScratchBytes);
+    int rc = BQA_OK;
+    unsigned char* base = static_cast<unsigned char*>(noalloc_scratch_address(&rc));
+    if (rc) return rc;
+    void* lu = base;
+    void* ul = base + ((one + 255) & ~size_t(255));
+    cudaStream_t st = as_stream(stream);
+    const size_t colmax_bytes = (size_t)n * (dtype == BQA_C64 ? 4 : 8);
+    cudaError_t e = cudaMemsetAsync(colmax, 0, colmax_bytes, st);
+    if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "bqa_canonicalize_noalloc: %s", cudaGetErrorString(e));
+    if (dtype == BQA_C64) {
+        rc = env_dispatch<float>(ext_msgs, edges, n, eps, lu, ul, status, st);
+        if (rc) return rc;
+        return canon_dispatch<float>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    }
+    rc = env_dispatch<double>(ext_msgs, edges, n, eps, lu, ul, status, st);
+    if (rc) return rc;
+    return canon_dispatch<double>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
 }
 
 }  // extern "C"

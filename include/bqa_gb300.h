@@ -23,8 +23,8 @@
  *  - Every entry point returns a status (BQA_OK = 0).  No entry point aborts, and every
  *    device-side iteration is capped; a cap that is hit is reported through a device
  *    status word, never by spinning.
- *  - Scratch buffers are allocated by the caller and passed in; the library allocates
- *    no device memory.
+ *  - Scratch buffers are allocated by the caller and passed in; the library calls no
+ *    allocator (bqa_canonicalize_noalloc keeps its scratch in a static device array).
  */
 #ifndef BQA_GB300_H
 #define BQA_GB300_H
@@ -173,6 +173,22 @@ int32_t bqa_edge_zz(const void* pm, int32_t edges, int32_t chi, int32_t dtype, d
  */
 int32_t bqa_project_nodes(void* tensors, int32_t count, int32_t node_elems, int32_t dtype, const int32_t* positions,
                           const int32_t* outcomes, int32_t m, double* norm2_scratch, void* stream);
+
+/*
+ * bqa_env_factor followed by bqa_bond_canon with no caller scratch.  No counterpart in the
+ * reference: it serves callers that cannot allocate device memory (a host whose device heap
+ * belongs to an external pool allocator, or a pipeline that must avoid the device-wide
+ * synchronisation of cudaMalloc/cudaFree).  The factors lu and ul live in a 64 MiB static
+ * device array inside the library, held by every GPU that loads it until process exit, so
+ * 2 * edges * n^2 * sizeof(complex) must not exceed 64 MiB (BQA_ERR_UNSUPPORTED otherwise;
+ * e.g. 65,536 edges at n = 8 or 4,096 at n = 32 in complex64).  Inputs: ext_msgs[edges][n][n].
+ * Outputs as bqa_bond_canon (canon, lmbds, status bits OR-ed in); colmax is zeroed here
+ * before it is filled.  The first call on a device looks up the array's device address, so
+ * make it before any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race.
+ */
+int32_t bqa_canonicalize_noalloc(const void* ext_msgs, int32_t edges, int32_t n, int32_t dtype, double eps,
+                                 void* canon, void* lmbds, void* colmax, int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }
