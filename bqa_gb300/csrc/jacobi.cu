@@ -37,9 +37,25 @@ __device__ __forceinline__ C shfl_xor_c(C v, int r, int w) {
     return v;
 }
 
-template <int W, typename R, bool WITH_V>
-__device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typename Cx<R>::T (&v)[W], int lane) {
+// V lives in shared memory: the segment's W columns at a padded stride VS = W + 2 (complex
+// elements), so 128-bit column loads from 8 lanes at a time hit 8 distinct bank groups.
+// Two such blocks alternate (a rotation reads one and writes the other), so a lane never
+// holds a whole new column in registers.
+template <int W> struct VStride { static constexpr int VS = W + 2; static constexpr int BLOCK = W * VS; };
+
+// One-sided Jacobi on the segment's columns.  a: this lane's column (registers); sV: the
+// segment's two V blocks (shared), initialised to I here.  Returns the block holding V.
+template <int W, typename R>
+__device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typename Cx<R>::T* sV, int lane,
+                                               const typename Cx<R>::T** vfinal) {
     using C = typename Cx<R>::T;
+    constexpr int VS = VStride<W>::VS;
+    C* vcur = sV;
+    C* vnxt = sV + VStride<W>::BLOCK;
+#pragma unroll
+    for (int i = 0; i < W; ++i) vcur[lane * VS + i] = c_make(i == lane ? R(1) : R(0), R(0));
+    __syncwarp();
+    *vfinal = vcur;
     const R tol = (R)W * jacobi_eps<R>();
     R fro2 = 0;
 #pragma unroll
@@ -51,45 +67,71 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
         int rotated = 0;
 #pragma unroll 1
         for (int r = 1; r < W; ++r) {
-            const bool low = lane < (lane ^ r);
-            R alpha = 0, beta = 0;
-            C g = c_zero<C>();
+            const int partner = lane ^ r;
+            const bool low = lane < partner;
+            C o[W];
+            R alpha0 = 0, alpha1 = 0, beta0 = 0, beta1 = 0;
+            C g0 = c_zero<C>(), g1 = c_zero<C>();
 #pragma unroll
             for (int i = 0; i < W; ++i) {
-                const C o = shfl_xor_c(a[i], r, W);
-                const C p = low ? a[i] : o;
-                const C q = low ? o : a[i];
-                alpha = fma(p.x, p.x, fma(p.y, p.y, alpha));
-                beta = fma(q.x, q.x, fma(q.y, q.y, beta));
-                g = c_fma_conj(p, q, g);
+                o[i] = shfl_xor_c(a[i], r, W);
+                const C p = low ? a[i] : o[i];
+                const C q = low ? o[i] : a[i];
+                if (i & 1) {
+                    alpha1 = fma(p.x, p.x, fma(p.y, p.y, alpha1));
+                    beta1 = fma(q.x, q.x, fma(q.y, q.y, beta1));
+                    g1 = c_fma_conj(p, q, g1);
+                } else {
+                    alpha0 = fma(p.x, p.x, fma(p.y, p.y, alpha0));
+                    beta0 = fma(q.x, q.x, fma(q.y, q.y, beta0));
+                    g0 = c_fma_conj(p, q, g0);
+                }
             }
+            const R alpha = alpha0 + alpha1, beta = beta0 + beta1;
+            const C g = c_add(g0, g1);
             const R gabs = sqrt(c_abs2(g));
             const bool rot = alpha > R(0) && beta > R(0) && gabs > tol * sqrt(alpha) * sqrt(beta);
-            R c = 1, s = 0;
-            C eb = c_make(R(1), R(0));  // conj(e)
-            if (rot) {
-                const R zeta = (beta - alpha) / (R(2) * gabs);
-                const R t = copysign(R(1), zeta) / (fabs(zeta) + hypot(R(1), zeta));
-                c = R(1) / sqrt(fma(t, t, R(1)));
-                s = c * t;
-                eb = c_make(g.x / gabs, -g.y / gabs);
-                rotated |= (alpha > col_floor && beta > col_floor);
-            }
-#pragma unroll
-            for (int i = 0; i < W; ++i) {
-                const C o = shfl_xor_c(a[i], r, W);
-                const C p = low ? a[i] : o;
-                const C q = c_mul(eb, low ? o : a[i]);
-                a[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
-            }
-            if (WITH_V) {
+            // both lanes of a pair take the same branch (identical inputs and operand order)
+            if (__any_sync(BQA_FULL_MASK, rot)) {
+                R c = 1, s = 0;
+                C eb = c_make(R(1), R(0));  // conj(e)
+                if (rot) {
+                    const R zeta = (beta - alpha) / (R(2) * gabs);
+                    const R t = copysign(R(1), zeta) / (fabs(zeta) + hypot(R(1), zeta));
+                    c = R(1) / sqrt(fma(t, t, R(1)));
+                    s = c * t;
+                    eb = c_make(g.x / gabs, -g.y / gabs);
+                    rotated |= (alpha > col_floor && beta > col_floor);
+                }
 #pragma unroll
                 for (int i = 0; i < W; ++i) {
-                    const C o = shfl_xor_c(v[i], r, W);
-                    const C p = low ? v[i] : o;
-                    const C q = c_mul(eb, low ? o : v[i]);
-                    v[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
+                    const C p = low ? a[i] : o[i];
+                    const C q = c_mul(eb, low ? o[i] : a[i]);
+                    a[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
                 }
+                // V: read own and partner columns of the current block, write own of the next
+                const C* vown = vcur + lane * VS;
+                const C* vpart = vcur + partner * VS;
+                C* vout = vnxt + lane * VS;
+#pragma unroll
+                for (int i = 0; i < W; i += 2) {
+                    C vo0, vo1, vp0, vp1;
+                    if (sizeof(R) == 4) {
+                        const float4 x = *reinterpret_cast<const float4*>(vown + i);
+                        const float4 y = *reinterpret_cast<const float4*>(vpart + i);
+                        vo0 = c_make((R)x.x, (R)x.y); vo1 = c_make((R)x.z, (R)x.w);
+                        vp0 = c_make((R)y.x, (R)y.y); vp1 = c_make((R)y.z, (R)y.w);
+                    } else {
+                        vo0 = vown[i]; vo1 = vown[i + 1]; vp0 = vpart[i]; vp1 = vpart[i + 1];
+                    }
+                    const C p0 = low ? vo0 : vp0, p1 = low ? vo1 : vp1;
+                    const C q0 = c_mul(eb, low ? vp0 : vo0), q1 = c_mul(eb, low ? vp1 : vo1);
+                    vout[i] = low ? c_make(c * p0.x - s * q0.x, c * p0.y - s * q0.y) : c_make(s * p0.x + c * q0.x, s * p0.y + c * q0.y);
+                    vout[i + 1] = low ? c_make(c * p1.x - s * q1.x, c * p1.y - s * q1.y) : c_make(s * p1.x + c * q1.x, s * p1.y + c * q1.y);
+                }
+                __syncwarp();
+                C* t = vcur; vcur = vnxt; vnxt = t;
+                *vfinal = vcur;
             }
         }
         if (!__any_sync(BQA_FULL_MASK, rotated)) return true;
@@ -110,21 +152,23 @@ __device__ __forceinline__ R seg_sum(R x) {
 // are built from the accumulated V, which stays unitary to working precision, while
 // a_j / sigma_j carries a relative error eps |m| / sigma_j for small sigma_j.
 template <int W, typename R>
-__global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
+__global__ void __launch_bounds__(128, 3) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ lu,
                                                          typename Cx<R>::T* __restrict__ ul, int32_t* status) {
     using C = typename Cx<R>::T;
+    constexpr int VS = VStride<W>::VS;
+    extern __shared__ double4 smem_raw[];
     const int lane = threadIdx.x & (W - 1);
+    C* sV = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / W) * 2 * VStride<W>::BLOCK;
     const int mat = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = mat < count;
     const size_t base = (size_t)(live ? mat : 0) * n * n;
-    C a[W], v[W];
+    C a[W];
 #pragma unroll
-    for (int i = 0; i < W; ++i) {
-        a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
-        v[i] = c_make(i == lane ? R(1) : R(0), R(0));
-    }
-    const bool ok = jacobi_columns<W, R, true>(a, v, lane);
+    for (int i = 0; i < W; ++i) a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
+    const C* vblk;
+    const bool ok = jacobi_columns<W, R>(a, sV, lane, &vblk);
+    const C* v = vblk + lane * VS;
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
     R nrm2 = 0;
 #pragma unroll
@@ -148,16 +192,18 @@ __global__ void __launch_bounds__(128) env_factor_kernel(const typename Cx<R>::T
 // Per undirected edge p: ker = lu[p] lu[p+h]^T = us s vhs; lambdas; canonicalisers
 // (src/bqa/state.py:171-200).
 template <int W, typename R>
-__global__ void __launch_bounds__(128) bond_canon_kernel(const typename Cx<R>::T* __restrict__ lu,
+__global__ void __launch_bounds__(128, 3) bond_canon_kernel(const typename Cx<R>::T* __restrict__ lu,
                                                          const typename Cx<R>::T* __restrict__ ul, int edges, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ canon,
                                                          R* __restrict__ lmbds, typename Cx<R>::Bits* colmax,
                                                          int32_t* status) {
     using C = typename Cx<R>::T;
     extern __shared__ double4 smem_raw[];
+    constexpr int VS = VStride<W>::VS;
     const int lane = threadIdx.x & (W - 1);
     const int seg = threadIdx.x / W;
     C* sm = reinterpret_cast<C*>(smem_raw) + (size_t)seg * W * W;
+    C* sV = reinterpret_cast<C*>(smem_raw) + (size_t)128 * W + (size_t)seg * 2 * VStride<W>::BLOCK;
     const int half = edges / 2;
     const int p = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = p < half;
@@ -166,7 +212,7 @@ __global__ void __launch_bounds__(128) bond_canon_kernel(const typename Cx<R>::T
     // stage lu_f, then ker[:, lane] = lu_f . lu_b[lane, :]^T
     for (int i = lane; i < n * n; i += W) sm[i] = live ? lu[(size_t)pf * nn + i] : c_zero<C>();
     __syncwarp();
-    C a[W], v[W];
+    C a[W];
     {
         C brow[W];
 #pragma unroll
@@ -181,10 +227,11 @@ __global__ void __launch_bounds__(128) bond_canon_kernel(const typename Cx<R>::T
                     if (k < n) acc = c_fma(sm[i * n + k], brow[k], acc);
             }
             a[i] = acc;
-            v[i] = c_make(i == lane ? R(1) : R(0), R(0));
         }
     }
-    const bool ok = jacobi_columns<W, R, true>(a, v, lane);
+    const C* vblk;
+    const bool ok = jacobi_columns<W, R>(a, sV, lane, &vblk);
+    const C* v = vblk + lane * VS;
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
     R nrm2 = 0;
 #pragma unroll
@@ -240,8 +287,11 @@ static int launch_env(const void* m, int count, int n, double eps, void* lu, voi
     using C = typename Cx<R>::T;
     const int per_block = 128 / W;
     const int blocks = (count + per_block - 1) / per_block;
-    env_factor_kernel<W, R><<<blocks, 128, 0, st>>>(static_cast<const C*>(m), count, n, (R)eps, static_cast<C*>(lu),
-                                                    static_cast<C*>(ul), status);
+    const size_t smem = (size_t)(128 / W) * 2 * VStride<W>::BLOCK * sizeof(C);
+    int rc = ensure_smem((const void*)env_factor_kernel<W, R>, smem, "env_factor");
+    if (rc) return rc;
+    env_factor_kernel<W, R><<<blocks, 128, smem, st>>>(static_cast<const C*>(m), count, n, (R)eps,
+                                                       static_cast<C*>(lu), static_cast<C*>(ul), status);
     return check_launch("env_factor");
 }
 
@@ -252,7 +302,7 @@ static int launch_canon(const void* lu, const void* ul, int edges, int n, double
     const int per_block = 128 / W;
     const int half = edges / 2;
     const int blocks = (half + per_block - 1) / per_block;
-    const size_t smem = (size_t)128 * W * sizeof(C);
+    const size_t smem = ((size_t)128 * W + (size_t)(128 / W) * 2 * VStride<W>::BLOCK) * sizeof(C);
     int rc = ensure_smem((const void*)bond_canon_kernel<W, R>, smem, "bond_canon");
     if (rc) return rc;
     bond_canon_kernel<W, R><<<blocks, 128, smem, st>>>(static_cast<const C*>(lu), static_cast<const C*>(ul), edges, n,
