@@ -319,7 +319,8 @@ def run_sweep_mode(args) -> None:
         c.tensors[0][:size].copy_((t / t.norm(dim=1, keepdim=True)).view(-1))
     eye = torch.eye(chi, dtype=job.msgs[0].dtype, device="cuda") / chi
     job.msgs[0][: ctx.edges_number * chi * chi].copy_(eye.expand(ctx.edges_number, chi, chi).reshape(-1))
-    job.chi, job.tcur, job.mcur = chi, 0, 0
+    job.chi = job.chis = chi
+    job.tcur = job.mcur = 0
     cls = job._class_array()
     flops, nbytes = job.bp_sweep_cost()
 

@@ -53,6 +53,7 @@ SIGNATURES = {
     "bqa_densities": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
     "bqa_psplit": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
     "bqa_edge_zz": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_lmbds_truncate": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_void_p]),
     "bqa_project_nodes": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p,
                                     c_void_p]),
     "bqa_canonicalize_noalloc": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,

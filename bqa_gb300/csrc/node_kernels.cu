@@ -480,6 +480,17 @@ __global__ void edge_zz_kernel(const typename Cx<R>::T* pm, int E, int chi, doub
     if (lane == 0) zz[warp] = (nr * dr + ni * di) / (dr * dr + di * di);
 }
 
+// lam[row][c] = 0 for dim <= c < stride: drops spectrum columns a truncation removed
+template <typename R>
+__global__ void lmbds_truncate_kernel(R* lam, int stride, int rows, int dim) {
+    const int w = stride - dim;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)rows * w;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / w), c = dim + (int)(i - (int64_t)r * w);
+        lam[(size_t)r * stride + c] = R(0);
+    }
+}
+
 template <typename R>
 static int finalize(void* a, void* b, int64_t n, void* parts, int32_t* ls, double eps, double damping, int max_iters,
                     cudaStream_t st) {
@@ -563,6 +574,21 @@ int32_t bqa_msgs_from_lmbds(const void* lmbds, int32_t lam_stride, int32_t edges
     else
         return set_error(BQA_ERR_ARG, "bqa_msgs_from_lmbds: unknown dtype %d", dtype);
     return check_launch("msgs_from_lmbds");
+}
+
+int32_t bqa_lmbds_truncate(void* lmbds, int32_t stride, int32_t rows, int32_t dim, int32_t dtype, void* stream) {
+    if (!lmbds || rows < 0 || dim < 0 || stride < dim) return set_error(BQA_ERR_ARG, "bqa_lmbds_truncate: bad argument");
+    if (rows == 0 || stride == dim) return BQA_OK;
+    int blocks = (int)(((int64_t)rows * (stride - dim) + 255) / 256);
+    blocks = blocks > 4096 ? 4096 : blocks;
+    cudaStream_t st = as_stream(stream);
+    if (dtype == BQA_C64)
+        lmbds_truncate_kernel<float><<<blocks, 256, 0, st>>>(static_cast<float*>(lmbds), stride, rows, dim);
+    else if (dtype == BQA_C128)
+        lmbds_truncate_kernel<double><<<blocks, 256, 0, st>>>(static_cast<double*>(lmbds), stride, rows, dim);
+    else
+        return set_error(BQA_ERR_ARG, "bqa_lmbds_truncate: unknown dtype %d", dtype);
+    return check_launch("lmbds_truncate");
 }
 
 int32_t bqa_edge_zz(const void* pm, int32_t edges, int32_t chi, int32_t dtype, double* zz, void* stream) {

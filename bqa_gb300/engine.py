@@ -70,7 +70,8 @@ class _DeviceClass:
 class Annealer:
     """One annealing job resident on one GPU."""
 
-    def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4):
+    def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4,
+                 pad_bonds: bool | None = None):
         import torch
         self.torch = torch
         if not torch.cuda.is_available():
@@ -87,7 +88,16 @@ class Annealer:
         E = ctx.edges_number
         self.E = E
         self.half = E // 2
-        chimax = ctx.max_bond_dim
+        # Storage bond dim: a bond dim above 4 that is not a multiple of 4 is stored zero-padded
+        # to the next multiple of 4, so the register-tiled complex64 message kernels (built for
+        # degrees 2-4 and chi % 4 == 0) serve every step.  Padding is exact: padded rows and
+        # columns of tensors and messages stay zero, their singular values are 0 (masked and
+        # sorted last, never counted by the truncation rank), and the truncation zeroes the
+        # spectrum columns it drops.
+        if pad_bonds is None:
+            pad_bonds = self.precision == "single" and all(d <= 4 for d in ctx.degree_to_layout)
+        self.pad_bonds = bool(pad_bonds)
+        chimax = self._store(ctx.max_bond_dim)
         for d in ctx.degree_to_layout:
             lim = self.lib.max_bond_dim(d, self.dtype)
             if chimax > lim:
@@ -169,6 +179,12 @@ class Annealer:
         return f, b
 
     # ---- helpers -------------------------------------------------------------------------
+    def _store(self, chi: int) -> int:
+        """Storage bond dim of logical bond dim ``chi``."""
+        if self.pad_bonds and chi > 4 and chi % 4:
+            return chi + 4 - chi % 4
+        return chi
+
     @property
     def stream(self) -> int:
         return self.torch.cuda.current_stream(self.device).cuda_stream
@@ -197,7 +213,7 @@ class Annealer:
     def reset(self) -> None:
         """Initial product state (src/bqa/state.py:41-74): every tensor [sqrt(.5), -sqrt(.5)],
         bond dim 1, lambdas 1, messages diag(lambda)/tr."""
-        self.chi = 1
+        self.chi = self.chis = 1
         self.tcur = 0
         self.mcur = 0
         init = self.torch.tensor([complex(INIT_STATE[0]), complex(INIT_STATE[1])], dtype=self.msgs[0].dtype,
@@ -216,11 +232,18 @@ class Annealer:
         chi = int(msgs.shape[-1])
         if chi > self.ctx.max_bond_dim:
             raise ValueError("state bond dim exceeds max_bond_dim")
-        self.chi, self.tcur, self.mcur = chi, 0, 0
+        chis = self._store(chi)
+        self.chi, self.chis, self.tcur, self.mcur = chi, chis, 0, 0
         for c in self.classes:
-            t = np.ascontiguousarray(degree_to_tensor[c.degree], dtype=self._np_cplx).reshape(-1)
+            t = np.asarray(degree_to_tensor[c.degree], dtype=self._np_cplx)
+            if chis != chi:
+                t = np.pad(t, [(0, 0), (0, 0)] + [(0, chis - chi)] * c.degree)
+            t = np.ascontiguousarray(t).reshape(-1)
             c.tensors[0][: t.size].copy_(torch.from_numpy(t))
-        m = np.ascontiguousarray(msgs, dtype=self._np_cplx).reshape(-1)
+        m = np.asarray(msgs, dtype=self._np_cplx)
+        if chis != chi:
+            m = np.pad(m, [(0, 0), (0, chis - chi), (0, chis - chi)])
+        m = np.ascontiguousarray(m).reshape(-1)
         self.msgs[0][: m.size].copy_(torch.from_numpy(m))
         if lmbds is not None:
             lam = np.ascontiguousarray(lmbds.real, dtype=self.real_np)
@@ -229,12 +252,13 @@ class Annealer:
 
     def get_state(self) -> tuple[dict, np.ndarray, np.ndarray]:
         """Numpy copies of (tensors per degree, messages (E, chi, chi), lambdas (E/2, chi))."""
-        chi = self.chi
+        chi, chis = self.chi, self.chis
         tens = {}
         for c in self.classes:
-            shape = (c.count, 2) + (chi,) * c.degree
-            tens[c.degree] = c.tensors[self.tcur][: int(np.prod(shape))].cpu().numpy().reshape(shape)
-        msgs = self._msgs_cur()[: self.E * chi * chi].cpu().numpy().reshape(self.E, chi, chi)
+            shape = (c.count, 2) + (chis,) * c.degree
+            t = c.tensors[self.tcur][: int(np.prod(shape))].cpu().numpy().reshape(shape)
+            tens[c.degree] = t[(slice(None), slice(None)) + (slice(0, chi),) * c.degree]
+        msgs = self._msgs_cur()[: self.E * chis * chis].cpu().numpy().reshape(self.E, chis, chis)[:, :chi, :chi]
         lam = self.lmbds[: self.half * self.lam_stride].cpu().numpy().reshape(self.half, self.lam_stride)[:, :chi]
         return tens, msgs, lam
 
@@ -247,7 +271,7 @@ class Annealer:
         messages diag(lambda)/tr.  Returns (new bond dim, truncation error bound)."""
         lib, st = self.lib, self.stream
         ctx = self.ctx
-        chi = self.chi
+        chi = self.chis
         n = 2 * chi
         eps = float(ctx.pinv_eps)
         cls = self._class_array()
@@ -269,13 +293,17 @@ class Annealer:
         dim = min(rank, ctx.max_bond_dim)
         err = float(np.sqrt(np.sum(max_l[dim:] ** 2)))
         log.info(f"Truncation performed, per edge error upper bound: {err}")
+        dims = self._store(dim)
+        if dims != dim:
+            # padded storage: the spectrum columns the truncation drops become exact zeros
+            lib.call("bqa_lmbds_truncate", _ptr(self.lmbds), n, self.half, dim, dt, st)
         cls = self._class_array(out=True)
-        self._launch("apply_update", 0.0, 0.0, lib.call, "bqa_apply_update", cls, len(self.classes), chi, dim, dt,
+        self._launch("apply_update", 0.0, 0.0, lib.call, "bqa_apply_update", cls, len(self.classes), chi, dims, dt,
                      _ptr(canon), _ptr(self.lmbds), n, float(ztime), float(xtime), st)
         self.tcur = 1 - self.tcur
-        self.chi = dim
+        self.chi, self.chis = dim, dims
         self.lam_stride = n
-        lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), n, self.E, dim, dt, _ptr(self._msgs_cur()), st)
+        lib.call("bqa_msgs_from_lmbds", _ptr(self.lmbds), n, self.E, dims, dt, _ptr(self._msgs_cur()), st)
         return dim, err
 
     def run_layer(self, xtime: float, ztime: float) -> dict:
@@ -298,14 +326,14 @@ class Annealer:
         a, b = self.msgs[self.mcur], self.msgs[1 - self.mcur]
         self.loop_state.zero_()
         self.dist_parts.zero_()
-        elems = self.E * self.chi * self.chi
+        elems = self.E * self.chis * self.chis
         launched = 0
         eps, damp = float(ctx.bp_eps), float(ctx.damping)
         flops, nbytes = self.bp_sweep_cost()
         first = len(self._events) if self._events is not None else 0
         while True:
             for _ in range(min(self.bp_check_every, ctx.max_bp_iters_number - launched)):
-                self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep", cls, len(self.classes), self.chi,
+                self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep", cls, len(self.classes), self.chis,
                              self.dtype, _ptr(a), _ptr(b), _ptr(self.dist_parts), _ptr(self.loop_state), st)
                 lib.call("bqa_bp_finalize", _ptr(a), _ptr(b), elems, self.dtype, _ptr(self.dist_parts),
                          _ptr(self.loop_state), eps, damp, ctx.max_bp_iters_number, st)
@@ -331,7 +359,7 @@ class Annealer:
     # ---- read-out ------------------------------------------------------------------------
     def density_matrices(self) -> np.ndarray:
         """(n, 2, 2) complex marginals (src/bqa/state.py:77-94)."""
-        self.lib.call("bqa_densities", self._class_array(), len(self.classes), self.chi, self.dtype,
+        self.lib.call("bqa_densities", self._class_array(), len(self.classes), self.chis, self.dtype,
                       _ptr(self._msgs_cur()), _ptr(self.rho), self.stream)
         return self.rho.view(-1, 2, 2).cpu().numpy().astype(np.complex128)
 
@@ -345,9 +373,9 @@ class Annealer:
     def edge_zz(self) -> np.ndarray:
         """BP two-site <Z_u Z_v> per undirected edge (oracle ``edge_zz``)."""
         pm = self.lu   # scratch of the simple update, idle between steps
-        self.lib.call("bqa_psplit", self._class_array(), len(self.classes), self.chi, self.dtype,
+        self.lib.call("bqa_psplit", self._class_array(), len(self.classes), self.chis, self.dtype,
                       _ptr(self._msgs_cur()), _ptr(pm), self.stream)
-        self.lib.call("bqa_edge_zz", _ptr(pm), self.E, self.chi, self.dtype, _ptr(self.zz), self.stream)
+        self.lib.call("bqa_edge_zz", _ptr(pm), self.E, self.chis, self.dtype, _ptr(self.zz), self.stream)
         return self.zz.cpu().numpy()
 
     def energy(self, zz: np.ndarray | None = None, z: np.ndarray | None = None) -> float:
@@ -378,7 +406,7 @@ class Annealer:
                 continue
             pos = self.torch.as_tensor(ctx.node_position[nodes[sel]].astype(np.int32), device=self.device)
             out = self.torch.as_tensor(outcomes[sel].astype(np.int32), device=self.device)
-            self.lib.call("bqa_project_nodes", _ptr(c.tensors[self.tcur]), c.count, 2 * self.chi ** c.degree,
+            self.lib.call("bqa_project_nodes", _ptr(c.tensors[self.tcur]), c.count, 2 * self.chis ** c.degree,
                           self.dtype, _ptr(pos), _ptr(out), int(pos.numel()), _ptr(self.norm2), self.stream)
 
     def measure(self) -> list:

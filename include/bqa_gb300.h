@@ -143,6 +143,13 @@ int32_t bqa_apply_update(const bqa_class* classes, int32_t n_classes, int32_t ch
                          const void* canon, const void* lmbds, int32_t lam_stride, double ztime, double xtime,
                          void* stream);
 
+/*
+ * Zero the spectrum columns [dim, stride) of every row of lmbds[rows][stride] (real): the
+ * columns a truncation to bond dim `dim` removes (src/bqa/backends.py:289-303), when the
+ * tensors are stored at a larger, zero-padded bond dimension.
+ */
+int32_t bqa_lmbds_truncate(void* lmbds, int32_t stride, int32_t rows, int32_t dim, int32_t dtype, void* stream);
+
 /* msgs[e] = diag(lmbds[e % (E/2)][0..dim-1]) / trace (src/bqa/state.py:56-57). */
 int32_t bqa_msgs_from_lmbds(const void* lmbds, int32_t lam_stride, int32_t edges, int32_t dim, int32_t dtype,
                             void* msgs, void* stream);

@@ -49,7 +49,7 @@ def random_state(name, chi, seed=0, precision="single"):
     tens = {d: t.astype(np.complex64).astype(np.complex128) for d, t in tens.items()}
     m = m.astype(np.complex64).astype(np.complex128)
     st = orc.OracleState(np.random.default_rng(0), tens, m, lam.astype(np.complex128))
-    job = Annealer(build_context(conf), precision=precision)
+    job = Annealer(build_context(conf), precision=precision, pad_bonds=False)
     job.set_state(tens, m, lam)
     return octx, st, job
 
@@ -145,7 +145,7 @@ def test_apply_update_matches_oracle(name, chi, dim):
     job.lib.call("bqa_apply_update", job._class_array(out=True), len(job.classes), chi, dim, job.dtype,
                  _ptr(job.ext), _ptr(job.lmbds), n, ztime, xtime, job.stream)
     job.tcur = 1
-    job.chi = dim
+    job.chi = job.chis = dim
     for c in job.classes:
         shape = (c.count, 2) + (dim,) * c.degree
         got = c.tensors[1][: int(np.prod(shape))].cpu().numpy().reshape(shape)
@@ -195,3 +195,24 @@ def test_double_precision_kernels_match_oracle_to_roundoff(name, chi):
                  _ptr(job.ext), 0.3, job.stream)
     assert rel_err(job.ext[: ext_w.size].cpu().numpy().reshape(ext_w.shape), ext_w) < 1e-12
     assert np.abs(job.density_matrices() - orc.get_density_matrices(octx, st)).max() < 1e-12
+
+
+@pytest.mark.parametrize("name,chi", [("rr3_n16_chi4", 6), ("rr4_n20_chi4", 7), ("grid3x4_chi4_damped", 5)])
+def test_zero_padded_bond_storage_is_exact(name, chi):
+    """A bond dim stored zero-padded to a multiple of 4 (tiled kernels) gives the same step as
+    the unpadded generic path: same new bond dim, marginals and bond spectra within 1e-5."""
+    conf = gc.config(name)
+    conf["max_bond_dim"] = chi + 2
+    octx, st, _ = random_state(name, chi, seed=8)
+    runs = []
+    for pad in (False, True):
+        job = Annealer(build_context(conf), pad_bonds=pad)
+        job.set_state(st.degree_to_tensor, st.msgs, st.lmbds)
+        assert job.chis == (chi if not pad else chi + 4 - chi % 4)
+        info = job.run_layer(0.07, 0.11)
+        _, _, lam = job.get_state()
+        runs.append((info["bond_dim"], job.bloch_vectors(), lam, job.edge_zz()))
+    assert runs[0][0] == runs[1][0]
+    assert np.abs(runs[0][1] - runs[1][1]).max() < 1e-5
+    assert np.abs(runs[0][2] - runs[1][2]).max() < 1e-5
+    assert np.abs(runs[0][3] - runs[1][3]).max() < 1e-5
