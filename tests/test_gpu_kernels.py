@@ -197,12 +197,13 @@ def test_double_precision_kernels_match_oracle_to_roundoff(name, chi):
     assert np.abs(job.density_matrices() - orc.get_density_matrices(octx, st)).max() < 1e-12
 
 
-@pytest.mark.parametrize("name,chi", [("rr3_n16_chi4", 6), ("rr4_n20_chi4", 7), ("grid3x4_chi4_damped", 5)])
-def test_zero_padded_bond_storage_is_exact(name, chi):
+@pytest.mark.parametrize("name,chi,maxd", [("rr3_n16_chi4", 6, 8), ("rr4_n20_chi4", 7, 8), ("grid3x4_chi4_damped", 5, 7),
+                                           ("rr3_n24_chi8", 13, 16)])
+def test_zero_padded_bond_storage_is_exact(name, chi, maxd):
     """A bond dim stored zero-padded to a multiple of 4 (tiled kernels) gives the same step as
     the unpadded generic path: same new bond dim, marginals and bond spectra within 1e-5."""
     conf = gc.config(name)
-    conf["max_bond_dim"] = chi + 2
+    conf["max_bond_dim"] = maxd
     octx, st, _ = random_state(name, chi, seed=8)
     runs = []
     for pad in (False, True):
