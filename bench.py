@@ -346,6 +346,52 @@ def run_sweep_mode(args) -> None:
                       "msg_updates_per_s": ctx.edges_number / (mean / 1000)}))
 
 
+def run_svd_mode(args) -> None:
+    """Time the truncation factorisation alone (environment SVDs + bond canonicalisation) on the
+    extended messages of a real saturated-regime state: the anneal runs untimed until the bond
+    dim saturates, then K repetitions of the two Jacobi kernels are timed with CUDA events."""
+    import torch
+    from bqa_gb300 import instances
+    from bqa_gb300.engine import Annealer, _ptr
+    from bqa_gb300.layout import build_context
+    ctx = build_context(instances.headline_gpu_job(n=args.n, seed=0, chi=args.chi))
+    steps = [i for i in ctx.instructions if isinstance(i, dict)]
+    job = Annealer(ctx, precision=args.precision)
+    s = 0
+    while job.bond_dim < args.chi and s < len(steps) - 1:
+        job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
+        s += 1
+    chi = job.chis
+    n = 2 * chi
+    lib, st, E = job.lib, job.stream, ctx.edges_number
+    lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job._msgs_cur()),
+             _ptr(job.ext), float(steps[s]["ztime"]), st)
+    ext = job.ext.clone()
+    canon = torch.empty_like(job.ext)
+    eps = float(ctx.pinv_eps)
+
+    def env():
+        lib.call("bqa_env_factor", _ptr(ext), E, n, job.dtype, eps, _ptr(job.lu), _ptr(job.ul), _ptr(job.status), st)
+
+    def can():
+        lib.call("bqa_bond_canon", _ptr(job.lu), _ptr(job.ul), E, n, job.dtype, eps, _ptr(canon), _ptr(job.lmbds),
+                 _ptr(job.colmax), _ptr(job.status), st)
+
+    out = {"mode": "svd", "n": args.n, "chi": chi, "matrices": E, "size": n, "step": s}
+    for name, fn in (("env_factor", env), ("bond_canon", can)):
+        for _ in range(args.warmup):
+            fn()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in evs:
+            a.record()
+            fn()
+            b.record()
+        torch.cuda.synchronize()
+        out[name + "_ms"] = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    out["status"] = int(job.status.item())
+    print(json.dumps(out))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -355,7 +401,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep"])
+    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd"])
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     args = ap.parse_args()
     logging.basicConfig(level=logging.ERROR)
@@ -364,6 +410,8 @@ def main() -> None:
         run_reference_arm(args)
     elif args.mode == "sweep":
         run_sweep_mode(args)
+    elif args.mode == "svd":
+        run_svd_mode(args)
     else:
         run_gpu_arm(args)
 

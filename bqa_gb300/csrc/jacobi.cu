@@ -69,45 +69,41 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
         for (int r = 1; r < W; ++r) {
             const int partner = lane ^ r;
             const bool low = lane < partner;
-            C o[W];
-            R alpha0 = 0, alpha1 = 0, beta0 = 0, beta1 = 0;
-            C g0 = c_zero<C>(), g1 = c_zero<C>();
+            // Gram entries of the pair from sums both lanes form bit-identically: the squared
+            // norms, Sx = sum Re(conj(own) partner), and the cross sums S1 = sum own.x partner.y,
+            // S2 = sum own.y partner.x (on the other lane of the pair S1 and S2 swap roles).
+            R nown = 0, npart = 0, sx = 0, s1 = 0, s2 = 0;
 #pragma unroll
             for (int i = 0; i < W; ++i) {
-                o[i] = shfl_xor_c(a[i], r, W);
-                const C p = low ? a[i] : o[i];
-                const C q = low ? o[i] : a[i];
-                if (i & 1) {
-                    alpha1 = fma(p.x, p.x, fma(p.y, p.y, alpha1));
-                    beta1 = fma(q.x, q.x, fma(q.y, q.y, beta1));
-                    g1 = c_fma_conj(p, q, g1);
-                } else {
-                    alpha0 = fma(p.x, p.x, fma(p.y, p.y, alpha0));
-                    beta0 = fma(q.x, q.x, fma(q.y, q.y, beta0));
-                    g0 = c_fma_conj(p, q, g0);
-                }
+                const C o = shfl_xor_c(a[i], r, W);
+                nown = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, nown));
+                npart = fma(o.x, o.x, fma(o.y, o.y, npart));
+                sx = fma(a[i].x, o.x, fma(a[i].y, o.y, sx));
+                s1 = fma(a[i].x, o.y, s1);
+                s2 = fma(a[i].y, o.x, s2);
             }
-            const R alpha = alpha0 + alpha1, beta = beta0 + beta1;
-            const C g = c_add(g0, g1);
+            // p = column of the lower lane, q = of the higher: gamma = p^H q
+            const R alpha = low ? nown : npart, beta = low ? npart : nown;
+            const C g = c_make(sx, low ? s1 - s2 : s2 - s1);
             const R gabs = sqrt(c_abs2(g));
             const bool rot = alpha > R(0) && beta > R(0) && gabs > tol * sqrt(alpha) * sqrt(beta);
-            // both lanes of a pair take the same branch (identical inputs and operand order)
             if (__any_sync(BQA_FULL_MASK, rot)) {
-                R c = 1, s = 0;
-                C eb = c_make(R(1), R(0));  // conj(e)
+                // own' = k1 own + k2 partner; lower lane: (c, -s conj(e)), higher: (c conj(e), s)
+                C k1 = c_make(R(1), R(0)), k2 = c_zero<C>();
                 if (rot) {
                     const R zeta = (beta - alpha) / (R(2) * gabs);
                     const R t = copysign(R(1), zeta) / (fabs(zeta) + hypot(R(1), zeta));
-                    c = R(1) / sqrt(fma(t, t, R(1)));
-                    s = c * t;
-                    eb = c_make(g.x / gabs, -g.y / gabs);
+                    const R c = R(1) / sqrt(fma(t, t, R(1)));
+                    const R sn = c * t;
+                    const C eb = c_make(g.x / gabs, -g.y / gabs);  // conj(e)
+                    k1 = low ? c_make(c, R(0)) : c_scale(eb, c);
+                    k2 = low ? c_scale(eb, -sn) : c_make(sn, R(0));
                     rotated |= (alpha > col_floor && beta > col_floor);
                 }
 #pragma unroll
                 for (int i = 0; i < W; ++i) {
-                    const C p = low ? a[i] : o[i];
-                    const C q = c_mul(eb, low ? o[i] : a[i]);
-                    a[i] = low ? c_make(c * p.x - s * q.x, c * p.y - s * q.y) : c_make(s * p.x + c * q.x, s * p.y + c * q.y);
+                    const C o = shfl_xor_c(a[i], r, W);
+                    a[i] = c_fma(k2, o, c_mul(k1, a[i]));
                 }
                 // V: read own and partner columns of the current block, write own of the next
                 const C* vown = vcur + lane * VS;
@@ -124,13 +120,11 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                     } else {
                         vo0 = vown[i]; vo1 = vown[i + 1]; vp0 = vpart[i]; vp1 = vpart[i + 1];
                     }
-                    const C p0 = low ? vo0 : vp0, p1 = low ? vo1 : vp1;
-                    const C q0 = c_mul(eb, low ? vp0 : vo0), q1 = c_mul(eb, low ? vp1 : vo1);
-                    vout[i] = low ? c_make(c * p0.x - s * q0.x, c * p0.y - s * q0.y) : c_make(s * p0.x + c * q0.x, s * p0.y + c * q0.y);
-                    vout[i + 1] = low ? c_make(c * p1.x - s * q1.x, c * p1.y - s * q1.y) : c_make(s * p1.x + c * q1.x, s * p1.y + c * q1.y);
+                    vout[i] = c_fma(k2, vp0, c_mul(k1, vo0));
+                    vout[i + 1] = c_fma(k2, vp1, c_mul(k1, vo1));
                 }
                 __syncwarp();
-                C* t = vcur; vcur = vnxt; vnxt = t;
+                C* tt = vcur; vcur = vnxt; vnxt = tt;
                 *vfinal = vcur;
             }
         }
@@ -152,7 +146,7 @@ __device__ __forceinline__ R seg_sum(R x) {
 // are built from the accumulated V, which stays unitary to working precision, while
 // a_j / sigma_j carries a relative error eps |m| / sigma_j for small sigma_j.
 template <int W, typename R>
-__global__ void __launch_bounds__(128, 3) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
+__global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ lu,
                                                          typename Cx<R>::T* __restrict__ ul, int32_t* status) {
     using C = typename Cx<R>::T;
@@ -192,7 +186,7 @@ __global__ void __launch_bounds__(128, 3) env_factor_kernel(const typename Cx<R>
 // Per undirected edge p: ker = lu[p] lu[p+h]^T = us s vhs; lambdas; canonicalisers
 // (src/bqa/state.py:171-200).
 template <int W, typename R>
-__global__ void __launch_bounds__(128, 3) bond_canon_kernel(const typename Cx<R>::T* __restrict__ lu,
+__global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>::T* __restrict__ lu,
                                                          const typename Cx<R>::T* __restrict__ ul, int edges, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ canon,
                                                          R* __restrict__ lmbds, typename Cx<R>::Bits* colmax,
