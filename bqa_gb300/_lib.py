@@ -40,6 +40,8 @@ SIGNATURES = {
     "bqa_max_bond_dim": (c_int32, [c_int32, c_int32]),
     "bqa_bp_sweep": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
                                c_void_p]),
+    "bqa_bp_sweep_split": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                     c_int32, c_void_p, c_void_p, c_void_p]),
     "bqa_bp_finalize": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_double, c_double,
                                   c_int32, c_void_p]),
     "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),

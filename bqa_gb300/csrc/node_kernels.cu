@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
 
     const C* msgs_in = a.msgs_a;
     C* msgs_out = a.msgs_b;
-    if (MODE == MODE_BP && a.loop_state != nullptr) {
+    if ((MODE == MODE_BP || MODE == MODE_PSPLIT) && a.loop_state != nullptr) {
         if (a.loop_state[0]) return;                        // BP loop already done
         if (a.loop_state[2]) { msgs_in = a.msgs_b; msgs_out = const_cast<C*>(a.msgs_a); }
     }
@@ -329,6 +329,138 @@ static int try_tiled(const NodeArgs<float>& a, int count, cudaStream_t st, int* 
     BQA_TILED(4, 4) BQA_TILED(4, 8)
 #undef BQA_TILED
     return 0;
+}
+
+
+// Half-node register-tiled kernel: CTA (node, s) computes P_s of every bond of the node and
+// writes it to pm[slot][s] (the layout of the PSPLIT mode); bp_combine_kernel turns
+// P_0 + P_1 into messages.  Same schedule of shared bond products as tiled_node_kernel.
+template <int D, int CHI>
+__global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_kernel(NodeArgs<float> a) {
+    using S = tiled::HalfShape<D, CHI>;
+    static_assert(CHI % 4 == 0 && D >= 2 && D <= 4, "half kernel shapes");
+    static_assert(S::CLOSE_TILES <= S::THREADS, "close tiles exceed the block");
+    constexpr int PS = S::PER_S, N2 = S::N2, TH = S::THREADS, SW = S::SW;
+    extern __shared__ double4 smem_raw[];
+    float2* sT = reinterpret_cast<float2*>(smem_raw);
+    float2* sA = sT + PS;
+    float2* sB = sA + PS;
+    float2* sMt = sB + PS;
+    float2* sP = sMt + D * N2;
+    const float2* msgs_in = a.msgs_a;
+    if (a.loop_state != nullptr) {
+        if (a.loop_state[0]) return;
+        if (a.loop_state[2]) msgs_in = a.msgs_b;
+    }
+    const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
+    {
+        const float4* tg = reinterpret_cast<const float4*>(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS);
+        for (int i = threadIdx.x; i < PS / 2; i += TH)
+            *reinterpret_cast<float4*>(sT + tiled::swz<SW>(2 * i)) = tg[i];
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
+        for (int o = threadIdx.x; o < N2; o += TH) {
+            const int i = o / CHI, j = o - i * CHI;
+            sMt[k * N2 + j * CHI + i] = mg[o];
+        }
+    }
+    __syncthreads();
+    auto prod = [&](const float2* X, float2* Y, int k) {
+        tiled::product<D, CHI, TH, SW, 1>(X, Y, sMt + k * N2, k);
+        __syncthreads();
+    };
+    auto emit = [&](int idx, const float2* R) {
+        tiled::close_tiled<CHI, TH, S::KS, PS, SW, 1>(sT, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
+        __syncthreads();
+        float4* og = reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2);
+        const float4* sp = reinterpret_cast<const float4*>(sP);
+        for (int i = threadIdx.x; i < N2 / 2; i += TH) og[i] = sp[i];
+        __syncthreads();
+    };
+    if (D == 2) {
+        prod(sT, sA, 1); emit(0, sA);
+        prod(sT, sA, 0); emit(1, sA);
+    } else if (D == 3) {
+        prod(sT, sA, 0);
+        prod(sA, sB, 1); emit(2, sB);
+        prod(sA, sB, 2); emit(1, sB);
+        prod(sT, sA, 1);
+        prod(sA, sB, 2); emit(0, sB);
+    } else {
+        prod(sT, sB, 0); prod(sB, sA, 1);
+        prod(sA, sB, 2); emit(3, sB);
+        prod(sA, sB, 3); emit(2, sB);
+        prod(sT, sB, 2); prod(sB, sA, 3);
+        prod(sA, sB, 0); emit(1, sB);
+        prod(sA, sB, 1); emit(0, sB);
+    }
+}
+
+template <int D, int CHI>
+static int launch_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    using S = tiled::HalfShape<D, CHI>;
+    const size_t smem = (size_t)S::SMEM_ELEMS * sizeof(float2);
+    int rc = ensure_smem((const void*)tiled_half_kernel<D, CHI>, smem, "tiled half kernel");
+    if (rc) return rc;
+    tiled_half_kernel<D, CHI><<<2 * count, S::THREADS, smem, st>>>(args);
+    return check_launch("tiled half kernel");
+}
+
+// 1 if a half-node kernel covers (degree, chi) and was launched
+static int try_half(const NodeArgs<float>& a, int count, cudaStream_t st, int* rc) {
+    const int d = a.d, chi = a.chi;
+#define BQA_HALF(DD, CC) \
+    if (d == DD && chi == CC) { *rc = launch_half<DD, CC>(a, count, st); return 1; }
+    BQA_HALF(2, 8) BQA_HALF(2, 12) BQA_HALF(2, 16)
+    BQA_HALF(3, 4) BQA_HALF(3, 8) BQA_HALF(3, 12) BQA_HALF(3, 16)
+    BQA_HALF(4, 4) BQA_HALF(4, 8)
+#undef BQA_HALF
+    return 0;
+}
+
+// BP messages from the open-bond blocks: msg[e] = (P_0 + P_1)/tr, with the convergence maxima
+// max|new-old|^2 and max|new+old|^2 folded per block into dist_parts.  One warp per slot.
+template <typename R>
+__global__ void __launch_bounds__(256) bp_combine_kernel(const typename Cx<R>::T* __restrict__ pm, int E, int chi,
+                                                         const typename Cx<R>::T* msgs_a, typename Cx<R>::T* msgs_b,
+                                                         const int32_t* loop_state, typename Cx<R>::Bits* dist_parts) {
+    using C = typename Cx<R>::T;
+    __shared__ R sRed[32];
+    const C* msgs_in = msgs_a;
+    C* msgs_out = msgs_b;
+    if (loop_state != nullptr) {
+        if (loop_state[0]) return;
+        if (loop_state[2]) { msgs_in = msgs_b; msgs_out = const_cast<C*>(msgs_a); }
+    }
+    const int lane = threadIdx.x & 31;
+    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n2 = chi * chi;
+    R num2 = 0, den2 = 0;
+    if (slot < E) {
+        const C* p0 = pm + (size_t)slot * 2 * n2;
+        const C* p1 = p0 + n2;
+        C tr = c_zero<C>();
+        for (int q = lane; q < chi; q += 32) tr = c_add(tr, c_add(p0[q * chi + q], p1[q * chi + q]));
+        tr.x = warp_sum(tr.x);
+        tr.y = warp_sum(tr.y);
+        const C* old = msgs_in + (size_t)slot * n2;
+        C* og = msgs_out + (size_t)slot * n2;
+        for (int i = lane; i < n2; i += 32) {
+            const C m = c_div(c_add(p0[i], p1[i]), tr);
+            const C o = old[i];
+            og[i] = m;
+            num2 = fmax(num2, c_abs2(c_sub(m, o)));
+            den2 = fmax(den2, c_abs2(c_add(m, o)));
+        }
+    }
+    num2 = block_max(num2, sRed);
+    den2 = block_max(den2, sRed);
+    if (threadIdx.x == 0) {
+        atomic_max_nonneg(dist_parts, num2);
+        atomic_max_nonneg(dist_parts + 1, den2);
+    }
 }
 
 template <int MODE, typename R>
@@ -526,6 +658,46 @@ int32_t bqa_bp_sweep(const bqa_class* classes, int32_t n_classes, int32_t chi, i
     if (!msgs_a || !msgs_b || !dist_parts) return set_error(BQA_ERR_ARG, "bqa_bp_sweep: null buffer");
     return run_classes_dt(dtype, MODE_BP, classes, n_classes, chi, msgs_a, msgs_b, nullptr, dist_parts, loop_state, 0.0,
                           as_stream(stream));
+}
+
+int32_t bqa_bp_sweep_split(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, void* msgs_a,
+                           void* msgs_b, void* pm, int32_t edges, void* dist_parts, const int32_t* loop_state,
+                           void* stream) {
+    if (!classes || n_classes < 0 || chi < 1 || !msgs_a || !msgs_b || !pm || !dist_parts || edges < 2)
+        return set_error(BQA_ERR_ARG, "bqa_bp_sweep_split: bad argument");
+    if (dtype != BQA_C64 && dtype != BQA_C128) return set_error(BQA_ERR_ARG, "bqa_bp_sweep_split: unknown dtype %d", dtype);
+    cudaStream_t st = as_stream(stream);
+    for (int c = 0; c < n_classes; ++c) {
+        const bqa_class& k = classes[c];
+        if (k.count <= 0 || k.degree == 0) continue;
+        int rc = BQA_OK;
+        if (dtype == BQA_C64 && g_use_tiled) {
+            NodeArgs<float> a;
+            a.tensors = static_cast<const float2*>(k.tensor);
+            a.in_pos = k.in_pos; a.out_pos = k.out_pos; a.node_ids = k.node_ids; a.edge_ampl = k.edge_ampl;
+            a.d = k.degree; a.chi = chi;
+            a.msgs_a = static_cast<const float2*>(msgs_a); a.msgs_b = static_cast<float2*>(msgs_b);
+            a.out = static_cast<float2*>(pm); a.loop_state = loop_state; a.dist_parts = nullptr; a.ztime = 0.0;
+            if (try_half(a, k.count, st, &rc)) {
+                if (rc) return rc;
+                continue;
+            }
+        }
+        bqa_class one = k;
+        rc = run_classes_dt(dtype, MODE_PSPLIT, &one, 1, chi, msgs_a, msgs_b, pm, nullptr, loop_state, 0.0, st);
+        if (rc) return rc;
+    }
+    const int blocks = (int)(((int64_t)edges * 32 + 255) / 256);
+    if (dtype == BQA_C64)
+        bp_combine_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float2*>(pm), edges, chi,
+                                                          static_cast<const float2*>(msgs_a), static_cast<float2*>(msgs_b),
+                                                          loop_state, static_cast<uint32_t*>(dist_parts));
+    else
+        bp_combine_kernel<double><<<blocks, 256, 0, st>>>(static_cast<const double2*>(pm), edges, chi,
+                                                           static_cast<const double2*>(msgs_a),
+                                                           static_cast<double2*>(msgs_b), loop_state,
+                                                           static_cast<unsigned long long*>(dist_parts));
+    return check_launch("bp_combine");
 }
 
 int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, int32_t dtype, void* dist_parts,

@@ -46,6 +46,23 @@ struct Shape {
     static constexpr int SMEM_ELEMS = 3 * NT + D * N2 + 2 * N2 + 128;
 };
 
+// One CTA per (node, physical index s): the two values of s never mix inside a message
+// contraction, so a node splits into two independent halves of half the shared memory.
+template <int D, int CHI>
+struct HalfShape {
+    static constexpr int PER_S = cpow(CHI, D);
+    static constexpr int N2 = CHI * CHI;
+    static constexpr int PROD_TILES = (CHI / 4) * (cpow(CHI, D - 1) / 4 > 0 ? cpow(CHI, D - 1) / 4 : 1);
+    static constexpr int R32 = ((PROD_TILES + 31) / 32) * 32;
+    static constexpr int THREADS = R32 > 512 ? 512 : R32;
+    static constexpr int CLOSE_TILES = (CHI / 4) * (CHI / 4);
+    static constexpr int KS_RAW = THREADS / CLOSE_TILES;
+    static constexpr int KS = KS_RAW >= 32 ? 32 : (KS_RAW >= 16 ? 16 : (KS_RAW >= 8 ? 8 : (KS_RAW >= 4 ? 4 : (KS_RAW >= 2 ? 2 : 1))));
+    static constexpr int SW = CHI == 16 ? 7 : (CHI == 8 ? 3 : 0);
+    // T_s, two buffers, D transposed messages, P_s
+    static constexpr int SMEM_ELEMS = 3 * PER_S + D * N2 + N2;
+};
+
 template <int SW>
 __device__ __forceinline__ int swz(int e) { return SW ? (e ^ (((e >> 4) & SW) << 1)) : e; }
 
@@ -140,22 +157,23 @@ __device__ __forceinline__ void product_last(const float2* __restrict__ X, float
     }
 }
 
-// Bond product on bond k of a [2][CHI]^D buffer.
-template <int D, int CHI, int THREADS, int SW>
+// Bond product on bond k of a [NS][CHI]^D buffer (NS = 2: both values of the physical index,
+// NS = 1: one of them).
+template <int D, int CHI, int THREADS, int SW, int NS = 2>
 __device__ __forceinline__ void product(const float2* X, float2* Y, const float2* Mt, int k) {
     if (k == D - 1)
-        product_last<CHI, THREADS, SW>(X, Y, Mt, 2 * cpow(CHI, D - 1));
+        product_last<CHI, THREADS, SW>(X, Y, Mt, NS * cpow(CHI, D - 1));
     else
-        product_inner<CHI, THREADS, SW>(X, Y, Mt, 2 * ipow(CHI, k), ipow(CHI, D - 1 - k));
+        product_inner<CHI, THREADS, SW>(X, Y, Mt, NS * ipow(CHI, k), ipow(CHI, D - 1 - k));
 }
 
 // P[s][a][b] = sum_{x<Ax, y<B} conj(T[s][x][a][y]) R[s][x][b][y]; per s the operands are
-// [Ax][CHI][B] with Ax * CHI * B = PER_S.  Result written to P[2][CHI][CHI].
-template <int CHI, int THREADS, int KS, int PER_S, int SW>
+// [Ax][CHI][B] with Ax * CHI * B = PER_S.  Result written to P[NS][CHI][CHI].
+template <int CHI, int THREADS, int KS, int PER_S, int SW, int NS = 2>
 __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const float2* __restrict__ Rt,
                                             float2* __restrict__ P, int Ax, int B) {
     constexpr int NG = CHI / 4;
-    constexpr int TILES = 2 * NG * NG;
+    constexpr int TILES = NS * NG * NG;
     const int t = threadIdx.x;
     const int ks = t % KS;
     const int tile = t / KS;

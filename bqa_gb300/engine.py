@@ -97,6 +97,8 @@ class Annealer:
         if pad_bonds is None:
             pad_bonds = self.precision == "single" and all(d <= 4 for d in ctx.degree_to_layout)
         self.pad_bonds = bool(pad_bonds)
+        # BP sweeps in two stages (half-node message kernels + combine) on the complex64 path
+        self.split_sweeps = self.precision == "single"
         chimax = self._store(ctx.max_bond_dim)
         for d in ctx.degree_to_layout:
             lim = self.lib.max_bond_dim(d, self.dtype)
@@ -333,8 +335,15 @@ class Annealer:
         first = len(self._events) if self._events is not None else 0
         while True:
             for _ in range(min(self.bp_check_every, ctx.max_bp_iters_number - launched)):
-                self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep", cls, len(self.classes), self.chis,
-                             self.dtype, _ptr(a), _ptr(b), _ptr(self.dist_parts), _ptr(self.loop_state), st)
+                if self.split_sweeps:
+                    # open-bond blocks into the idle simple-update scratch, then the messages
+                    self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep_split", cls, len(self.classes),
+                                 self.chis, self.dtype, _ptr(a), _ptr(b), _ptr(self.lu), self.E,
+                                 _ptr(self.dist_parts), _ptr(self.loop_state), st)
+                else:
+                    self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep", cls, len(self.classes),
+                                 self.chis, self.dtype, _ptr(a), _ptr(b), _ptr(self.dist_parts),
+                                 _ptr(self.loop_state), st)
                 lib.call("bqa_bp_finalize", _ptr(a), _ptr(b), elems, self.dtype, _ptr(self.dist_parts),
                          _ptr(self.loop_state), eps, damp, ctx.max_bp_iters_number, st)
                 launched += 1

@@ -89,6 +89,17 @@ int32_t bqa_bp_sweep(const bqa_class* classes /* host array */, int32_t n_classe
                      void* msgs_a, void* msgs_b, void* dist_parts, const int32_t* loop_state, void* stream);
 
 /*
+ * The same sweep as bqa_bp_sweep, in two stages through a caller scratch pm[E][2][chi][chi]:
+ * every node writes its phys-resolved open-bond blocks P_0, P_1 of every bond (complex64
+ * nodes of degree 2-4 at chi % 4 == 0 run one CTA per (node, physical index), in half the
+ * shared memory), then one kernel forms msg = (P_0 + P_1)/tr per slot and the convergence
+ * maxima.  Same inputs, outputs and loop_state behaviour as bqa_bp_sweep.
+ */
+int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi, int32_t dtype,
+                           void* msgs_a, void* msgs_b, void* pm, int32_t edges, void* dist_parts,
+                           const int32_t* loop_state, void* stream);
+
+/*
  * BP convergence decision and damping after one sweep (src/bqa/state.py:113-124,
  * Tensor.get_dist src/bqa/backends.py:492-495, damping src/bqa/backends.py:761-764).
  * loop_state is int32[8] = {done, sweeps, cur, exhausted, damp_pending, dist (float bits),

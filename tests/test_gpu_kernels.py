@@ -77,6 +77,32 @@ def test_bp_sweep_matches_oracle(name, chi):
 
 
 @pytest.mark.parametrize("name,chi", CASES)
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_split_bp_sweep_matches_oracle(name, chi, precision):
+    """Two-stage sweep (open-bond blocks through scratch, then messages) = one oracle sweep."""
+    if precision == "double" and chi > 8:
+        pytest.skip("complex128 node kernels hold chi <= 13 at degree 3")
+    octx, st, job = random_state(name, chi, seed=9, precision=precision)
+    want = np.empty_like(st.msgs)
+    for d, t in st.degree_to_tensor.items():
+        L = octx.degree_to_layout[d]
+        for mm, p in zip(orc.pass_msgs(t, [st.msgs[p] for p in L.input_msgs_position]), L.output_msgs_position):
+            want[p] = mm
+    job.dist_parts.zero_()
+    job.lib.call("bqa_bp_sweep_split", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.msgs[1]), _ptr(job.lu), octx.edges_number, _ptr(job.dist_parts), None, job.stream)
+    got = job.msgs[1][: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, want) < (RTOL if precision == "single" else 1e-12)
+    parts = job.dist_parts.cpu()
+    if precision == "single":
+        num, den = parts.view(torch.int32)[:2].view(torch.float32).numpy()
+    else:
+        num, den = parts.view(torch.float64).numpy()
+    d_want = orc.get_dist(want, st.msgs)
+    assert abs(np.sqrt(num) / np.sqrt(den) - d_want) < 1e-5 * max(1.0, d_want)
+
+
+@pytest.mark.parametrize("name,chi", CASES)
 def test_ext_msgs_match_oracle(name, chi):
     octx, st, job = random_state(name, chi, seed=1)
     ztime = 0.37
