@@ -80,8 +80,8 @@ def test_bp_sweep_matches_oracle(name, chi):
 @pytest.mark.parametrize("precision", ["single", "double"])
 def test_split_bp_sweep_matches_oracle(name, chi, precision):
     """Two-stage sweep (open-bond blocks through scratch, then messages) = one oracle sweep."""
-    if precision == "double" and chi > 8:
-        pytest.skip("complex128 node kernels hold chi <= 13 at degree 3")
+    if precision == "double" and chi > 5:
+        pytest.skip("complex128 node kernels hold a smaller bond dim (6 at degree 4)")
     octx, st, job = random_state(name, chi, seed=9, precision=precision)
     want = np.empty_like(st.msgs)
     for d, t in st.degree_to_tensor.items():
