@@ -13,6 +13,7 @@
 // (all factors are diagonal in s except Rx, which is applied after the bond products).
 #include "common.cuh"
 #include "internal.h"
+#include "tiled_node.cuh"
 
 namespace bqa {
 
@@ -127,6 +128,100 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyArgs<R> a) {
     for (int o = threadIdx.x; o < 2 * per_s; o += blockDim.x) og[o] = c_scale(cur[o], inv);
 }
 
+
+// ---- register-tiled update for dim == chi, complex64 ------------------------------------------
+// CTA (node, s) stages T_s and the three s-specific bond matrices W_k^s (with sqrt(lambda) and,
+// on bond 0, the Rz phase z_s folded in), runs the d bond products with the tiled GEMM of the
+// message kernels and writes z_s-weighted Y_s to tensor_out; apply_rx_norm_kernel then mixes the
+// two halves (Rx) and normalises each node.
+template <int D, int CHI>
+__global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_apply_half_kernel(ApplyArgs<float> a) {
+    using S = tiled::HalfShape<D, CHI>;
+    constexpr int PS = S::PER_S, N2 = S::N2, TH = S::THREADS, SW = S::SW, n = 2 * CHI;
+    extern __shared__ double4 smem_raw[];
+    float2* sX = reinterpret_cast<float2*>(smem_raw);
+    float2* sY = sX + PS;
+    float2* sW = sY + PS;           // D blocks of [j][c], CHI x CHI
+    const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
+    {
+        const float4* tg = reinterpret_cast<const float4*>(a.t_in + (size_t)node * 2 * PS + (size_t)s * PS);
+        for (int i = threadIdx.x; i < PS / 2; i += TH)
+            *reinterpret_cast<float4*>(sX + tiled::swz<SW>(2 * i)) = tg[i];
+    }
+    double sz, cz;
+    sincos(a.node_ampl[node] * a.ztime, &sz, &cz);
+    const float2 zs = make_float2((float)cz, s ? (float)sz : (float)-sz);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const HalfZZ<float> h = half_zz<float>(a.edge_ampl[node * D + k] * a.ztime);
+        const float2* Cc = a.canon + (size_t)a.in_pos[node * D + k] * n * n;
+        const float* lam = a.lmbds + (size_t)a.lmbd_pos[node * D + k] * a.lam_stride;
+        for (int o = threadIdx.x; o < N2; o += TH) {
+            const int j = o / CHI, c = o - j * CHI;
+            const float2 up = c_mul(h.a0, Cc[(size_t)j * n + c]);
+            const float2 dn = c_mul(h.a1, Cc[(size_t)(CHI + j) * n + c]);
+            float2 w = c_scale(s ? c_sub(up, dn) : c_add(up, dn), sqrtf(lam[c]));
+            if (k == 0) w = c_mul(zs, w);
+            sW[k * N2 + o] = w;
+        }
+    }
+    __syncthreads();
+    float2* cur = sX;
+    float2* nxt = sY;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        tiled::product<D, CHI, TH, SW, 1>(cur, nxt, sW + k * N2, k);
+        __syncthreads();
+        float2* t = cur; cur = nxt; nxt = t;
+    }
+    float4* og = reinterpret_cast<float4*>(a.t_out + (size_t)node * 2 * PS + (size_t)s * PS);
+    for (int i = threadIdx.x; i < PS / 2; i += TH) og[i] = *reinterpret_cast<const float4*>(cur + tiled::swz<SW>(2 * i));
+}
+
+// T[0] <- cos(x) T[0] - i sin(x) T[1], T[1] <- cos(x) T[1] - i sin(x) T[0], then T /= |T| per node.
+__global__ void __launch_bounds__(256) apply_rx_norm_kernel(float2* t, int per_s, float cx, float sx) {
+    __shared__ float sRed[32];
+    float2* tn = t + (size_t)blockIdx.x * 2 * per_s;
+    float acc[1] = {0.f};
+    for (int o = threadIdx.x; o < per_s; o += blockDim.x) {
+        const float2 y0 = tn[o], y1 = tn[per_s + o];
+        const float2 t0 = make_float2(cx * y0.x + sx * y1.y, cx * y0.y - sx * y1.x);
+        const float2 t1 = make_float2(cx * y1.x + sx * y0.y, cx * y1.y - sx * y0.x);
+        tn[o] = t0;
+        tn[per_s + o] = t1;
+        acc[0] += c_abs2(t0) + c_abs2(t1);
+    }
+    block_sum<1>(acc, sRed);
+    const float inv = 1.f / sqrtf(acc[0]);
+    for (int o = threadIdx.x; o < 2 * per_s; o += blockDim.x) tn[o] = c_scale(tn[o], inv);
+}
+
+template <int D, int CHI>
+static int launch_apply_half(const ApplyArgs<float>& a, int count, cudaStream_t st) {
+    using S = tiled::HalfShape<D, CHI>;
+    const size_t smem = ((size_t)2 * S::PER_S + (size_t)D * S::N2) * sizeof(float2);
+    int rc = ensure_smem((const void*)tiled_apply_half_kernel<D, CHI>, smem, "tiled apply");
+    if (rc) return rc;
+    tiled_apply_half_kernel<D, CHI><<<2 * count, S::THREADS, smem, st>>>(a);
+    rc = check_launch("tiled apply");
+    if (rc) return rc;
+    apply_rx_norm_kernel<<<count, 256, 0, st>>>(a.t_out, S::PER_S, a.cx, a.sx);
+    return check_launch("apply rx norm");
+}
+
+// 1 if a tiled update covers (degree, chi == dim) and was launched
+static int try_tiled_apply(const ApplyArgs<float>& a, int count, cudaStream_t st, int* rc) {
+    if (a.dim != a.chi) return 0;
+    const int d = a.d, chi = a.chi;
+#define BQA_TAPPLY(DD, CC) \
+    if (d == DD && chi == CC) { *rc = launch_apply_half<DD, CC>(a, count, st); return 1; }
+    BQA_TAPPLY(2, 8) BQA_TAPPLY(2, 12) BQA_TAPPLY(2, 16)
+    BQA_TAPPLY(3, 4) BQA_TAPPLY(3, 8) BQA_TAPPLY(3, 12) BQA_TAPPLY(3, 16)
+    BQA_TAPPLY(4, 4) BQA_TAPPLY(4, 8)
+#undef BQA_TAPPLY
+    return 0;
+}
+
 template <typename R>
 static int apply_classes(const bqa_class* classes, int n_classes, int chi, int dim, const void* canon,
                          const void* lmbds, int lam_stride, double ztime, double xtime, cudaStream_t st) {
@@ -155,6 +250,13 @@ static int apply_classes(const bqa_class* classes, int n_classes, int chi, int d
         a.ztime = ztime;
         a.cx = (R)cos(xtime);
         a.sx = (R)sin(xtime);
+        if constexpr (sizeof(R) == 4) {
+            int trc = BQA_OK;
+            if (k.degree >= 2 && try_tiled_apply(a, k.count, st, &trc)) {
+                if (trc) return trc;
+                continue;
+            }
+        }
         const int fib = 2 * ipow(cm, k.degree > 0 ? k.degree - 1 : 0);
         int threads = ((fib + 31) / 32) * 32;
         threads = threads < 64 ? 64 : (threads > 256 ? 256 : threads);
