@@ -10,6 +10,8 @@ from __future__ import annotations
 
 import logging
 
+import numpy as np
+
 from . import config as cfg
 from .engine import Annealer
 from .layout import build_context
@@ -17,7 +19,9 @@ from .layout import build_context
 log = logging.getLogger(__name__)
 
 
-def run_qa(config, device=None) -> list:
+def run_qa(config, device=None, as_arrays: bool = False) -> list:
+    """Run a job; with ``as_arrays`` the result values stay numpy arrays (n x 3 float64 Bloch
+    vectors, n int64 outcomes) instead of nested lists."""
     ctx = build_context(config)
     log.info("Context is built")
     job = Annealer(ctx, device=device)
@@ -28,9 +32,11 @@ def run_qa(config, device=None) -> list:
         if isinstance(ins, dict):
             job.run_layer(ins["xtime"], ins["ztime"])
         elif ins == cfg.MEASURE:
-            out.append(["measurement_outcomes", job.measure()])
+            outcomes = job.measure()
+            out.append(["measurement_outcomes", np.asarray(outcomes, dtype=np.int64) if as_arrays else outcomes])
         elif ins == cfg.GET_BLOCH_VECTORS:
-            out.append(["bloch_vectors", job.bloch_vectors().tolist()])
+            bloch = job.bloch_vectors()
+            out.append(["bloch_vectors", bloch if as_arrays else bloch.tolist()])
         else:
             raise ValueError(f"Unknown instruction {ins}")
     return out

@@ -107,3 +107,27 @@ def test_headline_cpu_case_matches_reference():
     err = np.abs(results[0] - want["result0_bloch_vectors"]).max()
     print(f"{name}: max Bloch error {err:.2e}, sweeps {[s['sweeps'] for s in job.stats][:10]}")
     assert err < 5e-3
+
+
+def test_cli_streams_the_run_qa_result(tmp_path):
+    """python -m bqa_gb300.cli on a JSON job gives the same result list as run_qa."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    conf = gc.manifest()["rr3_n12_measure"]["config"]
+    job = dict(conf)
+    job.pop("backend", None)
+    job["edges"] = [[[a, b], J] for a, b, J in conf["edges"]]
+    (tmp_path / "job.json").write_text(json.dumps(job))
+    root = Path(__file__).resolve().parents[1]
+    r = subprocess.run([sys.executable, "-m", "bqa_gb300.cli", "-i", "job.json", "-o", "out.json", "-l", "ERROR"],
+                       cwd=str(tmp_path), capture_output=True, text=True,
+                       env={**os.environ, "PYTHONPATH": str(root)})
+    assert r.returncode == 0, r.stderr
+    got = json.loads((tmp_path / "out.json").read_text())
+    want = bqa_gb300.run_qa(gc.config("rr3_n12_measure"))
+    assert [g[0] for g in got] == [w[0] for w in want]
+    assert np.abs(np.array(got[0][1]) - np.array(want[0][1])).max() < 1e-12
+    assert got[1][1] == want[1][1]
