@@ -392,6 +392,64 @@ def run_svd_mode(args) -> None:
     print(json.dumps(out))
 
 
+def serving_stream(jobs: int, rate: float, seed: int = 0):
+    """Poisson stream of annealing jobs (arrival time, config): random d-regular graphs with
+    n log-uniform in [100, 20000], d in {3, 4}, J = +-1, h ~ N(0, 0.5), bond dim in {4, 8},
+    20 or 50 steps over T = steps / 10."""
+    from bqa_gb300 import instances
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(jobs):
+        t += rng.exponential(1.0 / rate)
+        n = int(np.exp(rng.uniform(np.log(100), np.log(20000))))
+        d = int(rng.choice([3, 4]))
+        n += (n * d) % 2
+        chi = int(rng.choice([4, 8]))
+        steps = int(rng.choice([20, 50]))
+        e = instances.random_regular_edges(n, d, seed * 100003 + k)
+        conf = instances.qubo_config(e, 2.0 * rng.integers(0, 2, len(e)) - 1, rng.normal(0, 0.5, n),
+                                     max_bond_dim=chi, bp_eps=1e-5, pinv_eps=1e-6, max_bp_iter_number=50,
+                                     schedule=instances.anneal_schedule(steps / 10.0, steps))
+        out.append((t, conf))
+    return out
+
+
+def run_serve_mode(args) -> None:
+    """p50/p99 job latency and jobs/s of a Poisson job stream through the continuous-batching
+    server, next to the same jobs run one at a time (each job's latency then includes its
+    wait behind the earlier ones)."""
+    import torch
+    import bqa_gb300
+    from bqa_gb300.serve import JobServer
+    stream = serving_stream(args.jobs, args.rate, seed=1)
+    # warm-up: compile paths and allocator
+    bqa_gb300.run_qa(dict(stream[0][1]))
+    torch.cuda.synchronize()
+    srv = JobServer()
+    for t, conf in stream:
+        srv.submit(dict(conf), arrival=t)
+    srv._t0 = time.perf_counter()
+    srv.run(timeout=1800)
+    served = srv.stats()
+    # one at a time, same arrivals
+    t0 = time.perf_counter()
+    lat = []
+    clock = 0.0
+    for t, conf in stream:
+        now = time.perf_counter() - t0
+        if now < t:
+            time.sleep(t - now)
+        bqa_gb300.run_qa(dict(conf))
+        torch.cuda.synchronize()
+        lat.append(time.perf_counter() - t0 - t)
+    seq_span = time.perf_counter() - t0 - stream[0][0]
+    print(json.dumps({"mode": "serve", "jobs": args.jobs, "rate_per_s": args.rate, "served": served,
+                      "one_at_a_time": {"p50_s": float(np.percentile(lat, 50)),
+                                        "p99_s": float(np.percentile(lat, 99)),
+                                        "jobs_per_s": args.jobs / seq_span}}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -401,7 +459,9 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd"])
+    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve"])
+    ap.add_argument("--jobs", type=int, default=32)
+    ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     args = ap.parse_args()
     logging.basicConfig(level=logging.ERROR)
@@ -412,6 +472,8 @@ def main() -> None:
         run_sweep_mode(args)
     elif args.mode == "svd":
         run_svd_mode(args)
+    elif args.mode == "serve":
+        run_serve_mode(args)
     else:
         run_gpu_arm(args)
 
