@@ -280,7 +280,7 @@ def run_gpu_arm(args) -> None:
         "bp_msg_updates_per_s": ctx.edges_number * sum(sweeps) / (bp_ms / 1000.0) if bp_ms else None,
         "sweeps_per_step": float(np.mean(sweeps)), "bond_dim": window[-1]["bond_dim"],
         "time_split_ms": {k: round(v, 2) for k, v in sorted(by_name.items(), key=lambda kv: -kv[1])},
-        "roofline": {"kernel": "bp_sweep (node_kernel<16,BP,float>)", "bound": "tensor",
+        "roofline": {"kernel": "bp sweep (tiled_half_kernel<3,16> + bp_combine_kernel)", "bound": "tensor",
                      "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": achieved / pk["bf16_tflops"], "peak_source": f"{pk_kind} bf16 burst",
                      "traffic": None, "algorithmic_bytes_per_launch": bp_bytes / max(len(sweep_ev), 1),
@@ -325,8 +325,12 @@ def run_sweep_mode(args) -> None:
     flops, nbytes = job.bp_sweep_cost()
 
     def sweep():
-        job.lib.call("bqa_bp_sweep", cls, len(job.classes), chi, job.dtype, _ptr(job.msgs[0]), _ptr(job.msgs[1]),
-                     _ptr(job.dist_parts), None, job.stream)
+        if job.split_sweeps:
+            job.lib.call("bqa_bp_sweep_split", cls, len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                         _ptr(job.msgs[1]), _ptr(job.lu), ctx.edges_number, _ptr(job.dist_parts), None, job.stream)
+        else:
+            job.lib.call("bqa_bp_sweep", cls, len(job.classes), chi, job.dtype, _ptr(job.msgs[0]), _ptr(job.msgs[1]),
+                         _ptr(job.dist_parts), None, job.stream)
 
     for _ in range(args.warmup):
         sweep()
