@@ -42,6 +42,11 @@ FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 SAMPLE_N = 200
 
 
+# DRAM bytes one chi-16 degree-3 BP sweep moves per node: ncu capture of a 10k-node sweep,
+# tiled_half_kernel<3,16> 829.2 MB + bp_combine_kernel 224.9 MB (the work is per node).
+SWEEP_DRAM_BYTES_PER_NODE = (829.23e6 + 224.94e6) / 10000
+
+
 def peaks() -> tuple[dict, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -283,7 +288,10 @@ def run_gpu_arm(args) -> None:
         "roofline": {"kernel": "bp sweep (tiled_half_kernel<3,16> + bp_combine_kernel)", "bound": "tensor",
                      "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": achieved / pk["bf16_tflops"], "peak_source": f"{pk_kind} bf16 burst",
-                     "traffic": None, "algorithmic_bytes_per_launch": bp_bytes / max(len(sweep_ev), 1),
+                     "traffic": (SWEEP_DRAM_BYTES_PER_NODE * n_el if args.chi == 16 else None),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 10k-node sweep "
+                                       "(half-node kernel 829.2 MB + combine 224.9 MB), scaled by node count",
+                     "algorithmic_bytes_per_launch": bp_bytes / max(len(sweep_ev), 1),
                      "algorithmic_flops_per_launch": bp_flops / max(len(sweep_ev), 1),
                      "note": "complex64 SIMT contraction: 16 d^2 chi^(d+1) FLOP per node per sweep; "
                              "the FP32 CUDA-core peak (~80 TFLOP/s nominal) is the ceiling of this kernel"},
