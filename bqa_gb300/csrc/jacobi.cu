@@ -1,15 +1,17 @@
 // Batched one-sided Jacobi SVD (Hestenes) for the truncation step of the simple update.
 //
 // A segment of W lanes (W = 8, 16 or 32, a power of two >= n) owns one n x n complex
-// matrix, zero-padded to W x W: lane j keeps column j of A and column j of V in registers.
-// A sweep visits every column pair once: in round r (1 <= r < W) lane j pairs with lane
-// j ^ r, which is a perfect matching, and the W-1 rounds cover all pairs.  The pair's
-// Gram entries alpha = |a_p|^2, beta = |a_q|^2, gamma = a_p^H a_q are formed by both lanes
-// with the SAME operand order, so both make bit-identical rotation decisions; the rotation
-//     a_p' = c a_p - s conj(e) a_q,   a_q' = s a_p + c conj(e) a_q,   e = gamma/|gamma|
+// matrix, zero-padded to W x W: lane j keeps column j of A in registers; V is in shared
+// memory.  A sweep visits every column pair once: in round r (1 <= r < W) lane j pairs with
+// lane j ^ r, which is a perfect matching, and the W-1 rounds cover all pairs.  The pair's
+// Gram entries alpha = |a_p|^2, beta = |a_q|^2, gamma = a_p^H a_q are the same bits on both
+// lanes (each norm comes from its owner, gamma from sums formed with the same operand
+// order), so both make the same rotation decision; the unitary rotation
+//     a_p' = c a_p - s conj(e) a_q,   a_q' = c a_q + s e a_p,   e = gamma/|gamma|
 // with t = sign(zeta)/(|zeta| + sqrt(1+zeta^2)), zeta = (beta-alpha)/(2|gamma|),
-// c = 1/sqrt(1+t^2), s = c t, makes the pair orthogonal (the complex form of Hestenes'
-// method, Demmel & Veselic 1992).  At convergence A V = U Sigma with sigma_j = |a_j|.
+// c = 1/sqrt(1+t^2), s = c t, makes the pair orthogonal: a_p'^H a_q' =
+// e ((c^2 - s^2)|gamma| - c s (beta - alpha)) = 0 (the complex form of Hestenes' method,
+// Demmel & Veselic 1992).  At convergence A V = U Sigma with sigma_j = |a_j|.
 // A pair is rotated if |gamma| > tol sqrt(alpha beta).  Sweeps stop when a whole sweep
 // rotates no pair of SIGNIFICANT columns in the warp (both above the noise level of the
 // matrix, |a|^2 > W eps^2 |A|_F^2), or at the sweep cap (then a status bit is set).
@@ -37,29 +39,30 @@ __device__ __forceinline__ C shfl_xor_c(C v, int r, int w) {
     return v;
 }
 
-// V lives in shared memory: the segment's W columns at a padded stride VS = W + 2 (complex
-// elements), so 128-bit column loads from 8 lanes at a time hit 8 distinct bank groups.
-// Two such blocks alternate (a rotation reads one and writes the other), so a lane never
-// holds a whole new column in registers.
+// V lives in shared memory: column j of the segment's V at sV + j * VS, VS = W + 2 complex
+// elements, so 128-bit loads of 8 lanes' columns hit 8 distinct bank groups.  A rotation
+// updates the pair's two V columns in place: the lower lane of the pair rewrites rows
+// [0, W/2) of both columns, the higher lane rows [W/2, W), so one block suffices and each
+// round reads and writes every V element of a rotated pair once.
 template <int W> struct VStride { static constexpr int VS = W + 2; static constexpr int BLOCK = W * VS; };
 
 // One-sided Jacobi on the segment's columns.  a: this lane's column (registers); sV: the
-// segment's two V blocks (shared), initialised to I here.  Returns the block holding V.
+// segment's V block (shared), initialised to I here.  Returns whether it converged.
 template <int W, typename R>
-__device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typename Cx<R>::T* sV, int lane,
-                                               const typename Cx<R>::T** vfinal) {
+__device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typename Cx<R>::T* sV, int lane) {
     using C = typename Cx<R>::T;
     constexpr int VS = VStride<W>::VS;
-    C* vcur = sV;
-    C* vnxt = sV + VStride<W>::BLOCK;
+    constexpr int H = W / 2;
 #pragma unroll
-    for (int i = 0; i < W; ++i) vcur[lane * VS + i] = c_make(i == lane ? R(1) : R(0), R(0));
+    for (int i = 0; i < W; ++i) sV[lane * VS + i] = c_make(i == lane ? R(1) : R(0), R(0));
     __syncwarp();
-    *vfinal = vcur;
     const R tol = (R)W * jacobi_eps<R>();
-    R fro2 = 0;
+    // |a_lane|^2, recomputed (same operation order) whenever the column changes; the pair's
+    // norms come from their owners, so both lanes of a pair see the same alpha and beta
+    R nown = 0;
 #pragma unroll
-    for (int i = 0; i < W; ++i) fro2 += c_abs2(a[i]);
+    for (int i = 0; i < W; ++i) nown = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, nown));
+    R fro2 = nown;
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) fro2 += __shfl_xor_sync(BQA_FULL_MASK, fro2, o, W);
     const R col_floor = fmax((R)W * jacobi_eps<R>() * jacobi_eps<R>() * fro2, sizeof(R) == 4 ? R(1e-30) : R(1e-280));
@@ -69,63 +72,72 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
         for (int r = 1; r < W; ++r) {
             const int partner = lane ^ r;
             const bool low = lane < partner;
-            // Gram entries of the pair from sums both lanes form bit-identically: the squared
-            // norms, Sx = sum Re(conj(own) partner), and the cross sums S1 = sum own.x partner.y,
-            // S2 = sum own.y partner.x (on the other lane of the pair S1 and S2 swap roles).
-            R nown = 0, npart = 0, sx = 0, s1 = 0, s2 = 0;
+            const R npart = __shfl_xor_sync(BQA_FULL_MASK, nown, r, W);
+            // gamma = p^H q (p = column of the lower lane, q = of the higher) from sums both
+            // lanes form bit-identically: Sx = sum Re(conj(own) partner) and the cross sums
+            // S1 = sum own.x partner.y, S2 = sum own.y partner.x (they swap roles on the
+            // other lane; fma(a, b, c) == fma(b, a, c)).
+            R sx = 0, s1 = 0, s2 = 0;
 #pragma unroll
             for (int i = 0; i < W; ++i) {
                 const C o = shfl_xor_c(a[i], r, W);
-                nown = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, nown));
-                npart = fma(o.x, o.x, fma(o.y, o.y, npart));
                 sx = fma(a[i].x, o.x, fma(a[i].y, o.y, sx));
                 s1 = fma(a[i].x, o.y, s1);
                 s2 = fma(a[i].y, o.x, s2);
             }
-            // p = column of the lower lane, q = of the higher: gamma = p^H q
             const R alpha = low ? nown : npart, beta = low ? npart : nown;
             const C g = c_make(sx, low ? s1 - s2 : s2 - s1);
             const R gabs = sqrt(c_abs2(g));
             const bool rot = alpha > R(0) && beta > R(0) && gabs > tol * sqrt(alpha) * sqrt(beta);
             if (__any_sync(BQA_FULL_MASK, rot)) {
-                // own' = k1 own + k2 partner; lower lane: (c, -s conj(e)), higher: (c conj(e), s)
-                C k1 = c_make(R(1), R(0)), k2 = c_zero<C>();
+                // p' = c p - s conj(e) q,  q' = c q + s e p  (wp = -s conj(e), wq = s e);
+                // a lane that does not rotate keeps c = 1, w = 0, an exact no-op
+                R c = R(1);
+                C wp = c_zero<C>(), wq = c_zero<C>();
                 if (rot) {
                     const R zeta = (beta - alpha) / (R(2) * gabs);
                     const R t = copysign(R(1), zeta) / (fabs(zeta) + hypot(R(1), zeta));
-                    const R c = R(1) / sqrt(fma(t, t, R(1)));
+                    c = R(1) / sqrt(fma(t, t, R(1)));
                     const R sn = c * t;
-                    const C eb = c_make(g.x / gabs, -g.y / gabs);  // conj(e)
-                    k1 = low ? c_make(c, R(0)) : c_scale(eb, c);
-                    k2 = low ? c_scale(eb, -sn) : c_make(sn, R(0));
+                    const R ex = g.x / gabs, ey = g.y / gabs;
+                    wp = c_make(-sn * ex, sn * ey);
+                    wq = c_make(sn * ex, sn * ey);
                     rotated |= (alpha > col_floor && beta > col_floor);
                 }
+                const C wown = low ? wp : wq;
+                R n2 = 0;
 #pragma unroll
                 for (int i = 0; i < W; ++i) {
                     const C o = shfl_xor_c(a[i], r, W);
-                    a[i] = c_fma(k2, o, c_mul(k1, a[i]));
+                    a[i] = c_fma(wown, o, c_scale(a[i], c));
+                    n2 = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, n2));
                 }
-                // V: read own and partner columns of the current block, write own of the next
-                const C* vown = vcur + lane * VS;
-                const C* vpart = vcur + partner * VS;
-                C* vout = vnxt + lane * VS;
+                nown = n2;
+                if (rot) {
+                    C* vp = sV + (low ? lane : partner) * VS + (low ? 0 : H);
+                    C* vq = sV + (low ? partner : lane) * VS + (low ? 0 : H);
 #pragma unroll
-                for (int i = 0; i < W; i += 2) {
-                    C vo0, vo1, vp0, vp1;
-                    if (sizeof(R) == 4) {
-                        const float4 x = *reinterpret_cast<const float4*>(vown + i);
-                        const float4 y = *reinterpret_cast<const float4*>(vpart + i);
-                        vo0 = c_make((R)x.x, (R)x.y); vo1 = c_make((R)x.z, (R)x.w);
-                        vp0 = c_make((R)y.x, (R)y.y); vp1 = c_make((R)y.z, (R)y.w);
-                    } else {
-                        vo0 = vown[i]; vo1 = vown[i + 1]; vp0 = vpart[i]; vp1 = vpart[i + 1];
+                    for (int i = 0; i < H; i += 2) {
+                        C p0, p1, q0, q1;
+                        if (sizeof(R) == 4) {
+                            const float4 x = *reinterpret_cast<const float4*>(vp + i);
+                            const float4 y = *reinterpret_cast<const float4*>(vq + i);
+                            p0 = c_make((R)x.x, (R)x.y); p1 = c_make((R)x.z, (R)x.w);
+                            q0 = c_make((R)y.x, (R)y.y); q1 = c_make((R)y.z, (R)y.w);
+                        } else {
+                            p0 = vp[i]; p1 = vp[i + 1]; q0 = vq[i]; q1 = vq[i + 1];
+                        }
+                        const C np0 = c_fma(wp, q0, c_scale(p0, c)), np1 = c_fma(wp, q1, c_scale(p1, c));
+                        const C nq0 = c_fma(wq, p0, c_scale(q0, c)), nq1 = c_fma(wq, p1, c_scale(q1, c));
+                        if (sizeof(R) == 4) {
+                            *reinterpret_cast<float4*>(vp + i) = make_float4((float)np0.x, (float)np0.y, (float)np1.x, (float)np1.y);
+                            *reinterpret_cast<float4*>(vq + i) = make_float4((float)nq0.x, (float)nq0.y, (float)nq1.x, (float)nq1.y);
+                        } else {
+                            vp[i] = np0; vp[i + 1] = np1; vq[i] = nq0; vq[i + 1] = nq1;
+                        }
                     }
-                    vout[i] = c_fma(k2, vp0, c_mul(k1, vo0));
-                    vout[i + 1] = c_fma(k2, vp1, c_mul(k1, vo1));
                 }
                 __syncwarp();
-                C* tt = vcur; vcur = vnxt; vnxt = tt;
-                *vfinal = vcur;
             }
         }
         if (!__any_sync(BQA_FULL_MASK, rotated)) return true;
@@ -153,16 +165,15 @@ __global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>
     constexpr int VS = VStride<W>::VS;
     extern __shared__ double4 smem_raw[];
     const int lane = threadIdx.x & (W - 1);
-    C* sV = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / W) * 2 * VStride<W>::BLOCK;
+    C* sV = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / W) * VStride<W>::BLOCK;
     const int mat = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = mat < count;
     const size_t base = (size_t)(live ? mat : 0) * n * n;
     C a[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
-    const C* vblk;
-    const bool ok = jacobi_columns<W, R>(a, sV, lane, &vblk);
-    const C* v = vblk + lane * VS;
+    const bool ok = jacobi_columns<W, R>(a, sV, lane);
+    const C* v = sV + lane * VS;
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
     R nrm2 = 0;
 #pragma unroll
@@ -197,7 +208,7 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
     const int lane = threadIdx.x & (W - 1);
     const int seg = threadIdx.x / W;
     C* sm = reinterpret_cast<C*>(smem_raw) + (size_t)seg * W * W;
-    C* sV = reinterpret_cast<C*>(smem_raw) + (size_t)128 * W + (size_t)seg * 2 * VStride<W>::BLOCK;
+    C* sV = reinterpret_cast<C*>(smem_raw) + (size_t)128 * W + (size_t)seg * VStride<W>::BLOCK;
     const int half = edges / 2;
     const int p = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = p < half;
@@ -223,9 +234,8 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
             a[i] = acc;
         }
     }
-    const C* vblk;
-    const bool ok = jacobi_columns<W, R>(a, sV, lane, &vblk);
-    const C* v = vblk + lane * VS;
+    const bool ok = jacobi_columns<W, R>(a, sV, lane);
+    const C* v = sV + lane * VS;
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
     R nrm2 = 0;
 #pragma unroll
@@ -281,7 +291,7 @@ static int launch_env(const void* m, int count, int n, double eps, void* lu, voi
     using C = typename Cx<R>::T;
     const int per_block = 128 / W;
     const int blocks = (count + per_block - 1) / per_block;
-    const size_t smem = (size_t)(128 / W) * 2 * VStride<W>::BLOCK * sizeof(C);
+    const size_t smem = (size_t)(128 / W) * VStride<W>::BLOCK * sizeof(C);
     int rc = ensure_smem((const void*)env_factor_kernel<W, R>, smem, "env_factor");
     if (rc) return rc;
     env_factor_kernel<W, R><<<blocks, 128, smem, st>>>(static_cast<const C*>(m), count, n, (R)eps,
@@ -296,7 +306,7 @@ static int launch_canon(const void* lu, const void* ul, int edges, int n, double
     const int per_block = 128 / W;
     const int half = edges / 2;
     const int blocks = (half + per_block - 1) / per_block;
-    const size_t smem = ((size_t)128 * W + (size_t)(128 / W) * 2 * VStride<W>::BLOCK) * sizeof(C);
+    const size_t smem = ((size_t)128 * W + (size_t)(128 / W) * VStride<W>::BLOCK) * sizeof(C);
     int rc = ensure_smem((const void*)bond_canon_kernel<W, R>, smem, "bond_canon");
     if (rc) return rc;
     bond_canon_kernel<W, R><<<blocks, 128, smem, st>>>(static_cast<const C*>(lu), static_cast<const C*>(ul), edges, n,
