@@ -462,6 +462,63 @@ def run_serve_mode(args) -> None:
                                         "jobs_per_s": args.jobs / seq_span}}))
 
 
+def run_layout_mode(args) -> None:
+    """Degree-class compilation of an n-node random 3-regular job: config analysis, host
+    compiler and device compiler (kernels alone by CUDA events, and with the edge upload and
+    map read-back), median of --steps runs after --warmup."""
+    import torch
+    from bqa_gb300 import config as cfg, instances, layout
+    conf = instances.headline_gpu_job(n=args.n, steps=3)
+    c = cfg.analyse_config(conf, edge_arrays=True)
+    edges = c[cfg.EDGES_KEY].edges
+    n = args.n
+
+    def timed(fn):
+        ts = []
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)) * 1e3
+
+    host_ms = timed(lambda: layout.compile_layout(edges, n))
+    dev_ms = timed(lambda: layout.compile_layout_device(edges, n))
+    ctx_ms = timed(lambda: layout.build_context(conf, layout_device="cuda"))
+    # kernels alone: edges already on the device
+    from bqa_gb300 import _lib
+    lib = _lib.load()
+    dev = torch.device("cuda")
+    E = edges.shape[0]
+    d_edges = torch.as_tensor(edges.astype(np.int32), device=dev)
+    i32 = dict(dtype=torch.int32, device=dev)
+    bufs = [torch.empty(n, **i32) for _ in range(5)]
+    order = torch.empty(E, **i32)
+    first, count, status = torch.empty(256, **i32), torch.empty(256, **i32), torch.zeros(1, **i32)
+    node_ids, slots = torch.empty(n, **i32), torch.empty(3 * n, **i32)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ks = []
+    for i in range(args.warmup + args.steps):
+        e0.record(st)
+        lib.call("bqa_layout_degrees", d_edges.data_ptr(), E, n, 255, bufs[0].data_ptr(), bufs[1].data_ptr(),
+                 order.data_ptr(), bufs[2].data_ptr(), first.data_ptr(), count.data_ptr(), status.data_ptr(),
+                 st.cuda_stream)
+        lib.call("bqa_layout_class", 3, n, bufs[0].data_ptr(), bufs[1].data_ptr(), order.data_ptr(), n, E, None,
+                 None, node_ids.data_ptr(), bufs[3].data_ptr(), None, slots.data_ptr(), None, None, None,
+                 st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            ks.append(e0.elapsed_time(e1))
+    print(json.dumps({"mode": "layout", "n": n, "directed_edges": int(E),
+                      "host_compile_ms": host_ms, "device_compile_ms": dev_ms,
+                      "device_kernels_ms": float(np.median(ks)),
+                      "build_context_ms": ctx_ms}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -471,7 +528,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve"])
+    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout"])
     ap.add_argument("--jobs", type=int, default=32)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--precision", default="single", choices=["single", "double"])
@@ -486,6 +543,8 @@ def main() -> None:
         run_svd_mode(args)
     elif args.mode == "serve":
         run_serve_mode(args)
+    elif args.mode == "layout":
+        run_layout_mode(args)
     else:
         run_gpu_arm(args)
 

@@ -9,12 +9,14 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 2
+ABI_VERSION = 3
 BQA_C64 = 0
 BQA_C128 = 1
 
 BQA_OK = 0
 BQA_STATUS_SVD_NOT_CONVERGED = 1
+BQA_STATUS_LAYOUT_EDGE = 2
+BQA_STATUS_LAYOUT_DEGREE = 4
 
 
 class BqaClass(ctypes.Structure):
@@ -60,6 +62,11 @@ SIGNATURES = {
                                     c_void_p]),
     "bqa_canonicalize_noalloc": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_void_p]),
+    "bqa_layout_degrees": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bqa_layout_class": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p]),
 }
 
 

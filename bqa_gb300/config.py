@@ -21,7 +21,11 @@ backends registered in :data:`BACKENDS` are accepted.
 from __future__ import annotations
 
 import logging
+from itertools import chain
 from math import isclose
+from typing import NamedTuple
+
+import numpy as np
 
 log = logging.getLogger(__name__)
 
@@ -280,8 +284,96 @@ def _schedule(schedule):
         raise ConfigSyntaxError(f"Invalid schedule {schedule}") from e
 
 
-def analyse_config(config) -> dict:
-    """Validated config with defaults applied (reference ``_analyse_config``)."""
+class EdgeArrays(NamedTuple):
+    """Analysed edges as arrays: ``edges[p]`` = (src, dst) of directed edge (message slot)
+    ``p`` -- the user's edges in order, then their reversals -- and ``ampl[p]`` its coupling."""
+    edges: np.ndarray   # (E, 2) int64
+    ampl: np.ndarray    # (E,) float64
+
+
+# edge collections from this size are first offered to the vectorised acceptance test
+FAST_EDGES_MIN = 1024
+
+
+def _all_subclasses(kinds, base) -> bool:
+    return all(issubclass(k, base) for k in kinds)
+
+
+def _edges_fast(edges) -> EdgeArrays | None:
+    """Vectorised form of ``_edges`` for large edge collections: the same acceptance rules
+    (pairs of a 2-sequence of non-negative ``int`` ends that differ and a ``float``/``int``
+    coupling, no edge given twice in either orientation), checked on whole arrays.  Returns
+    None when any rule might fail; ``_edges`` then walks the input and raises the exact error."""
+    if isinstance(edges, dict):
+        ids, vals = list(edges.keys()), list(edges.values())
+    elif isinstance(edges, (list, tuple)):
+        if not _all_subclasses(set(map(type, edges)), (list, tuple)) or set(map(len, edges)) != {2}:
+            return None
+        ids, vals = [e[0] for e in edges], [e[1] for e in edges]
+    else:
+        return None
+    if not ids:
+        return None
+    if not _all_subclasses(set(map(type, ids)), (list, tuple)) or set(map(len, ids)) != {2}:
+        return None
+    if not _all_subclasses(set(map(type, chain.from_iterable(ids))), int):
+        return None
+    if not _all_subclasses(set(map(type, vals)), (int, float)):
+        return None
+    try:
+        arr = np.array(ids, dtype=np.int64)
+        ampl = np.array(vals, dtype=np.float64)
+    except (OverflowError, ValueError, TypeError):
+        return None
+    if arr.ndim != 2 or arr.shape[1] != 2 or (arr < 0).any() or (arr[:, 0] == arr[:, 1]).any():
+        return None
+    lo, hi = np.minimum(arr[:, 0], arr[:, 1]), np.maximum(arr[:, 0], arr[:, 1])
+    if int(hi.max()) >= 2 ** 31:
+        return None
+    key = np.sort(lo * (2 ** 31) + hi)
+    if (key[1:] == key[:-1]).any():
+        return None
+    return EdgeArrays(np.concatenate([arr, arr[:, ::-1]]), np.concatenate([ampl, ampl]))
+
+
+class NodeArrays(NamedTuple):
+    """Analysed node fields as arrays, in the user's order."""
+    ids: np.ndarray     # (m,) int64
+    fields: np.ndarray  # (m,) float64
+
+
+def _nodes_fast(nodes) -> NodeArrays | None:
+    """Vectorised form of ``_nodes`` (same acceptance rules: pairs of a non-negative ``int`` id
+    and a ``float``/``int`` field, no id twice); None when any rule might fail."""
+    if isinstance(nodes, dict):
+        ids, vals = list(nodes.keys()), list(nodes.values())
+    elif isinstance(nodes, (list, tuple)):
+        if not _all_subclasses(set(map(type, nodes)), (list, tuple)) or set(map(len, nodes)) != {2}:
+            return None
+        ids, vals = [e[0] for e in nodes], [e[1] for e in nodes]
+    else:
+        return None
+    if not ids or not _all_subclasses(set(map(type, ids)), int) \
+            or not _all_subclasses(set(map(type, vals)), (int, float)):
+        return None
+    try:
+        arr = np.array(ids, dtype=np.int64)
+        fields = np.array(vals, dtype=np.float64)
+    except (OverflowError, ValueError, TypeError):
+        return None
+    if (arr < 0).any():
+        return None
+    if not isinstance(nodes, dict):   # dict keys are distinct already
+        srt = np.sort(arr)
+        if (srt[1:] == srt[:-1]).any():
+            return None
+    return NodeArrays(arr, fields)
+
+
+def analyse_config(config, edge_arrays: bool = False) -> dict:
+    """Validated config with defaults applied (reference ``_analyse_config``).  With
+    ``edge_arrays`` the edges and nodes come back as ``EdgeArrays`` and ``NodeArrays``
+    instead of dicts (large collections are then validated by whole-array checks)."""
     if not isinstance(config, dict):
         raise ConfigSyntaxError(f"Config must be a dict, but got type {type(config)}")
     try:
@@ -301,9 +393,27 @@ def analyse_config(config) -> dict:
             SEED_KEY: _take(config, SEED_KEY, DEFAULTS[SEED_KEY], w),
             DAMPING_KEY: _take(config, DAMPING_KEY, DEFAULTS[DAMPING_KEY], w),
         }
+        nodes_out = None
+        if edge_arrays and isinstance(nodes, (dict, list, tuple)) and len(nodes) >= FAST_EDGES_MIN:
+            nodes_out = _nodes_fast(nodes)
+        if nodes_out is None:
+            nodes_out = _nodes(nodes)
+            if edge_arrays:
+                nodes_out = NodeArrays(np.array(list(nodes_out.keys()), dtype=np.int64),
+                                       np.array(list(nodes_out.values()), dtype=np.float64))
+        if edge_arrays:
+            fast = _edges_fast(edges) if isinstance(edges, (dict, list, tuple)) and len(edges) >= FAST_EDGES_MIN \
+                else None
+            if fast is None:
+                both = _edges(edges)
+                fast = EdgeArrays(np.array(list(both.keys()), dtype=np.int64).reshape(-1, 2),
+                                  np.array(list(both.values()), dtype=np.float64))
+            edges_out = fast
+        else:
+            edges_out = _edges(edges)
         return {
-            NODES_KEY: _nodes(nodes),
-            EDGES_KEY: _edges(edges),
+            NODES_KEY: nodes_out,
+            EDGES_KEY: edges_out,
             DEFAULT_FIELD_KEY: _number(out[DEFAULT_FIELD_KEY]),
             SCHEDULE_KEY: _schedule(schedule),
             MAX_BOND_DIM_KEY: _positive_int(out[MAX_BOND_DIM_KEY]),

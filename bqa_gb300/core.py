@@ -22,7 +22,9 @@ log = logging.getLogger(__name__)
 def run_qa(config, device=None, as_arrays: bool = False) -> list:
     """Run a job; with ``as_arrays`` the result values stay numpy arrays (n x 3 float64 Bloch
     vectors, n int64 outcomes) instead of nested lists."""
-    ctx = build_context(config)
+    import torch
+    on_gpu = torch.cuda.is_available()
+    ctx = build_context(config, layout_device=(device if device is not None else "cuda") if on_gpu else None)
     log.info("Context is built")
     job = Annealer(ctx, device=device)
     total = len(ctx.instructions)

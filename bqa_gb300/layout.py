@@ -111,23 +111,78 @@ def compile_layout(edge_list: np.ndarray, nodes_number: int):
     return classes, deg, node_position
 
 
-def build_context(config: dict) -> Context:
-    """Analyse a user config and compile its degree classes (reference ``config_to_context``)."""
-    c = cfg.analyse_config(config)
-    edges = c[cfg.EDGES_KEY]
-    if len(edges) == 0:
+def compile_layout_device(edge_list: np.ndarray, nodes_number: int, device=None, max_degree: int = 255):
+    """``compile_layout`` computed on the GPU (``bqa_layout_degrees`` + ``bqa_layout_class``):
+    degree histogram and slot grouping by atomics, per-node slot sort, per-degree stream
+    compaction by a single-CTA scan.  Returns the same ``(classes, deg, node_position)``,
+    bit for bit, copied back to host memory."""
+    import torch
+    from . import _lib
+    lib = _lib.load()
+    dev = torch.device(device if device is not None else "cuda")
+    edges = np.asarray(edge_list, dtype=np.int64).reshape(-1, 2)
+    E, n = edges.shape[0], int(nodes_number)
+    if E >= 2 ** 31 or n >= 2 ** 31:
+        raise ValueError("the device layout compiler takes fewer than 2^31 edges and nodes")
+    d_edges = torch.as_tensor(edges.astype(np.int32), device=dev)
+    i32 = dict(dtype=torch.int32, device=dev)
+    deg, start, fill, position = (torch.empty(n, **i32) for _ in range(4))
+    order = torch.empty(E, **i32)
+    first = torch.empty(max_degree + 1, **i32)
+    count = torch.empty(max_degree + 1, **i32)
+    status = torch.zeros(1, **i32)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    p = lambda t: t.data_ptr()
+    lib.call("bqa_layout_degrees", p(d_edges), E, n, max_degree, p(deg), p(start), p(order), p(fill), p(first),
+             p(count), p(status), stream)
+    st = int(status.cpu()[0])
+    if st & _lib.BQA_STATUS_LAYOUT_EDGE:
+        raise ValueError("edge list has an endpoint outside [0, n), a self-loop, or a slot whose reversal "
+                         "is not at slot + E/2")
+    if st & _lib.BQA_STATUS_LAYOUT_DEGREE:
+        raise ValueError(f"a node has degree above {max_degree}")
+    first_h, count_h = first.cpu().numpy(), count.cpu().numpy()
+    degrees = sorted((d for d in range(max_degree + 1) if count_h[d] > 0), key=lambda d: int(first_h[d]))
+    out = {}
+    for d in degrees:
+        B = int(count_h[d])
+        node_ids = torch.empty(B, **i32)
+        slots = torch.empty(B * d, **i32) if d > 0 else None
+        lib.call("bqa_layout_class", d, B, p(deg), p(start), p(order), n, E, None, None, p(node_ids), p(position),
+                 None, p(slots) if slots is not None else None, None, None, None, stream)
+        out[d] = (node_ids, slots)
+    classes = {}
+    for d, (node_ids, slots) in out.items():
+        B = node_ids.shape[0]
+        sl = (slots.view(B, d).T.cpu().numpy().astype(np.int64) if d > 0
+              else np.zeros((0, B), dtype=np.int64))
+        classes[d] = (node_ids.cpu().numpy().astype(np.int64), sl)
+    return classes, deg.cpu().numpy().astype(np.int64), position.cpu().numpy().astype(np.int64)
+
+
+# directed-edge count from which build_context compiles on the device when given one
+DEVICE_LAYOUT_MIN_EDGES = 1 << 16
+
+
+def build_context(config: dict, layout_device=None) -> Context:
+    """Analyse a user config and compile its degree classes (reference ``config_to_context``).
+    With ``layout_device`` set, graphs of at least ``DEVICE_LAYOUT_MIN_EDGES`` directed edges
+    are compiled by the device layout compiler (identical maps)."""
+    c = cfg.analyse_config(config, edge_arrays=True)
+    edge_list, ampl = c[cfg.EDGES_KEY]
+    if edge_list.shape[0] == 0:
         raise cfg.ConfigSyntaxError("Invalid config") from cfg.ConfigSyntaxError(
             "`edges` must hold at least one edge")
-    edge_list = np.array(list(edges.keys()), dtype=np.int64)
-    ampl = np.array(list(edges.values()), dtype=np.float64)
     E = edge_list.shape[0]
     half = E // 2
-    nodes_cfg = c[cfg.NODES_KEY]
-    n = 1 + max(max(nodes_cfg.keys(), default=-1), int(edge_list.max()))
+    node_ids, node_fields = c[cfg.NODES_KEY]
+    n = 1 + max(int(node_ids.max()) if node_ids.size else -1, int(edge_list.max()))
     node_ampl = np.full(n, c[cfg.DEFAULT_FIELD_KEY], dtype=np.float64)
-    for k, v in nodes_cfg.items():
-        node_ampl[k] = v
-    classes, deg, node_position = compile_layout(edge_list, n)
+    node_ampl[node_ids] = node_fields
+    if layout_device is not None and E >= DEVICE_LAYOUT_MIN_EDGES:
+        classes, deg, node_position = compile_layout_device(edge_list, n, layout_device)
+    else:
+        classes, deg, node_position = compile_layout(edge_list, n)
     layouts = {}
     for d, (nodes, slots) in classes.items():
         rev = (slots + half) % E if d > 0 else slots

@@ -95,7 +95,7 @@ class JobServer:
     def submit(self, config: dict, arrival: float | None = None) -> int:
         """Queue a job (arrival = now by default); returns its id.  Configs that cannot fit the
         budget even alone are rejected with ValueError."""
-        ctx = build_context(config)
+        ctx = build_context(config, layout_device=self.device)
         fp = job_footprint(ctx, self.precision)
         if fp > self.budget:
             raise ValueError(f"job needs {fp} device bytes, above the server budget {self.budget}")

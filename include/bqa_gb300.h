@@ -46,7 +46,10 @@ enum { BQA_C64 = 0, BQA_C128 = 1 };
 
 /* device status word bits (written by kernels into a caller int32) */
 enum {
-    BQA_STATUS_SVD_NOT_CONVERGED = 1  /* a Jacobi SVD hit its sweep cap */
+    BQA_STATUS_SVD_NOT_CONVERGED = 1, /* a Jacobi SVD hit its sweep cap */
+    BQA_STATUS_LAYOUT_EDGE = 2,       /* an edge endpoint outside [0, n), a self-loop, or slot p + E/2
+                                         not the reversal of slot p */
+    BQA_STATUS_LAYOUT_DEGREE = 4      /* a node's degree exceeds max_degree */
 };
 
 /* One degree class: the B nodes of degree d (reference ``Layout``,
@@ -207,6 +210,36 @@ int32_t bqa_project_nodes(void* tensors, int32_t count, int32_t node_elems, int3
  */
 int32_t bqa_canonicalize_noalloc(const void* ext_msgs, int32_t edges, int32_t n, int32_t dtype, double eps,
                                  void* canon, void* lmbds, void* colmax, int32_t* status, void* stream);
+
+/*
+ * Degree-class compilation on the device, first stage (replaces the per-node loop of
+ * _make_degree_to_layout, src/bqa/config/config_canonicalization.py:62-131).
+ * edges: int32 [E][2] (src, dst) in message-slot order, E even, slot p + E/2 the reversal of
+ * slot p (the reference's edge dict: user edges, then their reversals).  Outputs
+ * (caller-allocated device int32): deg[n]; start[n] = exclusive scan of deg; order[E] = the
+ * slots grouped by source node, increasing slot inside a group (bond k of node v is
+ * order[start[v] + k]); class_first[max_degree + 1] = lowest node id of each degree (only
+ * meaningful where class_count > 0); class_count[max_degree + 1].  fill[n] is scratch.
+ * Bad edges set BQA_STATUS_LAYOUT_EDGE and nodes of degree > max_degree
+ * BQA_STATUS_LAYOUT_DEGREE in *status; the outputs are then undefined.  The host orders the
+ * classes by class_first (first appearance over node ids, as the reference's dict does).
+ */
+int32_t bqa_layout_degrees(const int32_t* edges, int32_t E, int32_t n, int32_t max_degree, int32_t* deg,
+                           int32_t* start, int32_t* order, int32_t* fill, int32_t* class_first,
+                           int32_t* class_count, int32_t* status, void* stream);
+
+/*
+ * Second stage, one call per degree class (reference ``Layout`` fields,
+ * src/bqa/config/config_canonicalization.py:25-32,82-131): node_ids[count] = the nodes of
+ * this degree in increasing id; position[v] = index of v in its class (written for this
+ * class's nodes); node-major [count][degree] maps out_pos (slot node -> nbr_k), in_pos
+ * ((out + E/2) % E), lmbd_pos (out % (E/2)), edge_ampl (slot_ampl[out], the coupling J);
+ * node_ampl[count] = node_field[v].  in_pos, lmbd_pos, edge_ampl, node_ampl may be NULL.
+ */
+int32_t bqa_layout_class(int32_t degree, int32_t count, const int32_t* deg, const int32_t* start,
+                         const int32_t* order, int32_t n, int32_t E, const double* slot_ampl,
+                         const double* node_field, int32_t* node_ids, int32_t* position, int32_t* in_pos,
+                         int32_t* out_pos, int32_t* lmbd_pos, double* edge_ampl, double* node_ampl, void* stream);
 
 #ifdef __cplusplus
 }
