@@ -275,28 +275,31 @@ __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kern
         tiled::product<D, CHI, TH, SW>(X, Y, sMt + k * N2, k);
         __syncthreads();
     };
-    auto emit = [&](int idx, const float2* R) {
-        tiled::close_tiled<CHI, TH, S::KS, PER_S, SW>(sT, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
+    // P[a][b] = sum conj(X[..a..]) R[..b..] over every index but bond idx
+    auto emit = [&](int idx, const float2* X, const float2* R) {
+        tiled::close_tiled<CHI, TH, S::KS, PER_S, SW>(X, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
         __syncthreads();
         write_outputs<MODE, float>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
         __syncthreads();
     };
     if (D == 2) {
-        prod(sT, sA, 1); emit(0, sA);
-        prod(sT, sA, 0); emit(1, sA);
+        prod(sT, sA, 1); emit(0, sT, sA);
+        prod(sT, sA, 0); emit(1, sT, sA);
     } else if (D == 3) {
-        prod(sT, sA, 0);                    // U = T x0
-        prod(sA, sB, 1); emit(2, sB);       // U x1
-        prod(sA, sB, 2); emit(1, sB);       // U x2
-        prod(sT, sA, 1);                    // T x1
-        prod(sA, sB, 2); emit(0, sB);       // (T x1) x2
+        prod(sT, sA, 1);                    // V1 = T x1
+        prod(sT, sB, 2);                    // V2 = T x2
+        emit(0, sA, sB);
+        tiled::product_first_inplace<D, CHI, TH, SW, 2>(sT, sMt);   // V0 = T x0 over T
+        __syncthreads();
+        emit(2, sT, sA);
+        emit(1, sT, sB);
     } else {
         prod(sT, sB, 0); prod(sB, sA, 1);   // U = T x0 x1
-        prod(sA, sB, 2); emit(3, sB);
-        prod(sA, sB, 3); emit(2, sB);
+        prod(sA, sB, 2); emit(3, sT, sB);
+        prod(sA, sB, 3); emit(2, sT, sB);
         prod(sT, sB, 2); prod(sB, sA, 3);   // V = T x2 x3
-        prod(sA, sB, 0); emit(1, sB);
-        prod(sA, sB, 1); emit(0, sB);
+        prod(sA, sB, 0); emit(1, sT, sB);
+        prod(sA, sB, 1); emit(0, sT, sB);
     }
     if (MODE == MODE_BP) {
         num2 = block_max(num2, sRed);
@@ -334,7 +337,7 @@ static int try_tiled(const NodeArgs<float>& a, int count, cudaStream_t st, int* 
 
 // Half-node register-tiled kernel: CTA (node, s) computes P_s of every bond of the node and
 // writes it to pm[slot][s] (the layout of the PSPLIT mode); bp_combine_kernel turns
-// P_0 + P_1 into messages.  Same schedule of shared bond products as tiled_node_kernel.
+// P_0 + P_1 into messages.  Same contraction schedules as tiled_node_kernel.
 template <int D, int CHI>
 __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_kernel(NodeArgs<float> a) {
     using S = tiled::HalfShape<D, CHI>;
@@ -371,8 +374,8 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         tiled::product<D, CHI, TH, SW, 1>(X, Y, sMt + k * N2, k);
         __syncthreads();
     };
-    auto emit = [&](int idx, const float2* R) {
-        tiled::close_tiled<CHI, TH, S::KS, PS, SW, 1>(sT, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
+    auto emit = [&](int idx, const float2* X, const float2* R) {
+        tiled::close_tiled<CHI, TH, S::KS, PS, SW, 1>(X, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
         __syncthreads();
         float4* og = reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2);
         const float4* sp = reinterpret_cast<const float4*>(sP);
@@ -380,21 +383,23 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         __syncthreads();
     };
     if (D == 2) {
-        prod(sT, sA, 1); emit(0, sA);
-        prod(sT, sA, 0); emit(1, sA);
+        prod(sT, sA, 1); emit(0, sT, sA);
+        prod(sT, sA, 0); emit(1, sT, sA);
     } else if (D == 3) {
-        prod(sT, sA, 0);
-        prod(sA, sB, 1); emit(2, sB);
-        prod(sA, sB, 2); emit(1, sB);
         prod(sT, sA, 1);
-        prod(sA, sB, 2); emit(0, sB);
+        prod(sT, sB, 2);
+        emit(0, sA, sB);
+        tiled::product_first_inplace<D, CHI, TH, SW, 1>(sT, sMt);
+        __syncthreads();
+        emit(2, sT, sA);
+        emit(1, sT, sB);
     } else {
         prod(sT, sB, 0); prod(sB, sA, 1);
-        prod(sA, sB, 2); emit(3, sB);
-        prod(sA, sB, 3); emit(2, sB);
+        prod(sA, sB, 2); emit(3, sT, sB);
+        prod(sA, sB, 3); emit(2, sT, sB);
         prod(sT, sB, 2); prod(sB, sA, 3);
-        prod(sA, sB, 0); emit(1, sB);
-        prod(sA, sB, 1); emit(0, sB);
+        prod(sA, sB, 0); emit(1, sT, sB);
+        prod(sA, sB, 1); emit(0, sT, sB);
     }
 }
 

@@ -8,7 +8,7 @@
 //       the last bond (B = 1).  Operands come in as 128-bit loads (two complex values) from
 //       the tensor and from the transposed message Mt[j][i] = M[i][j].
 //   closing contraction for bond idx:
-//       P_s[a][b] = sum_{x,y} conj(T[s][x][a][y]) R[s][x][b][y]
+//       P_s[a][b] = sum_{x,y} conj(X[s][x][a][y]) R[s][x][b][y]   (X = T or a product of T)
 //       a thread owns a 4x4 tile of (a, b) for one K-slice; the KS slices of a tile sit in
 //       adjacent lanes and are summed with xor-shuffles.
 //
@@ -18,9 +18,16 @@
 // group; with it, 8 consecutive rows hit 8 distinct groups, and every aligned pair of
 // complex values stays contiguous (bit 0 is untouched).
 //
-// The outgoing messages share bond products: with U = T x_0 M_0, the messages of bonds 2 and
-// 1 (D = 3) close U x_1 M_1 and U x_2 M_2, and bond 0 closes (T x_1 M_1) x_2 M_2: 5 products
-// and 3 closing contractions instead of 6 + 3 (D = 4: 8 + 4 instead of 12 + 4).
+// D = 3 splits the two messages of each outgoing message between the two sides of the
+// closing contraction.  BP messages are Hermitian (M^H = M), so
+//     sum_x conj(T[..x..]) M[x][y] = conj((T x M)[..y..]),
+// and with V_k = T x_k M_k the message of bond 0 is the closing contraction of V_1 (conj
+// side) with V_2, bond 1 of V_0 with V_2, bond 2 of V_0 with V_1: 3 products and 3 closing
+// contractions instead of the reference order's 6 + 3.  V_0 is formed in place over T once T
+// has served V_1 and V_2, so three tensor buffers still suffice.  D = 4 shares bond
+// products instead: with U = T x_0 M_0 x_1 M_1 the messages of bonds 3 and 2 close U x_2 M_2
+// and U x_3 M_3, and V = T x_2 M_2 x_3 M_3 serves bonds 1 and 0: 8 products and 4 closing
+// contractions instead of 12 + 4.
 #pragma once
 
 #include "common.cuh"
@@ -153,6 +160,51 @@ __device__ __forceinline__ void product_last(const float2* __restrict__ X, float
             const int yb = (a0 + u) * CHI + ig * 4;
             st2(Y + swz<SW>(yb), acc[u][0], acc[u][1]);
             st2(Y + swz<SW>(yb + 2), acc[u][2], acc[u][3]);
+        }
+    }
+}
+
+// X <- X x_0 M in place (bond 0 of a [NS][CHI]^D buffer): every thread owns at most one
+// 4x4 tile, accumulates it from X, and writes it back only after the barrier that follows
+// the last read of X by any thread.
+template <int D, int CHI, int THREADS, int SW, int NS>
+__device__ __forceinline__ void product_first_inplace(float2* X, const float2* __restrict__ Mt) {
+    constexpr int NIG = CHI / 4;
+    constexpr int B = cpow(CHI, D - 1);
+    constexpr int NBG = B / 4;
+    constexpr int TILES = NS * NIG * NBG;
+    static_assert(TILES <= THREADS, "in-place bond-0 product needs one tile per thread");
+    const int t = threadIdx.x;
+    const int bg = t % NBG, ig = (t / NBG) % NIG, a = t / (NBG * NIG);
+    float2 acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+    if (t < TILES) {
+        const int xb = a * CHI * B + bg * 4;
+        const float2* mp = Mt + ig * 4;
+#pragma unroll 4
+        for (int j = 0; j < CHI; ++j) {
+            float2 x[4], m[4];
+            const int e = xb + j * B;
+            ld2(X + swz<SW>(e), x[0], x[1]);
+            ld2(X + swz<SW>(e + 2), x[2], x[3]);
+            ld2(mp + j * CHI, m[0], m[1]);
+            ld2(mp + j * CHI + 2, m[2], m[3]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = c_fma(m[u], x[v], acc[u][v]);
+        }
+    }
+    __syncthreads();
+    if (t < TILES) {
+        const int yb = (a * CHI + ig * 4) * B + bg * 4;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            st2(X + swz<SW>(yb + u * B), acc[u][0], acc[u][1]);
+            st2(X + swz<SW>(yb + u * B + 2), acc[u][2], acc[u][3]);
         }
     }
 }
