@@ -9,7 +9,7 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 3
+ABI_VERSION = 4
 BQA_C64 = 0
 BQA_C128 = 1
 
@@ -47,6 +47,8 @@ SIGNATURES = {
     "bqa_bp_finalize": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_double, c_double,
                                   c_int32, c_void_p]),
     "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),
+    "bqa_ext_msgs_split": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32,
+                                     c_void_p, c_double, c_void_p, c_void_p]),
     "bqa_env_factor": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
     "bqa_bond_canon": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,

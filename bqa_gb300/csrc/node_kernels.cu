@@ -425,6 +425,40 @@ static int try_half(const NodeArgs<float>& a, int count, cudaStream_t st, int* r
     return 0;
 }
 
+// Extended messages from the open-bond blocks (the EXT epilogue of write_outputs as a pass of
+// its own): block (r, c) of the 2chi x 2chi message of slot e is
+// conj(a_r) a_c (P_0 + (-1)^(r+c) P_1) / ((|a_0|^2 + |a_1|^2) tr), a_0, a_1 the half-ZZ
+// coefficients of J[e % (E/2)] * ztime (src/bqa/state.py:127-139, backends.py:519-526).
+// One warp per slot; every lane forms the trace in the same order as write_outputs, so from
+// the same blocks the output equals the one-pass kernel's bit for bit.
+template <typename R>
+__global__ void __launch_bounds__(256) ext_combine_kernel(const typename Cx<R>::T* __restrict__ pm, int E, int chi,
+                                                          const double* __restrict__ edge_j, double ztime,
+                                                          typename Cx<R>::T* __restrict__ ext) {
+    using C = typename Cx<R>::T;
+    const int lane = threadIdx.x & 31;
+    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (slot >= E) return;
+    const int n2 = chi * chi, n = 2 * chi;
+    const C* p0 = pm + (size_t)slot * 2 * n2;
+    const C* p1 = p0 + n2;
+    C tr = c_zero<C>();
+    for (int q = 0; q < chi; ++q) tr = c_add(tr, c_add(p0[q * chi + q], p1[q * chi + q]));
+    const HalfZZ<R> h = half_zz<R>(edge_j[slot % (E / 2)] * ztime);
+    const R scale = c_abs2(h.a0) + c_abs2(h.a1);
+    const C trx = c_scale(tr, scale);
+    C* og = ext + (size_t)slot * n * n;
+    for (int o = lane; o < n * n; o += 32) {
+        const int row = o / n, col = o - row * n;
+        const int e = row >= chi, f = col >= chi;
+        const int ia = row - e * chi, ib = col - f * chi;
+        const C a0 = p0[ia * chi + ib], a1 = p1[ia * chi + ib];
+        const C pe = ((e + f) & 1) ? c_sub(a0, a1) : c_add(a0, a1);
+        const C coef = c_mul(c_conj(e ? h.a1 : h.a0), f ? h.a1 : h.a0);
+        og[o] = c_div(c_mul(coef, pe), trx);
+    }
+}
+
 // BP messages from the open-bond blocks: msg[e] = (P_0 + P_1)/tr, with the convergence maxima
 // max|new-old|^2 and max|new+old|^2 folded per block into dist_parts.  One warp per slot.
 template <typename R>
@@ -720,6 +754,42 @@ int32_t bqa_ext_msgs(const bqa_class* classes, int32_t n_classes, int32_t chi, i
     if (!msgs || !ext_out) return set_error(BQA_ERR_ARG, "bqa_ext_msgs: null buffer");
     return run_classes_dt(dtype, MODE_EXT, classes, n_classes, chi, msgs, nullptr, ext_out, nullptr, nullptr, ztime,
                           as_stream(stream));
+}
+
+int32_t bqa_ext_msgs_split(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, const void* msgs,
+                           void* pm, int32_t edges, const double* edge_j, double ztime, void* ext_out, void* stream) {
+    if (!classes || n_classes < 0 || chi < 1 || !msgs || !pm || !edge_j || !ext_out || edges < 2 || edges % 2)
+        return set_error(BQA_ERR_ARG, "bqa_ext_msgs_split: bad argument");
+    if (dtype != BQA_C64 && dtype != BQA_C128) return set_error(BQA_ERR_ARG, "bqa_ext_msgs_split: unknown dtype %d", dtype);
+    cudaStream_t st = as_stream(stream);
+    for (int c = 0; c < n_classes; ++c) {
+        const bqa_class& k = classes[c];
+        if (k.count <= 0 || k.degree == 0) continue;
+        int rc = BQA_OK;
+        if (dtype == BQA_C64 && g_use_tiled) {
+            NodeArgs<float> a;
+            a.tensors = static_cast<const float2*>(k.tensor);
+            a.in_pos = k.in_pos; a.out_pos = k.out_pos; a.node_ids = k.node_ids; a.edge_ampl = k.edge_ampl;
+            a.d = k.degree; a.chi = chi;
+            a.msgs_a = static_cast<const float2*>(msgs); a.msgs_b = nullptr;
+            a.out = static_cast<float2*>(pm); a.loop_state = nullptr; a.dist_parts = nullptr; a.ztime = 0.0;
+            if (try_half(a, k.count, st, &rc)) {
+                if (rc) return rc;
+                continue;
+            }
+        }
+        bqa_class one = k;
+        rc = run_classes_dt(dtype, MODE_PSPLIT, &one, 1, chi, msgs, nullptr, pm, nullptr, nullptr, 0.0, st);
+        if (rc) return rc;
+    }
+    const int blocks = (int)(((int64_t)edges * 32 + 255) / 256);
+    if (dtype == BQA_C64)
+        ext_combine_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float2*>(pm), edges, chi, edge_j, ztime,
+                                                           static_cast<float2*>(ext_out));
+    else
+        ext_combine_kernel<double><<<blocks, 256, 0, st>>>(static_cast<const double2*>(pm), edges, chi, edge_j, ztime,
+                                                            static_cast<double2*>(ext_out));
+    return check_launch("ext_combine");
 }
 
 int32_t bqa_psplit(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, const void* msgs, void* pm,

@@ -132,6 +132,7 @@ class Annealer:
         self.lmbds = torch.empty(self.half * nmax, dtype=real, device=dev)
         # max over edges of each lambda column, as the real's bit pattern
         self.colmax = torch.zeros(nmax, dtype=torch.int32 if self.precision == "single" else torch.int64, device=dev)
+        self.edge_j = torch.as_tensor(np.asarray(ctx.edge_ampl, dtype=np.float64), device=dev)
         self.dist_parts = torch.zeros(2, dtype=torch.int64, device=dev)
         self.loop_state = torch.zeros(8, dtype=torch.int32, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -278,8 +279,14 @@ class Annealer:
         eps = float(ctx.pinv_eps)
         cls = self._class_array()
         dt = self.dtype
-        self._launch("ext_msgs", 0.0, 0.0, lib.call, "bqa_ext_msgs", cls, len(self.classes), chi, dt,
-                     _ptr(self._msgs_cur()), _ptr(self.ext), float(ztime), st)
+        if self.split_sweeps:
+            # half-node kernels write P_0, P_1 into lu (free until the environment factors)
+            self._launch("ext_msgs", 0.0, 0.0, lib.call, "bqa_ext_msgs_split", cls, len(self.classes), chi, dt,
+                         _ptr(self._msgs_cur()), _ptr(self.lu), self.E, _ptr(self.edge_j), float(ztime),
+                         _ptr(self.ext), st)
+        else:
+            self._launch("ext_msgs", 0.0, 0.0, lib.call, "bqa_ext_msgs", cls, len(self.classes), chi, dt,
+                         _ptr(self._msgs_cur()), _ptr(self.ext), float(ztime), st)
         self._launch("env_factor", 0.0, 0.0, lib.call, "bqa_env_factor", _ptr(self.ext), self.E, n, dt, eps,
                      _ptr(self.lu), _ptr(self.ul), _ptr(self.status), st)
         self.colmax.zero_()

@@ -126,6 +126,16 @@ int32_t bqa_ext_msgs(const bqa_class* classes, int32_t n_classes, int32_t chi, i
                      void* ext_out, double ztime, void* stream);
 
 /*
+ * bqa_ext_msgs in two stages, the way bqa_bp_sweep_split runs a sweep: the half-node kernels
+ * write P_0 and P_1 of every open bond to pm ([edges][2][chi][chi] scratch), then one pass per
+ * slot forms the extended message from them with the coupling edge_j[slot % (edges/2)]
+ * (edge_j: device double [edges/2], the J of each undirected edge).  Same output as
+ * bqa_ext_msgs.
+ */
+int32_t bqa_ext_msgs_split(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, const void* msgs,
+                           void* pm, int32_t edges, const double* edge_j, double ztime, void* ext_out, void* stream);
+
+/*
  * Environment factors of every (extended) message m = U S Vh, singular values <= eps
  * dropped (src/bqa/backends.py:483-490,709-727): lu = sqrt(S) Vh and ul = U pinv(sqrt(S)),
  * both [count][n][n], n <= 32.  One-sided Jacobi SVD per matrix in the dtype's precision;

@@ -114,6 +114,25 @@ def test_ext_msgs_match_oracle(name, chi):
 
 
 @pytest.mark.parametrize("name,chi", CASES)
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_ext_msgs_split_matches_oracle_and_one_pass(name, chi, precision):
+    """Two-stage extended messages (half-node blocks + per-slot combine) against the oracle
+    and against the one-pass kernel (same epilogue arithmetic; the blocks' K-split can
+    differ between the half-node and whole-node launch shapes, so agreement is to rounding)."""
+    octx, st, job = random_state(name, chi, seed=1, precision=precision)
+    ztime = 0.37
+    want = orc.get_extended_msgs(octx, ztime, st)
+    job.lib.call("bqa_ext_msgs_split", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.lu), job.E, _ptr(job.edge_j), ztime, _ptr(job.ext), job.stream)
+    got = job.ext[: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, want) < (RTOL if precision == "single" else 1e-12)
+    job.lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.ul), ztime, job.stream)
+    one = job.ul[: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, one) < (2e-6 if precision == "single" else 1e-14)
+
+
+@pytest.mark.parametrize("name,chi", CASES)
 def test_canonicalisers_match_oracle(name, chi):
     octx, st, job = random_state(name, chi, seed=2)
     ext = orc.get_extended_msgs(octx, 0.21, st).astype(np.complex64).astype(np.complex128)
