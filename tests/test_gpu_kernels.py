@@ -119,6 +119,8 @@ def test_ext_msgs_split_matches_oracle_and_one_pass(name, chi, precision):
     """Two-stage extended messages (half-node blocks + per-slot combine) against the oracle
     and against the one-pass kernel (same epilogue arithmetic; the blocks' K-split can
     differ between the half-node and whole-node launch shapes, so agreement is to rounding)."""
+    if precision == "double" and chi > 5:
+        pytest.skip("complex128 node kernels hold a smaller bond dim (6 at degree 4)")
     octx, st, job = random_state(name, chi, seed=1, precision=precision)
     ztime = 0.37
     want = orc.get_extended_msgs(octx, ztime, st)
