@@ -16,6 +16,9 @@
 #include "common.cuh"
 #include "internal.h"
 #include "tiled_node.cuh"
+#include "tiled_d3c16.cuh"
+
+#include <type_traits>
 
 namespace bqa {
 
@@ -26,6 +29,12 @@ enum NodeMode { MODE_BP = 0, MODE_EXT = 1, MODE_PSPLIT = 2, MODE_DENS = 3 };
 // takes the generic kernel, which tests use to cross-check the two).
 static const bool g_use_tiled = [] {
     const char* v = getenv("BQA_GB300_TILED");
+    return !(v && v[0] == '0');
+}();
+// Likewise BQA_GB300_SPECIALIZED=0 keeps the (3, 16) half-node kernel on the generic address
+// arithmetic (the two give bit-identical results).
+static const bool g_use_specialized = [] {
+    const char* v = getenv("BQA_GB300_SPECIALIZED");
     return !(v && v[0] == '0');
 }();
 
@@ -338,10 +347,13 @@ static int try_tiled(const NodeArgs<float>& a, int count, cudaStream_t st, int* 
 // Half-node register-tiled kernel: CTA (node, s) computes P_s of every bond of the node and
 // writes it to pm[slot][s] (the layout of the PSPLIT mode); bp_combine_kernel turns
 // P_0 + P_1 into messages.  Same contraction schedules as tiled_node_kernel.
-template <int D, int CHI>
+// SPEC: the (3, 16) shape with the address arithmetic of tiled_d3c16.cuh (same operations).
+template <int D, int CHI, bool SPEC>
 __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_kernel(NodeArgs<float> a) {
     using S = tiled::HalfShape<D, CHI>;
     static_assert(CHI % 4 == 0 && D >= 2 && D <= 4, "half kernel shapes");
+    static_assert(!SPEC || (D == 3 && CHI == 16 && S::THREADS == tiled::d3c16::TH && S::KS == 16),
+                  "specialised half kernel is built for degree 3, bond dim 16");
     static_assert(S::CLOSE_TILES <= S::THREADS, "close tiles exceed the block");
     constexpr int PS = S::PER_S, N2 = S::N2, TH = S::THREADS, SW = S::SW;
     extern __shared__ double4 smem_raw[];
@@ -358,8 +370,12 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
     const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
     {
         const float4* tg = reinterpret_cast<const float4*>(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS);
-        for (int i = threadIdx.x; i < PS / 2; i += TH)
-            *reinterpret_cast<float4*>(sT + tiled::swz<SW>(2 * i)) = tg[i];
+        if constexpr (SPEC) {
+            tiled::d3c16::load_half(sT, tg);
+        } else {
+            for (int i = threadIdx.x; i < PS / 2; i += TH)
+                *reinterpret_cast<float4*>(sT + tiled::swz<SW>(2 * i)) = tg[i];
+        }
     }
 #pragma unroll
     for (int k = 0; k < D; ++k) {
@@ -382,7 +398,27 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         for (int i = threadIdx.x; i < N2 / 2; i += TH) og[i] = sp[i];
         __syncthreads();
     };
-    if (D == 2) {
+    if constexpr (SPEC) {
+        namespace q = tiled::d3c16;
+        auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
+            constexpr int IDX = decltype(idx_tag)::value;
+            q::close<IDX>(X, R, sP);
+            __syncthreads();
+            float4* og = reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + IDX] * 2 + s) * N2);
+            const float4* sp = reinterpret_cast<const float4*>(sP);
+            for (int i = threadIdx.x; i < N2 / 2; i += TH) og[i] = sp[i];
+            __syncthreads();
+        };
+        q::prod1(sT, sA, sMt + N2);
+        __syncthreads();
+        q::prod2(sT, sB, sMt + 2 * N2);
+        __syncthreads();
+        emit_s(std::integral_constant<int, 0>{}, sA, sB);
+        q::prod0_inplace(sT, sMt);
+        __syncthreads();
+        emit_s(std::integral_constant<int, 2>{}, sT, sA);
+        emit_s(std::integral_constant<int, 1>{}, sT, sB);
+    } else if (D == 2) {
         prod(sT, sA, 1); emit(0, sT, sA);
         prod(sT, sA, 0); emit(1, sT, sA);
     } else if (D == 3) {
@@ -403,14 +439,22 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
     }
 }
 
-template <int D, int CHI>
-static int launch_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+template <int D, int CHI, bool SPEC>
+static int launch_half_k(const NodeArgs<float>& args, int count, cudaStream_t st) {
     using S = tiled::HalfShape<D, CHI>;
     const size_t smem = (size_t)S::SMEM_ELEMS * sizeof(float2);
-    int rc = ensure_smem((const void*)tiled_half_kernel<D, CHI>, smem, "tiled half kernel");
+    int rc = ensure_smem((const void*)tiled_half_kernel<D, CHI, SPEC>, smem, "tiled half kernel");
     if (rc) return rc;
-    tiled_half_kernel<D, CHI><<<2 * count, S::THREADS, smem, st>>>(args);
+    tiled_half_kernel<D, CHI, SPEC><<<2 * count, S::THREADS, smem, st>>>(args);
     return check_launch("tiled half kernel");
+}
+
+template <int D, int CHI>
+static int launch_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    if constexpr (D == 3 && CHI == 16) {
+        if (g_use_specialized) return launch_half_k<D, CHI, true>(args, count, st);
+    }
+    return launch_half_k<D, CHI, false>(args, count, st);
 }
 
 // 1 if a half-node kernel covers (degree, chi) and was launched

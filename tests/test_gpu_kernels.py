@@ -264,3 +264,36 @@ def test_zero_padded_bond_storage_is_exact(name, chi, maxd):
     assert np.abs(runs[0][1] - runs[1][1]).max() < 1e-5
     assert np.abs(runs[0][2] - runs[1][2]).max() < 1e-5
     assert np.abs(runs[0][3] - runs[1][3]).max() < 1e-5
+
+
+_SWEEP_SCRIPT = """
+import sys, numpy as np
+from tests.test_gpu_kernels import random_state
+from bqa_gb300.engine import _ptr
+octx, st, job = random_state("rr3_n16_chi4", 16, seed=11)
+job.lib.call("bqa_bp_sweep_split", job._class_array(), len(job.classes), 16, job.dtype, _ptr(job.msgs[0]),
+             _ptr(job.msgs[1]), _ptr(job.lu), job.E, _ptr(job.dist_parts), None, job.stream)
+msgs = job.msgs[1][: job.E * 256].cpu().numpy()
+job.lib.call("bqa_ext_msgs_split", job._class_array(), len(job.classes), 16, job.dtype, _ptr(job.msgs[0]),
+             _ptr(job.lu), job.E, _ptr(job.edge_j), 0.37, _ptr(job.ext), job.stream)
+ext = job.ext[: job.E * 1024].cpu().numpy()
+np.savez(sys.argv[1], msgs=msgs, ext=ext)
+"""
+
+
+def test_specialised_half_kernel_bit_identical_to_generic(tmp_path):
+    """The (3, 16) half-node kernel with closed-form addresses gives the generic kernel's bits."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    out = {}
+    for flag in ("1", "0"):
+        env = dict(os.environ, BQA_GB300_SPECIALIZED=flag, PYTHONPATH=str(root))
+        f = tmp_path / f"spec{flag}.npz"
+        subprocess.run([sys.executable, "-c", _SWEEP_SCRIPT, str(f)], cwd=root, env=env, check=True, timeout=600)
+        out[flag] = np.load(f)
+    assert np.array_equal(out["1"]["msgs"], out["0"]["msgs"])
+    assert np.array_equal(out["1"]["ext"], out["0"]["ext"])
+    assert np.abs(out["1"]["msgs"]).max() > 0
