@@ -272,9 +272,10 @@ __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kern
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
+        // transpose on the way in; consecutive threads write consecutive shared addresses
         for (int o = threadIdx.x; o < N2; o += TH) {
-            const int i = o / CHI, j = o - i * CHI;
-            sMt[k * N2 + j * CHI + i] = mg[o];
+            const int j = o / CHI, i = o - j * CHI;
+            sMt[k * N2 + o] = mg[i * CHI + j];
         }
     }
     __syncthreads();
@@ -380,9 +381,10 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
+        // transpose on the way in; consecutive threads write consecutive shared addresses
         for (int o = threadIdx.x; o < N2; o += TH) {
-            const int i = o / CHI, j = o - i * CHI;
-            sMt[k * N2 + j * CHI + i] = mg[o];
+            const int j = o / CHI, i = o - j * CHI;
+            sMt[k * N2 + o] = mg[i * CHI + j];
         }
     }
     __syncthreads();

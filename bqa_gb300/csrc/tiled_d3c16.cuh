@@ -142,26 +142,6 @@ __device__ __forceinline__ void prod0_inplace(float2* X, const float2* __restric
     }
 }
 
-// Sum the 16 K-slices of a tile (adjacent lanes) and write it to P[16][16]
-__device__ __forceinline__ void close_finish(float2 (&acc)[4][4], int ks, int ag, int bg, float2* __restrict__ P) {
-#pragma unroll
-    for (int off = 8; off > 0; off >>= 1) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                acc[u][v].x += __shfl_xor_sync(BQA_FULL_MASK, acc[u][v].x, off);
-                acc[u][v].y += __shfl_xor_sync(BQA_FULL_MASK, acc[u][v].y, off);
-            }
-    }
-    if (ks == 0) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) P[(ag * 4 + u) * 16 + bg * 4 + v] = acc[u][v];
-    }
-}
-
 // P[a][b] = sum conj(X[..]) R[..] over every index but bond IDX; thread = (tile (ag, bg), K-slice ks)
 template <int IDX>
 __device__ __forceinline__ void close(const float2* __restrict__ X, const float2* __restrict__ R,
@@ -241,7 +221,7 @@ __device__ __forceinline__ void close(const float2* __restrict__ X, const float2
                 for (int v = 0; v < 4; ++v) acc[u][v] = c_fma_conj(tv[u], rv[v], acc[u][v]);
         }
     }
-    close_finish(acc, ks, ag, bg, P);
+    reduce_tile<16, 16>(acc, ks, true, P, ag, bg);
 }
 
 }  // namespace d3c16

@@ -10,7 +10,7 @@
 //   closing contraction for bond idx:
 //       P_s[a][b] = sum_{x,y} conj(X[s][x][a][y]) R[s][x][b][y]   (X = T or a product of T)
 //       a thread owns a 4x4 tile of (a, b) for one K-slice; the KS slices of a tile sit in
-//       adjacent lanes and are summed with xor-shuffles.
+//       adjacent lanes and are summed by recursive halving (reduce_tile).
 //
 // Tensor buffers in shared memory are XOR-swizzled in 16-byte chunks: element e lives at
 // e ^ (((e >> 4) & SW) << 1), SW = 7 for CHI = 16 and 3 for CHI = 8.  A 16-element row is
@@ -221,6 +221,42 @@ __device__ __forceinline__ void product(const float2* X, float2* Y, const float2
 
 // P[s][a][b] = sum_{x<Ax, y<B} conj(T[s][x][a][y]) R[s][x][b][y]; per s the operands are
 // [Ax][CHI][B] with Ax * CHI * B = PER_S.  Result written to P[NS][CHI][CHI].
+// Sum a 4x4 complex tile over its KS K-slices (KS adjacent lanes, a power of two <= 32) by
+// recursive halving: in the round with lane bit b every lane keeps one half of its values
+// and adds the partner's copy of that half, so after log2(KS) rounds lane ks holds the
+// 32/KS floats e = ks * (32/KS) + i of the tile (float e = component e & 1 of element e >> 1,
+// element q = 4u + v), each summed over all slices.  The lane writes them to P (row stride
+// CHI) if the tile is active.  32/KS * (2 - 2/KS) shuffles instead of 32 log2(KS).
+template <int KS, int CHI>
+__device__ __forceinline__ void reduce_tile(float2 (&acc)[4][4], int ks, bool active, float2* __restrict__ P,
+                                            int ag, int bg) {
+    float w[32];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        w[2 * q] = acc[q >> 2][q & 3].x;
+        w[2 * q + 1] = acc[q >> 2][q & 3].y;
+    }
+#pragma unroll
+    for (int b = KS / 2, n = 32; b > 0; b >>= 1, n >>= 1) {
+        const bool up = (ks & b) != 0;
+#pragma unroll
+        for (int i = 0; i < n / 2; ++i) {
+            const float send = up ? w[i] : w[n / 2 + i];
+            const float keep = up ? w[n / 2 + i] : w[i];
+            w[i] = keep + __shfl_xor_sync(BQA_FULL_MASK, send, b);
+        }
+    }
+    if (active) {
+        constexpr int NF = 32 / KS;
+        float* pf = reinterpret_cast<float*>(P);
+#pragma unroll
+        for (int i = 0; i < NF; ++i) {
+            const int e = ks * NF + i, q = e >> 1;
+            pf[2 * ((ag * 4 + (q >> 2)) * CHI + bg * 4 + (q & 3)) + (e & 1)] = w[i];
+        }
+    }
+}
+
 template <int CHI, int THREADS, int KS, int PER_S, int SW, int NS = 2>
 __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const float2* __restrict__ Rt,
                                             float2* __restrict__ P, int Ax, int B) {
@@ -276,23 +312,7 @@ __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const 
         }
     }
     // sum the KS slices (adjacent lanes)
-#pragma unroll
-    for (int off = KS / 2; off > 0; off >>= 1) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                acc[u][v].x += __shfl_xor_sync(BQA_FULL_MASK, acc[u][v].x, off);
-                acc[u][v].y += __shfl_xor_sync(BQA_FULL_MASK, acc[u][v].y, off);
-            }
-    }
-    if (active && ks == 0) {
-        float2* pp = P + (size_t)s * CHI * CHI;
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) pp[(ag * 4 + u) * CHI + bg * 4 + v] = acc[u][v];
-    }
+    reduce_tile<KS, CHI>(acc, ks, active, P + (size_t)s * CHI * CHI, ag, bg);
 }
 
 }  // namespace tiled
