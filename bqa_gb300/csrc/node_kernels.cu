@@ -31,9 +31,8 @@ static const bool g_use_tiled = [] {
     const char* v = getenv("BQA_GB300_TILED");
     return !(v && v[0] == '0');
 }();
-// Likewise BQA_GB300_SPECIALIZED=0 keeps the (3, 16) half-node kernel on the generic form (the
-// two agree to complex64 rounding; the specialised one sums real and imaginary parts of each
-// complex product in separate packed accumulators).
+// Likewise BQA_GB300_SPECIALIZED=0 keeps the (3, 16) half-node kernel on the generic address
+// arithmetic (the two give bit-identical results).
 static const bool g_use_specialized = [] {
     const char* v = getenv("BQA_GB300_SPECIALIZED");
     return !(v && v[0] == '0');
@@ -349,10 +348,9 @@ static int try_tiled(const NodeArgs<float>& a, int count, cudaStream_t st, int* 
 // Half-node register-tiled kernel: CTA (node, s) computes P_s of every bond of the node and
 // writes it to pm[slot][s] (the layout of the PSPLIT mode); bp_combine_kernel turns
 // P_0 + P_1 into messages.  Same contraction schedules as tiled_node_kernel.
-// SPEC: the (3, 16) shape with the closed-form addresses and packed FMAs of tiled_d3c16.cuh
-// (<= 128 registers, so two 110 KB CTAs share an SM).
+// SPEC: the (3, 16) shape with the address arithmetic of tiled_d3c16.cuh (same operations).
 template <int D, int CHI, bool SPEC>
-__global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS, SPEC ? 2 : 1) tiled_half_kernel(NodeArgs<float> a) {
+__global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_kernel(NodeArgs<float> a) {
     using S = tiled::HalfShape<D, CHI>;
     static_assert(CHI % 4 == 0 && D >= 2 && D <= 4, "half kernel shapes");
     static_assert(!SPEC || (D == 3 && CHI == 16 && S::THREADS == tiled::d3c16::TH && S::KS == 16),
@@ -364,8 +362,7 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS, SPEC ? 2 : 
     float2* sA = sT + PS;
     float2* sB = sA + PS;
     float2* sMt = sB + PS;
-    // the specialised kernel keeps the messages expanded (twice the space) before P
-    float2* sP = sMt + (SPEC ? 2 : 1) * D * N2;
+    float2* sP = sMt + D * N2;
     const float2* msgs_in = a.msgs_a;
     if (a.loop_state != nullptr) {
         if (a.loop_state[0]) return;
@@ -384,14 +381,10 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS, SPEC ? 2 : 
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
-        if constexpr (SPEC) {
-            tiled::d3c16::load_msg_expanded(reinterpret_cast<float4*>(sMt) + k * N2, mg);
-        } else {
-            // transpose on the way in; consecutive threads write consecutive shared addresses
-            for (int o = threadIdx.x; o < N2; o += TH) {
-                const int j = o / CHI, i = o - j * CHI;
-                sMt[k * N2 + o] = mg[i * CHI + j];
-            }
+        // transpose on the way in; consecutive threads write consecutive shared addresses
+        for (int o = threadIdx.x; o < N2; o += TH) {
+            const int j = o / CHI, i = o - j * CHI;
+            sMt[k * N2 + o] = mg[i * CHI + j];
         }
     }
     __syncthreads();
@@ -409,7 +402,6 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS, SPEC ? 2 : 
     };
     if constexpr (SPEC) {
         namespace q = tiled::d3c16;
-        const float4* sMe = reinterpret_cast<const float4*>(sMt);
         auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
             constexpr int IDX = decltype(idx_tag)::value;
             q::close<IDX>(X, R, sP);
@@ -419,12 +411,12 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS, SPEC ? 2 : 
             for (int i = threadIdx.x; i < N2 / 2; i += TH) og[i] = sp[i];
             __syncthreads();
         };
-        q::prod1(sT, sA, sMe + N2);
+        q::prod1(sT, sA, sMt + N2);
         __syncthreads();
-        q::prod2(sT, sB, sMe + 2 * N2);
+        q::prod2(sT, sB, sMt + 2 * N2);
         __syncthreads();
         emit_s(std::integral_constant<int, 0>{}, sA, sB);
-        q::prod0_inplace(sT, sMe);
+        q::prod0_inplace(sT, sMt);
         __syncthreads();
         emit_s(std::integral_constant<int, 2>{}, sT, sA);
         emit_s(std::integral_constant<int, 1>{}, sT, sB);
@@ -452,7 +444,7 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS, SPEC ? 2 : 
 template <int D, int CHI, bool SPEC>
 static int launch_half_k(const NodeArgs<float>& args, int count, cudaStream_t st) {
     using S = tiled::HalfShape<D, CHI>;
-    const size_t smem = ((size_t)S::SMEM_ELEMS + (SPEC ? (size_t)D * S::N2 : 0)) * sizeof(float2);
+    const size_t smem = (size_t)S::SMEM_ELEMS * sizeof(float2);
     int rc = ensure_smem((const void*)tiled_half_kernel<D, CHI, SPEC>, smem, "tiled half kernel");
     if (rc) return rc;
     tiled_half_kernel<D, CHI, SPEC><<<2 * count, S::THREADS, smem, st>>>(args);

@@ -9,13 +9,6 @@
 // loop indices that are compile-time after unrolling, so the generic form's three integer
 // operations per load disappear; the arithmetic and its order are the generic functions'.
 // Each closed form was checked against the generic swizzle for every thread and index.
-//
-// The complex multiply-adds run as packed FP32 pairs (__ffma2_rn, two FMAs per instruction):
-// a tile keeps two float2 accumulators per element, acc1 += (a.x, a.x) * b and
-// acc2 += (a.y, a.y) * b, combined once at the end into a*b = (acc1.x - acc2.y,
-// acc1.y + acc2.x) (conj(a)*b = (acc1.x + acc2.y, acc1.y - acc2.x)).  The broadcast operand of
-// a product is the message, stored in shared memory pre-expanded as (m.x, m.x, m.y, m.y), so
-// one 128-bit load gives both pairs; this halves the FMA instructions of the GEMMs.
 #pragma once
 
 #include "tiled_node.cuh"
@@ -41,56 +34,29 @@ __device__ __forceinline__ void zero(float2 (&acc)[4][4]) {
         for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
 }
 
-// the message Mt[j][i] of one bond, expanded: Me[j * 16 + i] = (m.x, m.x, m.y, m.y)
-__device__ __forceinline__ void load_msg_expanded(float4* __restrict__ Me, const float2* __restrict__ mg) {
-    for (int o = threadIdx.x; o < 256; o += TH) {
-        const int j = o >> 4, i = o & 15;
-        const float2 m = mg[i * 16 + j];
-        Me[o] = make_float4(m.x, m.x, m.y, m.y);
-    }
-}
-
-// acc{1,2}[u][v] += (a_u.x, a_u.x) * b_v, (a_u.y, a_u.y) * b_v
-__device__ __forceinline__ void pmac(float2 (&acc1)[4][4], float2 (&acc2)[4][4], const float4 (&a)[4],
-                                     const float2 (&b)[4]) {
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const float2 ax = make_float2(a[u].x, a[u].y), ay = make_float2(a[u].z, a[u].w);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            acc1[u][v] = __ffma2_rn(ax, b[v], acc1[u][v]);
-            acc2[u][v] = __ffma2_rn(ay, b[v], acc2[u][v]);
-        }
-    }
-}
-
-__device__ __forceinline__ float2 combine(float2 a1, float2 a2) { return make_float2(a1.x - a2.y, a1.y + a2.x); }
-__device__ __forceinline__ float2 combine_conj(float2 a1, float2 a2) {
-    return make_float2(a1.x + a2.y, a1.y - a2.x);
-}
-
 // Y = X x_1 M (bond 1): thread = tile (a = x0, ig = 4 values of the new x1, bg = 4 values of x2)
 __device__ __forceinline__ void prod1(const float2* __restrict__ X, float2* __restrict__ Y,
-                                      const float4* __restrict__ Me) {
+                                      const float2* __restrict__ Mt) {
     const int t = threadIdx.x;
     const int bg = t & 3, ig = (t >> 2) & 3, a = t >> 4;
     const float2* P[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) P[m] = X + a * 256 + 4 * (bg ^ m);
-    const float4* mp = Me + ig * 4;
-    float2 acc1[4][4], acc2[4][4];
-    zero(acc1);
-    zero(acc2);
+    const float2* mp = Mt + ig * 4;
+    float2 acc[4][4];
+    zero(acc);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-        float2 x[4];
-        float4 m[4];
+        float2 x[4], m[4];
         const float2* pj = P[(j >> 1) & 3] + j * 16;
         ld2(pj + 2 * (j & 1), x[0], x[1]);
         ld2(pj + 2 * (1 ^ (j & 1)), x[2], x[3]);
+        ld2(mp + j * 16, m[0], m[1]);
+        ld2(mp + j * 16 + 2, m[2], m[3]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) m[u] = mp[j * 16 + u];
-        pmac(acc1, acc2, m, x);
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = c_fma(m[u], x[v], acc[u][v]);
     }
     float2* Q[2];
 #pragma unroll
@@ -98,41 +64,41 @@ __device__ __forceinline__ void prod1(const float2* __restrict__ X, float2* __re
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         float2* q = Q[u >> 1] + u * 16;
-        st2(q + 2 * (u & 1), combine(acc1[u][0], acc2[u][0]), combine(acc1[u][1], acc2[u][1]));
-        st2(q + 2 * (1 ^ (u & 1)), combine(acc1[u][2], acc2[u][2]), combine(acc1[u][3], acc2[u][3]));
+        st2(q + 2 * (u & 1), acc[u][0], acc[u][1]);
+        st2(q + 2 * (1 ^ (u & 1)), acc[u][2], acc[u][3]);
     }
 }
 
 // Y = X x_2 M (last bond): thread = tile (4 rows a0.., ig = 4 values of the new x2)
 __device__ __forceinline__ void prod2(const float2* __restrict__ X, float2* __restrict__ Y,
-                                      const float4* __restrict__ Me) {
+                                      const float2* __restrict__ Mt) {
     const int t = threadIdx.x;
     const int ig = t & 3, a0 = (t >> 2) * 4, p = (t >> 2) & 1;
     // rows a0..a0+3 have (row & 7) = 4p + u: the swizzle flips bit 3 of the column when p = 1
     const float2* R0 = X + a0 * 16 + 8 * p;
     const float2* R1 = X + a0 * 16 - 8 * p;
-    const float4* mp = Me + ig * 4;
-    // Y[a][i] = sum_j X[a][j] Mt[j][i]: the message (expanded) is the broadcast operand, so
-    // the accumulators are indexed [v = i][u = row]
-    float2 acc1[4][4], acc2[4][4];
-    zero(acc1);
-    zero(acc2);
+    const float2* mp = Mt + ig * 4;
+    float2 acc[4][4];
+    zero(acc);
 #pragma unroll
     for (int j = 0; j < 16; j += 2) {
-        float2 xa[4], xb[4];
-        float4 m0[4], m1[4];
+        float2 x[4][2], m0[4], m1[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int xo = j ^ (2 * u);
-            ld2(((xo & 8) ? R1 : R0) + u * 16 + xo, xa[u], xb[u]);
+            ld2(((xo & 8) ? R1 : R0) + u * 16 + xo, x[u][0], x[u][1]);
         }
+        ld2(mp + j * 16, m0[0], m0[1]);
+        ld2(mp + j * 16 + 2, m0[2], m0[3]);
+        ld2(mp + (j + 1) * 16, m1[0], m1[1]);
+        ld2(mp + (j + 1) * 16 + 2, m1[2], m1[3]);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            m0[v] = mp[j * 16 + v];
-            m1[v] = mp[(j + 1) * 16 + v];
-        }
-        pmac(acc1, acc2, m0, xa);
-        pmac(acc1, acc2, m1, xb);
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                acc[u][v] = c_fma(x[u][0], m0[v], acc[u][v]);
+                acc[u][v] = c_fma(x[u][1], m1[v], acc[u][v]);
+            }
     }
     float2* S[2];
 #pragma unroll
@@ -140,38 +106,39 @@ __device__ __forceinline__ void prod2(const float2* __restrict__ X, float2* __re
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         float2* q = S[u >> 1] + u * 16;
-        st2(q + 2 * (u & 1), combine(acc1[0][u], acc2[0][u]), combine(acc1[1][u], acc2[1][u]));
-        st2(q + 2 * (1 ^ (u & 1)), combine(acc1[2][u], acc2[2][u]), combine(acc1[3][u], acc2[3][u]));
+        st2(q + 2 * (u & 1), acc[u][0], acc[u][1]);
+        st2(q + 2 * (1 ^ (u & 1)), acc[u][2], acc[u][3]);
     }
 }
 
 // X <- X x_0 M in place (bond 0): thread = tile (ig = 4 values of the new x0, bg = 4 values of
 // (x1, x2)); all reads precede the barrier, all writes follow it
-__device__ __forceinline__ void prod0_inplace(float2* X, const float4* __restrict__ Me) {
+__device__ __forceinline__ void prod0_inplace(float2* X, const float2* __restrict__ Mt) {
     const int t = threadIdx.x;
     const int bg = t & 63, ig = t >> 6;
     const int c = ((bg >> 2) & 7) << 1;
     const int b0 = (bg >> 2) * 16 + ((4 * (bg & 3)) ^ c);
     const int b2 = (bg >> 2) * 16 + ((4 * (bg & 3) + 2) ^ c);
-    const float4* mp = Me + ig * 4;
-    float2 acc1[4][4], acc2[4][4];
-    zero(acc1);
-    zero(acc2);
+    const float2* mp = Mt + ig * 4;
+    float2 acc[4][4];
+    zero(acc);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-        float2 x[4];
-        float4 m[4];
+        float2 x[4], m[4];
         ld2(X + b0 + j * 256, x[0], x[1]);
         ld2(X + b2 + j * 256, x[2], x[3]);
+        ld2(mp + j * 16, m[0], m[1]);
+        ld2(mp + j * 16 + 2, m[2], m[3]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) m[u] = mp[j * 16 + u];
-        pmac(acc1, acc2, m, x);
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = c_fma(m[u], x[v], acc[u][v]);
     }
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        st2(X + (ig * 4 + u) * 256 + b0, combine(acc1[u][0], acc2[u][0]), combine(acc1[u][1], acc2[u][1]));
-        st2(X + (ig * 4 + u) * 256 + b2, combine(acc1[u][2], acc2[u][2]), combine(acc1[u][3], acc2[u][3]));
+        st2(X + (ig * 4 + u) * 256 + b0, acc[u][0], acc[u][1]);
+        st2(X + (ig * 4 + u) * 256 + b2, acc[u][2], acc[u][3]);
     }
 }
 
@@ -183,16 +150,8 @@ __device__ __forceinline__ void close(const float2* __restrict__ X, const float2
     const int ks = t & 15, tile = t >> 4;
     const int ag = tile >> 2, bg = tile & 3;
     const int b3 = ks >> 3;
-    // conj(t) r accumulated as acc1 += (t.x, t.x) r, acc2 += (t.y, t.y) r
-    float2 acc1[4][4], acc2[4][4];
-    zero(acc1);
-    zero(acc2);
-    auto cmac = [&](const float2 (&tv)[4], const float2 (&rv)[4]) {
-        float4 ta[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) ta[u] = make_float4(tv[u].x, tv[u].x, tv[u].y, tv[u].y);
-        pmac(acc1, acc2, ta, rv);
-    };
+    float2 acc[4][4];
+    zero(acc);
     if (IDX == 0) {
         // K = (x1, x2) in pairs: y = 2 (ks + 16 it); rows (4ag + u) * 16 + b3 + 2 it
         const int z = (ks & 7) ^ b3;
@@ -205,13 +164,18 @@ __device__ __forceinline__ void close(const float2* __restrict__ X, const float2
         }
 #pragma unroll
         for (int it = 0; it < 8; ++it) {
-            float2 t0[4], t1[4], r0[4], r1[4];
+            float2 tv[4][2], rv[4][2];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) ld2(TB[it & 3] + u * 256 + 32 * it, t0[u], t1[u]);
+            for (int u = 0; u < 4; ++u) ld2(TB[it & 3] + u * 256 + 32 * it, tv[u][0], tv[u][1]);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) ld2(RB[it & 3] + v * 256 + 32 * it, r0[v], r1[v]);
-            cmac(t0, r0);
-            cmac(t1, r1);
+            for (int v = 0; v < 4; ++v) ld2(RB[it & 3] + v * 256 + 32 * it, rv[v][0], rv[v][1]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    acc[u][v] = c_fma_conj(tv[u][0], rv[v][0], acc[u][v]);
+                    acc[u][v] = c_fma_conj(tv[u][1], rv[v][1], acc[u][v]);
+                }
         }
     } else if (IDX == 1) {
         // K = (x0, x2 pairs): x0 = b3 + 2 it, x2 = 2 (ks & 7); rows x0 * 16 + 4ag + u
@@ -224,13 +188,18 @@ __device__ __forceinline__ void close(const float2* __restrict__ X, const float2
         }
 #pragma unroll
         for (int it = 0; it < 8; ++it) {
-            float2 t0[4], t1[4], r0[4], r1[4];
+            float2 tv[4][2], rv[4][2];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) ld2(TB[u] + 512 * it, t0[u], t1[u]);
+            for (int u = 0; u < 4; ++u) ld2(TB[u] + 512 * it, tv[u][0], tv[u][1]);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) ld2(RB[v] + 512 * it, r0[v], r1[v]);
-            cmac(t0, r0);
-            cmac(t1, r1);
+            for (int v = 0; v < 4; ++v) ld2(RB[v] + 512 * it, rv[v][0], rv[v][1]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    acc[u][v] = c_fma_conj(tv[u][0], rv[v][0], acc[u][v]);
+                    acc[u][v] = c_fma_conj(tv[u][1], rv[v][1], acc[u][v]);
+                }
         }
     } else {
         // K = (x0, x1) rows x = ks + 16 it; the open index x2 = 4ag + u (4bg + v)
@@ -246,14 +215,12 @@ __device__ __forceinline__ void close(const float2* __restrict__ X, const float2
             ld2(T2 + 256 * it, tv[2], tv[3]);
             ld2(R0 + 256 * it, rv[0], rv[1]);
             ld2(R2 + 256 * it, rv[2], rv[3]);
-            cmac(tv, rv);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = c_fma_conj(tv[u], rv[v], acc[u][v]);
         }
     }
-    float2 acc[4][4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = combine_conj(acc1[u][v], acc2[u][v]);
     reduce_tile<16, 16>(acc, ks, true, P, ag, bg);
 }
 
