@@ -46,6 +46,27 @@ __device__ __forceinline__ C shfl_xor_c(C v, int r, int w) {
 // round reads and writes every V element of a rotated pair once.
 template <int W> struct VStride { static constexpr int VS = W + 2; static constexpr int BLOCK = W * VS; };
 
+constexpr int NP = 4;  // partial sums per reduction over a column
+
+template <int N, typename R>
+__device__ __forceinline__ R sum_parts(const R (&p)[N]) {
+    R s = p[0];
+#pragma unroll
+    for (int k = 1; k < N; ++k) s += p[k];
+    return s;
+}
+
+// |a|^2 of this lane's column, in NP interleaved partial sums
+template <int W, typename R>
+__device__ __forceinline__ R col_norm2(const typename Cx<R>::T (&a)[W]) {
+    R p[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) p[k] = R(0);
+#pragma unroll
+    for (int i = 0; i < W; ++i) p[i % NP] = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, p[i % NP]));
+    return sum_parts<NP>(p);
+}
+
 // One-sided Jacobi on the segment's columns.  a: this lane's column (registers); sV: the
 // segment's V block (shared), initialised to I here.  Returns whether it converged.
 template <int W, typename R>
@@ -59,9 +80,7 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
     const R tol = (R)W * jacobi_eps<R>();
     // |a_lane|^2, recomputed (same operation order) whenever the column changes; the pair's
     // norms come from their owners, so both lanes of a pair see the same alpha and beta
-    R nown = 0;
-#pragma unroll
-    for (int i = 0; i < W; ++i) nown = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, nown));
+    R nown = col_norm2<W, R>(a);
     R fro2 = nown;
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) fro2 += __shfl_xor_sync(BQA_FULL_MASK, fro2, o, W);
@@ -77,16 +96,21 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
             // lanes form bit-identically: Sx = sum Re(conj(own) partner) and the cross sums
             // S1 = sum own.x partner.y, S2 = sum own.y partner.x (they swap roles on the
             // other lane; fma(a, b, c) == fma(b, a, c)).
-            R sx = 0, s1 = 0, s2 = 0;
+            // NP independent partial sums per quantity (short dependency chains), combined in
+            // a fixed order, so both lanes still form identical bits
+            R sx[NP], s1[NP], s2[NP];
+#pragma unroll
+            for (int k = 0; k < NP; ++k) sx[k] = s1[k] = s2[k] = R(0);
 #pragma unroll
             for (int i = 0; i < W; ++i) {
                 const C o = shfl_xor_c(a[i], r, W);
-                sx = fma(a[i].x, o.x, fma(a[i].y, o.y, sx));
-                s1 = fma(a[i].x, o.y, s1);
-                s2 = fma(a[i].y, o.x, s2);
+                sx[i % NP] = fma(a[i].x, o.x, fma(a[i].y, o.y, sx[i % NP]));
+                s1[i % NP] = fma(a[i].x, o.y, s1[i % NP]);
+                s2[i % NP] = fma(a[i].y, o.x, s2[i % NP]);
             }
+            const R sxs = sum_parts<NP>(sx), s1s = sum_parts<NP>(s1), s2s = sum_parts<NP>(s2);
             const R alpha = low ? nown : npart, beta = low ? npart : nown;
-            const C g = c_make(sx, low ? s1 - s2 : s2 - s1);
+            const C g = c_make(sxs, low ? s1s - s2s : s2s - s1s);
             const R gabs = sqrt(c_abs2(g));
             const bool rot = alpha > R(0) && beta > R(0) && gabs > tol * sqrt(alpha) * sqrt(beta);
             if (__any_sync(BQA_FULL_MASK, rot)) {
@@ -105,14 +129,12 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                     rotated |= (alpha > col_floor && beta > col_floor);
                 }
                 const C wown = low ? wp : wq;
-                R n2 = 0;
 #pragma unroll
                 for (int i = 0; i < W; ++i) {
                     const C o = shfl_xor_c(a[i], r, W);
                     a[i] = c_fma(wown, o, c_scale(a[i], c));
-                    n2 = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, n2));
                 }
-                nown = n2;
+                nown = col_norm2<W, R>(a);
                 if (rot) {
                     C* vp = sV + (low ? lane : partner) * VS + (low ? 0 : H);
                     C* vq = sV + (low ? partner : lane) * VS + (low ? 0 : H);
