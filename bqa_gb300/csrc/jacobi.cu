@@ -136,26 +136,30 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                 }
                 nown = col_norm2<W, R>(a);
                 if (rot) {
-                    C* vp = sV + (low ? lane : partner) * VS + (low ? 0 : H);
-                    C* vq = sV + (low ? partner : lane) * VS + (low ? 0 : H);
+                    // own column first, partner's second: in each access the two lanes of a
+                    // pair touch different columns, so their half-column offsets (H rows =
+                    // 128 bytes in complex64) do not fall in the same bank group
+                    const C wpart = low ? wq : wp;
+                    C* vo = sV + lane * VS + (low ? 0 : H);
+                    C* vx = sV + partner * VS + (low ? 0 : H);
 #pragma unroll
                     for (int i = 0; i < H; i += 2) {
-                        C p0, p1, q0, q1;
+                        C o0, o1, x0, x1;
                         if (sizeof(R) == 4) {
-                            const float4 x = *reinterpret_cast<const float4*>(vp + i);
-                            const float4 y = *reinterpret_cast<const float4*>(vq + i);
-                            p0 = c_make((R)x.x, (R)x.y); p1 = c_make((R)x.z, (R)x.w);
-                            q0 = c_make((R)y.x, (R)y.y); q1 = c_make((R)y.z, (R)y.w);
+                            const float4 u = *reinterpret_cast<const float4*>(vo + i);
+                            const float4 v = *reinterpret_cast<const float4*>(vx + i);
+                            o0 = c_make((R)u.x, (R)u.y); o1 = c_make((R)u.z, (R)u.w);
+                            x0 = c_make((R)v.x, (R)v.y); x1 = c_make((R)v.z, (R)v.w);
                         } else {
-                            p0 = vp[i]; p1 = vp[i + 1]; q0 = vq[i]; q1 = vq[i + 1];
+                            o0 = vo[i]; o1 = vo[i + 1]; x0 = vx[i]; x1 = vx[i + 1];
                         }
-                        const C np0 = c_fma(wp, q0, c_scale(p0, c)), np1 = c_fma(wp, q1, c_scale(p1, c));
-                        const C nq0 = c_fma(wq, p0, c_scale(q0, c)), nq1 = c_fma(wq, p1, c_scale(q1, c));
+                        const C no0 = c_fma(wown, x0, c_scale(o0, c)), no1 = c_fma(wown, x1, c_scale(o1, c));
+                        const C nx0 = c_fma(wpart, o0, c_scale(x0, c)), nx1 = c_fma(wpart, o1, c_scale(x1, c));
                         if (sizeof(R) == 4) {
-                            *reinterpret_cast<float4*>(vp + i) = make_float4((float)np0.x, (float)np0.y, (float)np1.x, (float)np1.y);
-                            *reinterpret_cast<float4*>(vq + i) = make_float4((float)nq0.x, (float)nq0.y, (float)nq1.x, (float)nq1.y);
+                            *reinterpret_cast<float4*>(vo + i) = make_float4((float)no0.x, (float)no0.y, (float)no1.x, (float)no1.y);
+                            *reinterpret_cast<float4*>(vx + i) = make_float4((float)nx0.x, (float)nx0.y, (float)nx1.x, (float)nx1.y);
                         } else {
-                            vp[i] = np0; vp[i + 1] = np1; vq[i] = nq0; vq[i + 1] = nq1;
+                            vo[i] = no0; vo[i + 1] = no1; vx[i] = nx0; vx[i + 1] = nx1;
                         }
                     }
                 }
