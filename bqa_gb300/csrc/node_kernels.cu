@@ -241,7 +241,8 @@ __global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
 }
 
 
-// Register-tiled complex64 kernel for compile-time (D, CHI), BP and extended messages.
+// Register-tiled complex64 kernel for compile-time (D, CHI): BP messages, extended messages,
+// densities.
 template <int D, int CHI, int MODE>
 __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kernel(NodeArgs<float> a) {
     using S = tiled::Shape<D, CHI>;
@@ -292,7 +293,33 @@ __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kern
         write_outputs<MODE, float>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
         __syncthreads();
     };
-    if (D == 2) {
+    if constexpr (MODE == MODE_DENS) {
+        // rho[s][s'] = sum (T x_all M)[s, ..] conj(T[s', ..]) (backends.py:440-448): both
+        // buffers share one swizzle, so the sum runs over shared positions directly
+        const float2* cur = sT;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            float2* nxt = (k & 1) ? sB : sA;
+            prod(cur, nxt, k);
+            cur = nxt;
+        }
+        float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int p = threadIdx.x; p < PER_S; p += TH) {
+            const float2 x0 = cur[p], x1 = cur[PER_S + p];
+            const float2 t0 = sT[p], t1 = sT[PER_S + p];
+            const float2 r00 = c_fma_conj(t0, x0, c_zero<float2>()), r01 = c_fma_conj(t1, x0, c_zero<float2>());
+            const float2 r10 = c_fma_conj(t0, x1, c_zero<float2>()), r11 = c_fma_conj(t1, x1, c_zero<float2>());
+            v[0] += r00.x; v[1] += r00.y; v[2] += r01.x; v[3] += r01.y;
+            v[4] += r10.x; v[5] += r10.y; v[6] += r11.x; v[7] += r11.y;
+        }
+        block_sum<8>(v, sRed);
+        if (threadIdx.x < 4) {
+            const float2 tr = c_make(v[0] + v[6], v[1] + v[7]);
+            const float2 r = c_make(v[2 * threadIdx.x], v[2 * threadIdx.x + 1]);
+            a.out[(size_t)a.node_ids[node] * 4 + threadIdx.x] = c_div(r, tr);
+        }
+        return;
+    } else if (D == 2) {
         prod(sT, sA, 1); emit(0, sT, sA);
         prod(sT, sA, 0); emit(1, sT, sA);
     } else if (D == 3) {
@@ -551,7 +578,7 @@ __global__ void __launch_bounds__(256) bp_combine_kernel(const typename Cx<R>::T
 template <int MODE, typename R>
 static int launch_node_mode(const NodeArgs<R>& args, int count, cudaStream_t st) {
     const int chi = args.chi, d = args.d;
-    if constexpr (sizeof(R) == 4 && (MODE == MODE_BP || MODE == MODE_EXT)) {
+    if constexpr (sizeof(R) == 4 && (MODE == MODE_BP || MODE == MODE_EXT || MODE == MODE_DENS)) {
         if (g_use_tiled) {
             int rc = BQA_OK;
             if (try_tiled<MODE>(args, count, st, &rc)) return rc;
