@@ -251,6 +251,14 @@ int32_t bqa_layout_class(int32_t degree, int32_t count, const int32_t* deg, cons
                          const double* node_field, int32_t* node_ids, int32_t* position, int32_t* in_pos,
                          int32_t* out_pos, int32_t* lmbd_pos, double* edge_ampl, double* node_ampl, void* stream);
 
+/*
+ * FP32 FMA throughput probe (no reference counterpart; measurement only): `blocks` CTAs of 256
+ * threads each run 16 independent FMA chains for `iters` iterations, 2 * 16 * iters *
+ * blocks * 256 FLOP in all, and write one float per thread to out[blocks * 256].  Timed by
+ * the caller, it gives the FP32 CUDA-core peak the complex64 kernels are measured against.
+ */
+int32_t bqa_fp32_fma_probe(int32_t blocks, int32_t iters, float* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -297,3 +297,15 @@ def test_specialised_half_kernel_bit_identical_to_generic(tmp_path):
     assert np.array_equal(out["1"]["msgs"], out["0"]["msgs"])
     assert np.array_equal(out["1"]["ext"], out["0"]["ext"])
     assert np.abs(out["1"]["msgs"]).max() > 0
+
+
+def test_fp32_fma_probe_runs():
+    """The FP32 throughput probe launches, writes every output and gives a plausible rate."""
+    import bench
+    lib = _lib.load()
+    out = torch.full((152 * 256,), float("nan"), device="cuda")
+    lib.call("bqa_fp32_fma_probe", 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert torch.isfinite(out).all()
+    tf = bench.fp32_peak_tflops(lib, torch.device("cuda"))
+    assert 5.0 < tf < 500.0
