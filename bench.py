@@ -246,6 +246,10 @@ def run_gpu_arm(args) -> None:
         job.run_layer(*step_at(s + i))
     s += args.warmup
 
+    # the end-to-end pass below replays the timed steps from this state
+    snap = job.snapshot()
+    s_timed = s
+
     # timed region: K steps, device-timed with CUDA events on the launch stream
     job.enable_kernel_timing(True)
     job.stats.clear()
@@ -266,12 +270,15 @@ def run_gpu_arm(args) -> None:
     job.enable_kernel_timing(False)
     window = list(job.stats)
 
-    # end to end through the step API with host results: per step the instruction goes in by
-    # value, the new marginals of every qubit come back to host memory
+    # end to end through the step API with host results, over the same K steps from the same
+    # state: per step the instruction goes in by value, the new marginals of every qubit come
+    # back to host memory
+    job.restore(snap)
+    del snap
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for i in range(args.steps):
-        job.run_layer(*step_at(s + i))
+        job.run_layer(*step_at(s_timed + i))
         bloch = job.bloch_vectors()
     e2e_s = time.perf_counter() - t0
 
@@ -328,7 +335,8 @@ def run_gpu_arm(args) -> None:
                                    "probe": "bqa_fp32_fma_probe, 16 independent FMA chains per thread"}},
         "e2e": {"value": world * args.steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 16,
                 "d2h_bytes_per_step": int(n_el * 4 * 8 + 2 * args.chi * 4 + 64),
-                "what": "Annealer.run_layer + bloch_vectors per step (host scalars in, all marginals out)"},
+                "what": "Annealer.run_layer + bloch_vectors per step (host scalars in, all marginals out), "
+                        "the timed window's steps replayed from a snapshot of its starting state"},
         "gpu_launches": gpu_launches(job, kt, args.steps),
         "clocks": clocks.summary(),
         "prep": {"steps": prep_steps, "seconds": round(prep_s, 1)},

@@ -253,6 +253,27 @@ class Annealer:
             self.lam_stride = lam.shape[1]
             self.lmbds[: lam.size].copy_(torch.from_numpy(lam.reshape(-1)))
 
+    def snapshot(self) -> dict:
+        """Device-side copy of the evolving state (current tensors, messages, lambdas, bond
+        dims, host RNG); ``restore`` puts it back, so a run can resume from this point."""
+        n_t = {id(c): c.count * 2 * self.chis ** c.degree for c in self.classes}
+        return {
+            "tensors": [c.tensors[self.tcur][: n_t[id(c)]].clone() for c in self.classes],
+            "msgs": self._msgs_cur()[: self.E * self.chis * self.chis].clone(),
+            "lmbds": self.lmbds.clone(),
+            "dims": (self.chi, self.chis, self.lam_stride),
+            "rng": self.rng.bit_generator.state,
+        }
+
+    def restore(self, snap: dict) -> None:
+        self.chi, self.chis, self.lam_stride = snap["dims"]
+        self.tcur, self.mcur = 0, 0
+        for c, t in zip(self.classes, snap["tensors"]):
+            c.tensors[0][: t.numel()].copy_(t)
+        self.msgs[0][: snap["msgs"].numel()].copy_(snap["msgs"])
+        self.lmbds.copy_(snap["lmbds"])
+        self.rng.bit_generator.state = snap["rng"]
+
     def get_state(self) -> tuple[dict, np.ndarray, np.ndarray]:
         """Numpy copies of (tensors per degree, messages (E, chi, chi), lambdas (E/2, chi))."""
         chi, chis = self.chi, self.chis

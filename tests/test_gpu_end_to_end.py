@@ -131,3 +131,22 @@ def test_cli_streams_the_run_qa_result(tmp_path):
     assert [g[0] for g in got] == [w[0] for w in want]
     assert np.abs(np.array(got[0][1]) - np.array(want[0][1])).max() < 1e-12
     assert got[1][1] == want[1][1]
+
+
+def test_snapshot_restore_replays_identically():
+    """A run resumed from a snapshot repeats the same steps bit for bit."""
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
+    ctx = build_context(gc.config("rr3_n16_chi4"))
+    steps = [i for i in ctx.instructions if isinstance(i, dict)]
+    job = Annealer(ctx)
+    for ins in steps[:3]:
+        job.run_layer(ins["xtime"], ins["ztime"])
+    snap = job.snapshot()
+    for ins in steps[3:6]:
+        job.run_layer(ins["xtime"], ins["ztime"])
+    first = job.bloch_vectors()
+    job.restore(snap)
+    for ins in steps[3:6]:
+        job.run_layer(ins["xtime"], ins["ztime"])
+    assert np.array_equal(job.bloch_vectors(), first)
