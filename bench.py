@@ -561,6 +561,41 @@ def run_layout_mode(args) -> None:
                       "build_context_ms": ctx_ms}))
 
 
+def run_small_mode(args) -> None:
+    """The 1000-qubit chi-4 job (random 3-regular, J, h ~ N(0,1), T 10, 100 steps, bp_eps 1e-6,
+    <= 100 sweeps) through run_qa, wall-clock from config to result after one untimed run,
+    and the per-step time split (host overhead = wall minus device kernel time)."""
+    import torch
+    import bqa_gb300
+    from bqa_gb300 import instances
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
+    conf = instances.headline_cpu_job()
+    bqa_gb300.run_qa(dict(conf))
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        bqa_gb300.run_qa(dict(conf))
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    ctx = build_context(dict(conf))
+    job = Annealer(ctx)
+    job.enable_kernel_timing(True)
+    steps = [i for i in ctx.instructions if isinstance(i, dict)]
+    t0 = time.perf_counter()
+    for ins in steps:
+        job.run_layer(ins["xtime"], ins["ztime"])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    kt = job.kernel_times()
+    dev_ms = sum(k[1] for k in kt)
+    print(json.dumps({"mode": "small", "job": "random 3-regular n=1000, chi 4, 100 steps",
+                      "run_qa_s": float(np.median(ts)), "steps_per_s": len(steps) / float(np.median(ts)),
+                      "steps_wall_s": wall, "device_kernel_s": dev_ms / 1e3,
+                      "mean_sweeps": float(np.mean([w["sweeps"] for w in job.stats]))}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -570,7 +605,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout"])
+    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout", "small"])
     ap.add_argument("--jobs", type=int, default=32)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--precision", default="single", choices=["single", "double"])
@@ -587,6 +622,8 @@ def main() -> None:
         run_serve_mode(args)
     elif args.mode == "layout":
         run_layout_mode(args)
+    elif args.mode == "small":
+        run_small_mode(args)
     else:
         run_gpu_arm(args)
 
