@@ -9,7 +9,7 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 5
+ABI_VERSION = 6
 BQA_C64 = 0
 BQA_C128 = 1
 
@@ -32,6 +32,8 @@ class BqaClass(ctypes.Structure):
         ("node_ampl", c_void_p),
         ("tensor", c_void_p),
         ("tensor_out", c_void_p),
+        ("scratch", c_void_p),
+        ("scratch_elems", c_int64),
     ]
 
 
@@ -40,6 +42,7 @@ SIGNATURES = {
     "bqa_abi_version": (c_int32, []),
     "bqa_last_error": (ctypes.c_char_p, []),
     "bqa_max_bond_dim": (c_int32, [c_int32, c_int32]),
+    "bqa_node_scratch_elems": (c_int64, [c_int32, c_int32, c_int32]),
     "bqa_bp_sweep": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
                                c_void_p]),
     "bqa_bp_sweep_split": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,

@@ -17,6 +17,9 @@ int ensure_smem(const void* kernel, size_t bytes, const char* what);
 
 constexpr size_t kMaxSmem = 227 * 1024;
 
+// shared memory of the generic tensor update at bond dims <= chi, in bytes (update.cu)
+size_t apply_smem_bytes(int d, int chi, size_t elem_bytes);
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 }  // namespace bqa

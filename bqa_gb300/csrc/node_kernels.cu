@@ -18,6 +18,7 @@
 #include "tiled_node.cuh"
 #include "tiled_d3c16.cuh"
 
+#include <algorithm>
 #include <type_traits>
 
 namespace bqa {
@@ -240,6 +241,184 @@ __global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
     }
 }
 
+
+// ---- node tensors beyond shared memory --------------------------------------------------------
+//
+// The same contractions with the work tensor in a per-CTA slice of caller scratch (global
+// memory; L2 serves a slice while its CTA works on it); T is read in place from the class
+// buffer, messages, open-bond blocks and reduction partials stay in shared memory.  Each CTA
+// walks nodes blockIdx.x, blockIdx.x + gridDim.x, ...  For outgoing bond idx the work tensor
+// is T with every other message applied, the products running in place: a thread reads its
+// whole fibre into registers before it writes it, and fibres are disjoint.
+
+// X[s][l][i][r] <- sum_j M[i][j] X[s][l][j][r] (n x n message, in place)
+template <int CM, typename C>
+__device__ __forceinline__ void mode_product_inplace(C* X, const C* M, int L, int n, int Rr) {
+    const int per_s = L * Rr;
+    for (int f = threadIdx.x; f < 2 * per_s; f += blockDim.x) {
+        const int s = f >= per_s;
+        const int g = f - s * per_s;
+        const int l = g / Rr, r = g - l * Rr;
+        C* xp = X + (size_t)(s * L + l) * n * Rr + r;
+        C x[CM];
+#pragma unroll
+        for (int j = 0; j < CM; ++j) x[j] = j < n ? xp[(size_t)j * Rr] : c_zero<C>();
+        for (int i = 0; i < n; ++i) {
+            const C* mr = M + i * n;
+            C acc = c_zero<C>();
+#pragma unroll
+            for (int j = 0; j < CM; ++j)
+                if (j < n) acc = c_fma(mr[j], x[j], acc);
+            xp[(size_t)i * Rr] = acc;
+        }
+    }
+}
+
+// P[s][a][b] = sum_{l, r} conj(T[s][l][a][r]) X[s][l][b][r] with T, X in global memory: thread
+// (s, a, slice ks) accumulates row a of P_s over its slice of (l, r) (consecutive threads take
+// consecutive r, so the loads coalesce); the KS slices meet in shared memory (red, KS x 2n^2).
+template <int CM, typename C>
+__device__ __forceinline__ void close_global(const C* __restrict__ T, const C* __restrict__ X, C* __restrict__ P,
+                                             C* __restrict__ red, int L, int n, int Rr) {
+    const int groups = 2 * n;
+    const int KS = blockDim.x / groups;            // >= 1: blockDim >= 2 * 16
+    const int t = threadIdx.x;
+    const int g = t / KS, ks = t - g * KS;
+    const int K = L * Rr;
+    const size_t per_s = (size_t)L * n * Rr;
+    const int n2 = n * n;
+    if (g < groups) {
+        const int s = g / n, a = g - s * n;
+        C acc[CM];
+#pragma unroll
+        for (int b = 0; b < CM; ++b) acc[b] = c_zero<C>();
+        for (int k = ks; k < K; k += KS) {
+            const int l = k / Rr, r = k - l * Rr;
+            const size_t base = s * per_s + (size_t)l * n * Rr + r;
+            const C tv = T[base + (size_t)a * Rr];
+#pragma unroll
+            for (int b = 0; b < CM; ++b)
+                if (b < n) acc[b] = c_fma_conj(tv, X[base + (size_t)b * Rr], acc[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < CM; ++b)
+            if (b < n) red[(size_t)ks * 2 * n2 + s * n2 + a * n + b] = acc[b];
+    }
+    __syncthreads();
+    for (int o = t; o < 2 * n2; o += blockDim.x) {
+        C sum = c_zero<C>();
+        for (int q = 0; q < KS; ++q) sum = c_add(sum, red[(size_t)q * 2 * n2 + o]);
+        P[o] = sum;
+    }
+}
+
+__host__ __device__ inline size_t node_global_smem_elems(int d, int chi, int threads) {
+    const int n2 = chi * chi;
+    const int ks = threads / (2 * chi) > 0 ? threads / (2 * chi) : 1;
+    return (size_t)d * n2 + 2 * (size_t)n2 + (size_t)ks * 2 * n2 + 64;
+}
+
+template <int CM, int MODE, typename R>
+__global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int count, typename Cx<R>::T* scratch) {
+    using C = typename Cx<R>::T;
+    extern __shared__ double4 smem_raw[];
+    C* sm = reinterpret_cast<C*>(smem_raw);
+    const int d = a.d, chi = a.chi, n2 = chi * chi;
+    const int per_s = ipow(chi, d);
+    const size_t NT = 2 * (size_t)per_s;
+    C* sM = sm;
+    C* sP = sM + (size_t)d * n2;
+    C* sRedC = sP + 2 * n2;
+    const int ks = (int)blockDim.x / (2 * chi) > 0 ? (int)blockDim.x / (2 * chi) : 1;
+    R* sRed = reinterpret_cast<R*>(sRedC + (size_t)ks * 2 * n2);
+    C* work = scratch + (size_t)blockIdx.x * NT;
+
+    const C* msgs_in = a.msgs_a;
+    C* msgs_out = a.msgs_b;
+    if ((MODE == MODE_BP || MODE == MODE_PSPLIT) && a.loop_state != nullptr) {
+        if (a.loop_state[0]) return;
+        if (a.loop_state[2]) { msgs_in = a.msgs_b; msgs_out = const_cast<C*>(a.msgs_a); }
+    }
+    R num2 = 0, den2 = 0;
+    for (int node = blockIdx.x; node < count; node += gridDim.x) {
+        const C* T = a.tensors + (size_t)node * NT;
+        for (int k = 0; k < d; ++k) {
+            const C* mg = msgs_in + (size_t)a.in_pos[node * d + k] * n2;
+            for (int i = threadIdx.x; i < n2; i += blockDim.x) sM[k * n2 + i] = mg[i];
+        }
+        if (MODE == MODE_DENS) {
+            for (size_t i = threadIdx.x; i < NT; i += blockDim.x) work[i] = T[i];
+            __syncthreads();
+            for (int k = 0; k < d; ++k) {
+                mode_product_inplace<CM>(work, sM + k * n2, ipow(chi, k), chi, ipow(chi, d - 1 - k));
+                __syncthreads();
+            }
+            R v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int o = threadIdx.x; o < per_s; o += blockDim.x) {
+                const C x0 = work[o], x1 = work[per_s + o];
+                const C t0 = T[o], t1 = T[per_s + o];
+                const C r00 = c_fma_conj(t0, x0, c_zero<C>()), r01 = c_fma_conj(t1, x0, c_zero<C>());
+                const C r10 = c_fma_conj(t0, x1, c_zero<C>()), r11 = c_fma_conj(t1, x1, c_zero<C>());
+                v[0] += r00.x; v[1] += r00.y; v[2] += r01.x; v[3] += r01.y;
+                v[4] += r10.x; v[5] += r10.y; v[6] += r11.x; v[7] += r11.y;
+            }
+            block_sum<8>(v, sRed);
+            if (threadIdx.x < 4) {
+                const C tr = c_make(v[0] + v[6], v[1] + v[7]);
+                const C r = c_make(v[2 * threadIdx.x], v[2 * threadIdx.x + 1]);
+                a.out[(size_t)a.node_ids[node] * 4 + threadIdx.x] = c_div(r, tr);
+            }
+            __syncthreads();
+            continue;
+        }
+        for (int idx = 0; idx < d; ++idx) {
+            for (size_t i = threadIdx.x; i < NT; i += blockDim.x) work[i] = T[i];
+            __syncthreads();
+            for (int k = 0; k < d; ++k) {
+                if (k == idx) continue;
+                mode_product_inplace<CM>(work, sM + k * n2, ipow(chi, k), chi, ipow(chi, d - 1 - k));
+                __syncthreads();
+            }
+            close_global<CM>(T, work, sP, sRedC, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
+            __syncthreads();
+            write_outputs<MODE, R>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
+            __syncthreads();
+        }
+    }
+    if (MODE == MODE_BP) {
+        num2 = block_max(num2, sRed);
+        den2 = block_max(den2, sRed);
+        if (threadIdx.x == 0) {
+            atomic_max_nonneg(a.dist_parts, num2);
+            atomic_max_nonneg(a.dist_parts + 1, den2);
+        }
+    }
+}
+
+template <int MODE, typename R>
+static int launch_node_global(const NodeArgs<R>& args, int count, void* scratch, int64_t scratch_elems,
+                              cudaStream_t st) {
+    using C = typename Cx<R>::T;
+    const int chi = args.chi, d = args.d;
+    const int64_t need = 2 * (int64_t)ipow(chi, d);
+    if (!scratch || scratch_elems < need)
+        return set_error(BQA_ERR_UNSUPPORTED,
+                         "degree %d at bond dim %d exceeds shared memory and the class has %lld of the %lld "
+                         "scratch elements a CTA needs (bqa_node_scratch_elems)",
+                         d, chi, (long long)scratch_elems, (long long)need);
+    const int64_t ctas = std::min<int64_t>((int64_t)count, scratch_elems / need);
+    constexpr int threads = 256;
+    const size_t smem = node_global_smem_elems(d, chi, threads) * sizeof(C);
+    void (*kern)(NodeArgs<R>, int, C*) = nullptr;
+    if (chi <= 4) kern = node_kernel_global<4, MODE, R>;
+    else if (chi <= 8) kern = node_kernel_global<8, MODE, R>;
+    else if (chi <= 16) kern = node_kernel_global<16, MODE, R>;
+    else return set_error(BQA_ERR_UNSUPPORTED, "node kernel: bond dim %d > 16", chi);
+    int rc = ensure_smem((const void*)kern, smem, "node kernel (global)");
+    if (rc) return rc;
+    kern<<<(int)ctas, threads, smem, st>>>(args, count, static_cast<C*>(scratch));
+    return check_launch("node kernel (global)");
+}
 
 // Register-tiled complex64 kernel for compile-time (D, CHI): BP messages, extended messages,
 // densities.
@@ -610,9 +789,7 @@ static int run_classes(int mode, const bqa_class* classes, int n_classes, int ch
         const bqa_class& k = classes[c];
         if (k.count <= 0) continue;
         if (k.degree == 0 && mode != MODE_DENS) continue;
-        if (node_smem_elems(k.degree, chi) * sizeof(C) > kMaxSmem)
-            return set_error(BQA_ERR_UNSUPPORTED, "degree %d at bond dim %d does not fit shared memory",
-                             k.degree, chi);
+        const bool global = node_smem_elems(k.degree, chi) * sizeof(C) > kMaxSmem;
         NodeArgs<R> a;
         a.tensors = static_cast<const C*>(k.tensor);
         a.in_pos = k.in_pos;
@@ -628,11 +805,22 @@ static int run_classes(int mode, const bqa_class* classes, int n_classes, int ch
         a.dist_parts = static_cast<typename Cx<R>::Bits*>(dist_parts);
         a.ztime = ztime;
         int rc = BQA_OK;
-        switch (mode) {
-            case MODE_BP: rc = launch_node_mode<MODE_BP>(a, k.count, st); break;
-            case MODE_EXT: rc = launch_node_mode<MODE_EXT>(a, k.count, st); break;
-            case MODE_PSPLIT: rc = launch_node_mode<MODE_PSPLIT>(a, k.count, st); break;
-            default: rc = launch_node_mode<MODE_DENS>(a, k.count, st); break;
+        if (global) {
+            switch (mode) {
+                case MODE_BP: rc = launch_node_global<MODE_BP>(a, k.count, k.scratch, k.scratch_elems, st); break;
+                case MODE_EXT: rc = launch_node_global<MODE_EXT>(a, k.count, k.scratch, k.scratch_elems, st); break;
+                case MODE_PSPLIT:
+                    rc = launch_node_global<MODE_PSPLIT>(a, k.count, k.scratch, k.scratch_elems, st);
+                    break;
+                default: rc = launch_node_global<MODE_DENS>(a, k.count, k.scratch, k.scratch_elems, st); break;
+            }
+        } else {
+            switch (mode) {
+                case MODE_BP: rc = launch_node_mode<MODE_BP>(a, k.count, st); break;
+                case MODE_EXT: rc = launch_node_mode<MODE_EXT>(a, k.count, st); break;
+                case MODE_PSPLIT: rc = launch_node_mode<MODE_PSPLIT>(a, k.count, st); break;
+                default: rc = launch_node_mode<MODE_DENS>(a, k.count, st); break;
+            }
         }
         if (rc) return rc;
     }
@@ -763,6 +951,16 @@ int32_t bqa_max_bond_dim(int32_t degree, int32_t dtype) {
     for (int chi = 1; chi <= 16; ++chi)
         if (node_smem_elems(degree, chi) * el <= kMaxSmem) best = chi;
     return best;
+}
+
+int64_t bqa_node_scratch_elems(int32_t degree, int32_t chi, int32_t dtype) {
+    if (degree < 0 || chi < 1 || (dtype != BQA_C64 && dtype != BQA_C128)) return 0;
+    const size_t el = dtype == BQA_C64 ? 8 : 16;
+    const bool msg_fits = node_smem_elems(degree, chi) * el <= kMaxSmem;
+    const bool upd_fits = apply_smem_bytes(degree, chi, el) <= kMaxSmem;
+    if (msg_fits && upd_fits) return 0;
+    // message kernels: one work tensor 2 chi^d; update: two 2 chi^d buffers
+    return 4 * (int64_t)ipow(chi, degree);
 }
 
 int32_t bqa_bp_sweep(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, void* msgs_a,

@@ -11,6 +11,8 @@
 //   _apply_z_layer / _apply_x_layer         src/bqa/state.py:142-156, backends.py:506-510
 //   _set_to_symmetric_gauge (tensor part)   src/bqa/state.py:219-227, backends.py:450-462
 // (all factors are diagonal in s except Rx, which is applied after the bond products).
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 #include "tiled_node.cuh"
@@ -129,6 +131,70 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyArgs<R> a) {
 }
 
 
+size_t apply_smem_bytes(int d, int chi, size_t elem_bytes) { return apply_smem_elems(d, chi, chi) * elem_bytes; }
+
+// Node tensors beyond shared memory: the same update with X and Y in a per-CTA slice of
+// caller scratch (2 x 2 m^d complex, m = max(chi, dim)); the bond matrices W stay in shared
+// memory.  Each CTA walks nodes blockIdx.x, blockIdx.x + gridDim.x, ...
+template <int CM, typename R>
+__global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int count, typename Cx<R>::T* scratch) {
+    using C = typename Cx<R>::T;
+    extern __shared__ double4 smem_raw[];
+    C* sW = reinterpret_cast<C*>(smem_raw);
+    const int d = a.d, chi = a.chi, dim = a.dim, n = 2 * chi;
+    const int m = chi > dim ? chi : dim;
+    const size_t buf = 2 * (size_t)ipow(m, d);
+    R* sRed = reinterpret_cast<R*>(sW + (size_t)d * 2 * dim * chi);
+    C* X0 = scratch + (size_t)blockIdx.x * 2 * buf;
+    C* Y0 = X0 + buf;
+    const int nin = 2 * ipow(chi, d);
+    const int per_s = ipow(dim, d);
+    for (int node = blockIdx.x; node < count; node += gridDim.x) {
+        const C* tg = a.t_in + (size_t)node * nin;
+        for (int i = threadIdx.x; i < nin; i += blockDim.x) X0[i] = tg[i];
+        for (int k = 0; k < d; ++k) {
+            const HalfZZ<R> h = half_zz<R>(a.edge_ampl[node * d + k] * a.ztime);
+            const C* Cc = a.canon + (size_t)a.in_pos[node * d + k] * n * n;
+            const R* lam = a.lmbds + (size_t)a.lmbd_pos[node * d + k] * a.lam_stride;
+            for (int o = threadIdx.x; o < 2 * dim * chi; o += blockDim.x) {
+                const int s = o / (dim * chi);
+                const int cj = o - s * dim * chi;
+                const int c = cj / chi, j = cj - c * chi;
+                const C up = c_mul(h.a0, Cc[(size_t)j * n + c]);
+                const C dn = c_mul(h.a1, Cc[(size_t)(chi + j) * n + c]);
+                const C w = s ? c_sub(up, dn) : c_add(up, dn);
+                sW[(size_t)k * 2 * dim * chi + o] = c_scale(w, sqrt(lam[c]));
+            }
+        }
+        __syncthreads();
+        C* cur = X0;
+        C* nxt = Y0;
+        for (int k = 0; k < d; ++k) {
+            const C* W0 = sW + (size_t)k * 2 * dim * chi;
+            bond_product<CM>(cur, nxt, W0, W0 + dim * chi, ipow(dim, k), chi, dim, ipow(chi, d - 1 - k));
+            __syncthreads();
+            C* t = cur; cur = nxt; nxt = t;
+        }
+        double sz, cz;
+        sincos(a.node_ampl[node] * a.ztime, &sz, &cz);
+        const C z0 = c_make((R)cz, (R)-sz), z1 = c_make((R)cz, (R)sz);
+        R acc[1] = {0};
+        for (int o = threadIdx.x; o < per_s; o += blockDim.x) {
+            const C y0 = c_mul(z0, cur[o]), y1 = c_mul(z1, cur[per_s + o]);
+            const C t0 = c_make(a.cx * y0.x + a.sx * y1.y, a.cx * y0.y - a.sx * y1.x);
+            const C t1 = c_make(a.cx * y1.x + a.sx * y0.y, a.cx * y1.y - a.sx * y0.x);
+            cur[o] = t0;
+            cur[per_s + o] = t1;
+            acc[0] += c_abs2(t0) + c_abs2(t1);
+        }
+        block_sum<1>(acc, sRed);
+        const R inv = R(1) / sqrt(acc[0]);
+        C* og = a.t_out + (size_t)node * 2 * per_s;
+        for (int o = threadIdx.x; o < 2 * per_s; o += blockDim.x) og[o] = c_scale(cur[o], inv);
+        __syncthreads();
+    }
+}
+
 // ---- register-tiled update for dim == chi, complex64 ------------------------------------------
 // CTA (node, s) stages T_s and the three s-specific bond matrices W_k^s (with sqrt(lambda) and,
 // on bond 0, the Rz phase z_s folded in), runs the d bond products with the tiled GEMM of the
@@ -231,9 +297,7 @@ static int apply_classes(const bqa_class* classes, int n_classes, int chi, int d
         const bqa_class& k = classes[c];
         if (k.count <= 0) continue;
         const size_t smem = apply_smem_elems(k.degree, chi, dim) * sizeof(C);
-        if (smem > kMaxSmem)
-            return set_error(BQA_ERR_UNSUPPORTED, "apply: degree %d at bond dim %d->%d does not fit shared memory",
-                             k.degree, chi, dim);
+        const bool global = smem > kMaxSmem;
         ApplyArgs<R> a;
         a.t_in = static_cast<const C*>(k.tensor);
         a.t_out = static_cast<C*>(k.tensor_out);
@@ -250,6 +314,27 @@ static int apply_classes(const bqa_class* classes, int n_classes, int chi, int d
         a.ztime = ztime;
         a.cx = (R)cos(xtime);
         a.sx = (R)sin(xtime);
+        if (global) {
+            const int64_t need = 4 * (int64_t)ipow(cm, k.degree);
+            if (!k.scratch || k.scratch_elems < need)
+                return set_error(BQA_ERR_UNSUPPORTED,
+                                 "apply: degree %d at bond dim %d->%d exceeds shared memory and the class has %lld "
+                                 "of the %lld scratch elements a CTA needs (bqa_node_scratch_elems)",
+                                 k.degree, chi, dim, (long long)k.scratch_elems, (long long)need);
+            const int64_t ctas = std::min<int64_t>((int64_t)k.count, k.scratch_elems / need);
+            const size_t gsmem = ((size_t)k.degree * 2 * dim * chi + 64) * sizeof(C);
+            void (*gk)(ApplyArgs<R>, int, C*) = nullptr;
+            if (chi <= 4) gk = apply_kernel_global<4, R>;
+            else if (chi <= 8) gk = apply_kernel_global<8, R>;
+            else if (chi <= 16) gk = apply_kernel_global<16, R>;
+            else return set_error(BQA_ERR_UNSUPPORTED, "apply: bond dim %d > 16", chi);
+            int rc = ensure_smem((const void*)gk, gsmem, "apply (global)");
+            if (rc) return rc;
+            gk<<<(int)ctas, 256, gsmem, st>>>(a, k.count, static_cast<C*>(k.scratch));
+            rc = check_launch("apply (global)");
+            if (rc) return rc;
+            continue;
+        }
         if constexpr (sizeof(R) == 4) {
             int trc = BQA_OK;
             if (k.degree >= 2 && try_tiled_apply(a, k.count, st, &trc)) {

@@ -100,13 +100,20 @@ class Annealer:
         # BP sweeps in two stages (half-node message kernels + combine) on the complex64 path
         self.split_sweeps = self.precision == "single"
         chimax = self._store(ctx.max_bond_dim)
-        for d in ctx.degree_to_layout:
-            lim = self.lib.max_bond_dim(d, self.dtype)
-            if chimax > lim:
-                raise NotImplementedError(
-                    f"max_bond_dim={chimax} with degree-{d} nodes is beyond what the GB300 kernels "
-                    f"hold on chip at {self.precision} precision (max {lim} for this degree)")
+        if chimax > 16:
+            raise NotImplementedError(
+                f"max_bond_dim={chimax}: the truncation's Jacobi SVDs take 2*chi <= 32 (chi <= 16)")
         dev = self.device
+        # classes whose node tensors exceed shared memory run on CTAs with work tensors in
+        # this scratch (one buffer, shared: classes run one after another on the stream)
+        n_ctas = 2 * torch.cuda.get_device_properties(self.device).multi_processor_count
+        scratch_elems = 0
+        for d, L in ctx.degree_to_layout.items():
+            per_cta = int(self.lib.dll.bqa_node_scratch_elems(d, chimax, self.dtype))
+            if per_cta:
+                scratch_elems = max(scratch_elems, min(L.batch_size, n_ctas) * per_cta)
+        self.scratch = torch.empty(scratch_elems, dtype=cplx, device=dev) if scratch_elems else None
+        self.scratch_elems = scratch_elems
         i32 = torch.int32
         self.classes: list[_DeviceClass] = []
         for d, L in ctx.degree_to_layout.items():
@@ -198,7 +205,8 @@ class Annealer:
             arr[i] = _lib.BqaClass(
                 c.degree, c.count, _ptr(c.node_ids), _ptr(c.in_pos), _ptr(c.out_pos), _ptr(c.lmbd_pos),
                 _ptr(c.edge_ampl), _ptr(c.node_ampl), _ptr(c.tensors[self.tcur]),
-                _ptr(c.tensors[1 - self.tcur]) if out else 0)
+                _ptr(c.tensors[1 - self.tcur]) if out else 0,
+                _ptr(self.scratch) if self.scratch is not None else 0, self.scratch_elems)
         return arr
 
     @property

@@ -23,6 +23,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import _lib
 from . import config as cfg
 from .engine import Annealer, resolve_precision
 from .layout import Context, build_context
@@ -47,6 +48,11 @@ def job_footprint(ctx: Context, precision: str | None = None) -> int:
     total += 2 * E * chi * chi * es                        # messages
     total += 3 * E * nmax * nmax * es                      # ext / lu / ul
     total += half * nmax * rs + n * 4 * es + half * 8      # lambdas, densities, <ZZ>
+    # work tensors for classes beyond shared memory (engine: min(count, 2 x SMs) CTAs)
+    lib = _lib.load()
+    dt = _lib.BQA_C64 if p == "single" else _lib.BQA_C128
+    total += max((min(L.batch_size, 2 * 152) * int(lib.dll.bqa_node_scratch_elems(d, chi, dt)) * es
+                  for d, L in ctx.degree_to_layout.items()), default=0)
     return int(total) + (1 << 20)
 
 

@@ -65,10 +65,21 @@ typedef struct bqa_class {
     const double* node_ampl;   /* [B]    field h of the node */
     void* tensor;              /* [B][2][chi^d] complex, current tensors */
     void* tensor_out;          /* [B][2][dim^d] complex, written by bqa_apply_update */
+    void* scratch;             /* complex work space for node tensors beyond shared memory (or NULL) */
+    int64_t scratch_elems;     /* its size in complex elements; see bqa_node_scratch_elems */
 } bqa_class;
 
 /* ABI version of this header (bumped on any signature change). */
 int32_t bqa_abi_version(void);
+
+/*
+ * Complex elements of scratch one CTA needs to process a class of degree `degree` at bond
+ * dim chi (updates to dims <= chi) when its node tensors exceed shared memory, 0 when they
+ * fit.  Such a class runs on min(count, scratch_elems / this) CTAs, each walking its share of
+ * the nodes with the work tensors in its slice of bqa_class.scratch (the reference handles
+ * any degree; this is the path for large chi^d, e.g. degree 5-6 at chi 8).
+ */
+int64_t bqa_node_scratch_elems(int32_t degree, int32_t chi, int32_t dtype);
 
 /* Text of the last error raised on the calling host thread (static storage). */
 const char* bqa_last_error(void);
