@@ -312,10 +312,12 @@ __device__ __forceinline__ void close_global(const C* __restrict__ T, const C* _
     }
 }
 
+// messages, P, the closing partials, then the block reductions' scratch (block_sum<8>
+// takes 8 x 32 reals: 128 complex elements hold them for float and double)
 __host__ __device__ inline size_t node_global_smem_elems(int d, int chi, int threads) {
     const int n2 = chi * chi;
     const int ks = threads / (2 * chi) > 0 ? threads / (2 * chi) : 1;
-    return (size_t)d * n2 + 2 * (size_t)n2 + (size_t)ks * 2 * n2 + 64;
+    return (size_t)d * n2 + 2 * (size_t)n2 + (size_t)ks * 2 * n2 + 128;
 }
 
 template <int CM, int MODE, typename R>
