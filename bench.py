@@ -596,6 +596,47 @@ def run_small_mode(args) -> None:
                       "mean_sweeps": float(np.mean([w["sweeps"] for w in job.stats]))}))
 
 
+def run_mixed_mode(args) -> None:
+    """Mixed degrees (periodic grid, degree 4, plus a configuration-model graph with degrees in
+    {2, 3, 5, 6}) at bond dim --chi: anneal until the bond dim saturates (at most 60 steps),
+    then time --steps steps; per-kernel split by CUDA events.  --n sets the extra nodes and the
+    grid side (sqrt(1.8 n)), the full mixed configuration being n = 50,000 (300 x 300)."""
+    import torch
+    from bqa_gb300 import instances
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
+    side = max(4, int(round(np.sqrt(1.8 * args.n))))
+    ctx = build_context(instances.mixed_degree_job(rows=side, cols=side, extra=args.n, chi=args.chi))
+    steps = [i for i in ctx.instructions if isinstance(i, dict)]
+    job = Annealer(ctx)
+    s, t0 = 0, time.perf_counter()
+    while job.bond_dim < args.chi and s < 60:
+        job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
+        s += 1
+    prep = time.perf_counter() - t0
+    for i in range(args.warmup):
+        job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
+        s += 1
+    job.enable_kernel_timing(True)
+    job.stats.clear()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for i in range(args.steps):
+        job.run_layer(steps[s + i]["xtime"], steps[s + i]["ztime"])
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    split: dict = {}
+    for name, t, _, _ in job.kernel_times():
+        split[name] = round(split.get(name, 0.0) + t / args.steps, 2)
+    print(json.dumps({"mode": "mixed", "nodes": ctx.nodes_number, "classes": {int(d): L.batch_size for d, L in
+                      ctx.degree_to_layout.items()}, "chi": job.bond_dim, "prep_steps": s - args.warmup,
+                      "prep_s": round(prep, 1), "steps_per_s": args.steps / (ms / 1e3),
+                      "sweeps_per_step": float(np.mean([w["sweeps"] for w in job.stats])),
+                      "ms_per_step_split": split, "scratch_bytes": job.scratch_elems * 8}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -605,7 +646,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout", "small"])
+    ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout", "small", "mixed"])
     ap.add_argument("--jobs", type=int, default=32)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--precision", default="single", choices=["single", "double"])
@@ -624,6 +665,8 @@ def main() -> None:
         run_layout_mode(args)
     elif args.mode == "small":
         run_small_mode(args)
+    elif args.mode == "mixed":
+        run_mixed_mode(args)
     else:
         run_gpu_arm(args)
 
