@@ -274,76 +274,52 @@ __device__ __forceinline__ void mode_product_inplace(C* X, const C* M, int L, in
     }
 }
 
-// P[s][a][b] = sum_{l, r} conj(X[s][l][a][r]) Y[s][l][b][r] with X, Y in global memory, in
-// chunks of KC positions k = (l, r) staged in shared memory (every element read once); thread t
-// owns output o = t % (2n^2) for slice t / (2n^2) of each chunk (2n^2 <= blockDim), or outputs
-// t, t + blockDim, ... for the whole chunk; slices meet in `red`.
-template <typename C>
-__device__ __forceinline__ void close_global(const C* __restrict__ X, const C* __restrict__ Y, C* __restrict__ P,
-                                             C* __restrict__ stage, C* __restrict__ red, int L, int n, int Rr) {
-    const int K = L * Rr;
-    const int KC = 1024 / n;
-    const int KP = KC + 1;                            // padded row: rows b, b+1 differ in bank
-    const int n2 = n * n, outs = 2 * n2;
-    const int slices = outs <= (int)blockDim.x ? (int)blockDim.x / outs : 1;
+// P[s][a][b] = sum_{l, r} conj(T[s][l][a][r]) X[s][l][b][r] with T, X in global memory: thread
+// (s, a, slice ks) accumulates row a of P_s over its slice of (l, r) (consecutive threads take
+// consecutive r, so the loads coalesce); the KS slices meet in shared memory (red, KS x 2n^2).
+template <int CM, typename C>
+__device__ __forceinline__ void close_global(const C* __restrict__ T, const C* __restrict__ X, C* __restrict__ P,
+                                             C* __restrict__ red, int L, int n, int Rr) {
+    const int groups = 2 * n;
+    const int KS = blockDim.x / groups;            // >= 1: blockDim >= 2 * 16
     const int t = threadIdx.x;
+    const int g = t / KS, ks = t - g * KS;
+    const int K = L * Rr;
     const size_t per_s = (size_t)L * n * Rr;
-    C* Xs = stage;                                    // [2][n][KP]
-    C* Ys = stage + 2 * n * KP;
-    C acc[2] = {c_zero<C>(), c_zero<C>()};
-    for (int k0 = 0; k0 < K; k0 += KC) {
-        const int kc = min(KC, K - k0);
-        for (int e = t; e < 2 * n * kc; e += blockDim.x) {
-            const int sa = e / kc, kk = e - sa * kc;
-            const int s = sa / n, a = sa - s * n;
-            const int k = k0 + kk, l = k / Rr, r = k - l * Rr;
-            const size_t src = s * per_s + ((size_t)l * n + a) * Rr + r;
-            Xs[sa * KP + kk] = X[src];
-            Ys[sa * KP + kk] = Y[src];
+    const int n2 = n * n;
+    if (g < groups) {
+        const int s = g / n, a = g - s * n;
+        C acc[CM];
+#pragma unroll
+        for (int b = 0; b < CM; ++b) acc[b] = c_zero<C>();
+        for (int k = ks; k < K; k += KS) {
+            const int l = k / Rr, r = k - l * Rr;
+            const size_t base = s * per_s + (size_t)l * n * Rr + r;
+            const C tv = T[base + (size_t)a * Rr];
+#pragma unroll
+            for (int b = 0; b < CM; ++b)
+                if (b < n) acc[b] = c_fma_conj(tv, X[base + (size_t)b * Rr], acc[b]);
         }
-        __syncthreads();
-        if (outs <= (int)blockDim.x) {
-            const int o = t % outs, sl = t / outs;
-            if (sl < slices) {
-                const int s = o / n2, ab = o - s * n2, a = ab / n, b = ab - a * n;
-                const C* xr = Xs + (s * n + a) * KP;
-                const C* yr = Ys + (s * n + b) * KP;
-                for (int kk = sl; kk < kc; kk += slices) acc[0] = c_fma_conj(xr[kk], yr[kk], acc[0]);
-            }
-        } else {
-            for (int q = 0; q < 2; ++q) {
-                const int o = t + q * blockDim.x;
-                if (o >= outs) break;
-                const int s = o / n2, ab = o - s * n2, a = ab / n, b = ab - a * n;
-                const C* xr = Xs + (s * n + a) * KP;
-                const C* yr = Ys + (s * n + b) * KP;
-                for (int kk = 0; kk < kc; ++kk) acc[q] = c_fma_conj(xr[kk], yr[kk], acc[q]);
-            }
-        }
-        __syncthreads();
+#pragma unroll
+        for (int b = 0; b < CM; ++b)
+            if (b < n) red[(size_t)ks * 2 * n2 + s * n2 + a * n + b] = acc[b];
     }
-    if (outs <= (int)blockDim.x) {
-        const int o = t % outs, sl = t / outs;
-        if (sl < slices) red[(size_t)sl * outs + o] = acc[0];
-        __syncthreads();
-        for (int o2 = t; o2 < outs; o2 += blockDim.x) {
-            C sum = c_zero<C>();
-            for (int q = 0; q < slices; ++q) sum = c_add(sum, red[(size_t)q * outs + o2]);
-            P[o2] = sum;
-        }
-    } else {
-        for (int q = 0; q < 2; ++q)
-            if (t + q * (int)blockDim.x < outs) P[t + q * blockDim.x] = acc[q];
+    __syncthreads();
+    for (int o = t; o < 2 * n2; o += blockDim.x) {
+        C sum = c_zero<C>();
+        for (int q = 0; q < KS; ++q) sum = c_add(sum, red[(size_t)q * 2 * n2 + o]);
+        P[o] = sum;
     }
 }
 
-// shared memory of the global kernel: messages, P, the close's staging and slice partials,
-// the block reductions' scratch (block_sum<8>: 8 x 32 reals fit 128 complex elements)
+// messages, P, the closing partials, then the block reductions' scratch (block_sum<8>
+// takes 8 x 32 reals: 128 complex elements hold them for float and double)
+// shared memory of the global kernel: messages, P, the close's slice partials, the block
+// reductions' scratch (block_sum<8>: 8 x 32 reals fit 128 complex elements)
 __host__ __device__ inline size_t node_global_smem_elems(int d, int chi, int threads) {
-    const int n2 = chi * chi, outs = 2 * n2;
-    const int KP = 1024 / chi + 1;
-    const int slices = outs <= threads ? threads / outs : 1;
-    return (size_t)d * n2 + 2 * (size_t)n2 + 4 * (size_t)chi * KP + (size_t)slices * outs + 128;
+    const int n2 = chi * chi;
+    const int ks = threads / (2 * chi) > 0 ? threads / (2 * chi) : 1;
+    return (size_t)d * n2 + 2 * (size_t)n2 + (size_t)ks * 2 * n2 + 128;
 }
 
 // T x_k M_k for k in [k0, k1) except `skip`, into W (copy of T, then products in place)
@@ -371,13 +347,11 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
     const int d = a.d, chi = a.chi, n2 = chi * chi;
     const int per_s = ipow(chi, d);
     const size_t NT = 2 * (size_t)per_s;
-    const int outs = 2 * n2, KP = 1024 / chi + 1;
-    const int slices = outs <= (int)blockDim.x ? (int)blockDim.x / outs : 1;
+    const int ks = (int)blockDim.x / (2 * chi) > 0 ? (int)blockDim.x / (2 * chi) : 1;
     C* sM = sm;
     C* sP = sM + (size_t)d * n2;
-    C* stage = sP + 2 * n2;
-    C* red = stage + 4 * (size_t)chi * KP;
-    R* sRed = reinterpret_cast<R*>(red + (size_t)slices * outs);
+    C* red = sP + 2 * n2;
+    R* sRed = reinterpret_cast<R*>(red + (size_t)ks * 2 * n2);
     C* Wa = scratch + (size_t)blockIdx.x * 2 * NT;
     C* Wb = Wa + NT;
     const int h = d / 2;
@@ -424,7 +398,7 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
             if (idx == h) apply_messages<CM>(T, Wa, sM, d, chi, NT, 0, h, -1);   // Wa = T x_A for idx in B
             if (idx < h) apply_messages<CM>(T, Wa, sM, d, chi, NT, 0, h, idx);
             else apply_messages<CM>(T, Wb, sM, d, chi, NT, h, d, idx);
-            close_global(Wa, Wb, sP, stage, red, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
+            close_global<CM>(Wa, Wb, sP, red, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
             __syncthreads();
             write_outputs<MODE, R>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
             __syncthreads();
