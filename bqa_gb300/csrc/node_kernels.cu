@@ -274,52 +274,94 @@ __device__ __forceinline__ void mode_product_inplace(C* X, const C* M, int L, in
     }
 }
 
-// P[s][a][b] = sum_{l, r} conj(T[s][l][a][r]) X[s][l][b][r] with T, X in global memory: thread
-// (s, a, slice ks) accumulates row a of P_s over its slice of (l, r) (consecutive threads take
-// consecutive r, so the loads coalesce); the KS slices meet in shared memory (red, KS x 2n^2).
-template <int CM, typename C>
-__device__ __forceinline__ void close_global(const C* __restrict__ T, const C* __restrict__ X, C* __restrict__ P,
-                                             C* __restrict__ red, int L, int n, int Rr) {
-    const int groups = 2 * n;
-    const int KS = blockDim.x / groups;            // >= 1: blockDim >= 2 * 16
-    const int t = threadIdx.x;
-    const int g = t / KS, ks = t - g * KS;
+// P[s][a][b] = sum_{l, r} conj(X[s][l][a][r]) Y[s][l][b][r] with X, Y in global memory.  Chunks
+// of KC positions k = (l, r) are staged in shared memory (each element read from global memory
+// once; rows padded to NP = n rounded up to 4, zero beyond n); thread (s, 4x4 tile of (a, b),
+// K-slice sl) accumulates its tile over the slice (8 shared loads per 16 complex FMAs); the
+// slices meet in `red` (4096 complex elements).
+constexpr int kCloseKC = 64;
+constexpr int kCloseRed = 4096;
+
+template <typename C>
+__device__ __forceinline__ void close_global(const C* __restrict__ X, const C* __restrict__ Y, C* __restrict__ P,
+                                             C* __restrict__ stage, C* __restrict__ red, int L, int n, int Rr) {
+    constexpr int KC = kCloseKC, KP = KC + 1;
     const int K = L * Rr;
+    const int NPd = (n + 3) & ~3;
+    const int ntile = NPd / 4;
+    const int tiles = 2 * ntile * ntile;
+    const int SL = (int)blockDim.x / tiles;            // >= 1 for n <= 16 and 256 threads
+    const int t = threadIdx.x;
+    const int tile = t / SL, sl = t - tile * SL;
+    const bool active = tile < tiles;
+    const int s = active ? tile / (ntile * ntile) : 0;
+    const int ag = active ? (tile / ntile) % ntile : 0, bg = active ? tile % ntile : 0;
     const size_t per_s = (size_t)L * n * Rr;
-    const int n2 = n * n;
-    if (g < groups) {
-        const int s = g / n, a = g - s * n;
-        C acc[CM];
+    C* Xs = stage;                                     // [2][NPd][KP]
+    C* Ys = stage + 2 * NPd * KP;
+    C acc[4][4];
 #pragma unroll
-        for (int b = 0; b < CM; ++b) acc[b] = c_zero<C>();
-        for (int k = ks; k < K; k += KS) {
-            const int l = k / Rr, r = k - l * Rr;
-            const size_t base = s * per_s + (size_t)l * n * Rr + r;
-            const C tv = T[base + (size_t)a * Rr];
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int b = 0; b < CM; ++b)
-                if (b < n) acc[b] = c_fma_conj(tv, X[base + (size_t)b * Rr], acc[b]);
+        for (int v = 0; v < 4; ++v) acc[u][v] = c_zero<C>();
+    for (int k0 = 0; k0 < K; k0 += KC) {
+        const int kc = min(KC, K - k0);
+        for (int e = t; e < 2 * NPd * KC; e += blockDim.x) {
+            const int sa = e / KC, kk = e - sa * KC;
+            const int ss = sa / NPd, aa = sa - ss * NPd;
+            C xv = c_zero<C>(), yv = c_zero<C>();
+            if (aa < n && kk < kc) {
+                const int k = k0 + kk, l = k / Rr, r = k - l * Rr;
+                const size_t src = ss * per_s + ((size_t)l * n + aa) * Rr + r;
+                xv = X[src];
+                yv = Y[src];
+            }
+            Xs[sa * KP + kk] = xv;
+            Ys[sa * KP + kk] = yv;
         }
+        __syncthreads();
+        if (active) {
+            const C* xr = Xs + (s * NPd + ag * 4) * KP;
+            const C* yr = Ys + (s * NPd + bg * 4) * KP;
+            for (int kk = sl; kk < kc; kk += SL) {
+                C xv[4], yv[4];
 #pragma unroll
-        for (int b = 0; b < CM; ++b)
-            if (b < n) red[(size_t)ks * 2 * n2 + s * n2 + a * n + b] = acc[b];
+                for (int u = 0; u < 4; ++u) xv[u] = xr[u * KP + kk];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) yv[v] = yr[v * KP + kk];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) acc[u][v] = c_fma_conj(xv[u], yv[v], acc[u][v]);
+            }
+        }
+        __syncthreads();
+    }
+    // slice partials: red[sl][tile][16]
+    if (active) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) red[((size_t)sl * tiles + tile) * 16 + u * 4 + v] = acc[u][v];
     }
     __syncthreads();
+    const int n2 = n * n;
     for (int o = t; o < 2 * n2; o += blockDim.x) {
+        const int os = o / n2, ab = o - os * n2, a = ab / n, b = ab - a * n;
+        const int tl = (os * ntile + a / 4) * ntile + b / 4, q = (a & 3) * 4 + (b & 3);
         C sum = c_zero<C>();
-        for (int q = 0; q < KS; ++q) sum = c_add(sum, red[(size_t)q * 2 * n2 + o]);
+        for (int z = 0; z < SL; ++z) sum = c_add(sum, red[((size_t)z * tiles + tl) * 16 + q]);
         P[o] = sum;
     }
 }
 
-// messages, P, the closing partials, then the block reductions' scratch (block_sum<8>
-// takes 8 x 32 reals: 128 complex elements hold them for float and double)
-// shared memory of the global kernel: messages, P, the close's slice partials, the block
-// reductions' scratch (block_sum<8>: 8 x 32 reals fit 128 complex elements)
+// shared memory of the global kernel: messages, P, the close's staging and slice partials, the
+// block reductions' scratch (block_sum<8>: 8 x 32 reals fit 128 complex elements)
 __host__ __device__ inline size_t node_global_smem_elems(int d, int chi, int threads) {
+    (void)threads;
     const int n2 = chi * chi;
-    const int ks = threads / (2 * chi) > 0 ? threads / (2 * chi) : 1;
-    return (size_t)d * n2 + 2 * (size_t)n2 + (size_t)ks * 2 * n2 + 128;
+    const int NPd = (chi + 3) & ~3;
+    return (size_t)d * n2 + 2 * (size_t)n2 + 4 * (size_t)NPd * (kCloseKC + 1) + kCloseRed + 128;
 }
 
 // T x_k M_k for k in [k0, k1) except `skip`, into W (copy of T, then products in place)
@@ -347,11 +389,12 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
     const int d = a.d, chi = a.chi, n2 = chi * chi;
     const int per_s = ipow(chi, d);
     const size_t NT = 2 * (size_t)per_s;
-    const int ks = (int)blockDim.x / (2 * chi) > 0 ? (int)blockDim.x / (2 * chi) : 1;
+    const int NPd = (chi + 3) & ~3;
     C* sM = sm;
     C* sP = sM + (size_t)d * n2;
-    C* red = sP + 2 * n2;
-    R* sRed = reinterpret_cast<R*>(red + (size_t)ks * 2 * n2);
+    C* stage = sP + 2 * n2;
+    C* red = stage + 4 * (size_t)NPd * (kCloseKC + 1);
+    R* sRed = reinterpret_cast<R*>(red + kCloseRed);
     C* Wa = scratch + (size_t)blockIdx.x * 2 * NT;
     C* Wb = Wa + NT;
     const int h = d / 2;
@@ -398,7 +441,7 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
             if (idx == h) apply_messages<CM>(T, Wa, sM, d, chi, NT, 0, h, -1);   // Wa = T x_A for idx in B
             if (idx < h) apply_messages<CM>(T, Wa, sM, d, chi, NT, 0, h, idx);
             else apply_messages<CM>(T, Wb, sM, d, chi, NT, h, d, idx);
-            close_global<CM>(Wa, Wb, sP, red, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
+            close_global(Wa, Wb, sP, stage, red, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
             __syncthreads();
             write_outputs<MODE, R>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
             __syncthreads();

@@ -104,9 +104,9 @@ class Annealer:
             raise NotImplementedError(
                 f"max_bond_dim={chimax}: the truncation's Jacobi SVDs take 2*chi <= 32 (chi <= 16)")
         dev = self.device
-        # classes whose node tensors exceed shared memory run on CTAs with work tensors in
-        # this scratch (one buffer, shared: classes run one after another on the stream)
-        n_ctas = 2 * torch.cuda.get_device_properties(self.device).multi_processor_count
+        # classes whose node tensors exceed shared memory run on up to 8 CTAs per SM with work
+        # tensors in this scratch (one buffer, shared: classes run one after another on the stream)
+        n_ctas = 8 * torch.cuda.get_device_properties(self.device).multi_processor_count
         scratch_elems = 0
         for d, L in ctx.degree_to_layout.items():
             per_cta = int(self.lib.dll.bqa_node_scratch_elems(d, chimax, self.dtype))

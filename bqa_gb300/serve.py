@@ -48,10 +48,10 @@ def job_footprint(ctx: Context, precision: str | None = None) -> int:
     total += 2 * E * chi * chi * es                        # messages
     total += 3 * E * nmax * nmax * es                      # ext / lu / ul
     total += half * nmax * rs + n * 4 * es + half * 8      # lambdas, densities, <ZZ>
-    # work tensors for classes beyond shared memory (engine: min(count, 2 x SMs) CTAs)
+    # work tensors for classes beyond shared memory (engine: min(count, 8 x SMs) CTAs)
     lib = _lib.load()
     dt = _lib.BQA_C64 if p == "single" else _lib.BQA_C128
-    total += max((min(L.batch_size, 2 * 152) * int(lib.dll.bqa_node_scratch_elems(d, chi, dt)) * es
+    total += max((min(L.batch_size, 8 * 152) * int(lib.dll.bqa_node_scratch_elems(d, chi, dt)) * es
                   for d, L in ctx.degree_to_layout.items()), default=0)
     return int(total) + (1 << 20)
 
