@@ -364,15 +364,22 @@ __host__ __device__ inline size_t node_global_smem_elems(int d, int chi, int thr
     return (size_t)d * n2 + 2 * (size_t)n2 + 4 * (size_t)NPd * (kCloseKC + 1) + kCloseRed + 128;
 }
 
-// T x_k M_k for k in [k0, k1) except `skip`, into W (copy of T, then products in place)
+// T x_k M_k for k in [k0, k1) except `skip`, into W: the first product reads T and writes W,
+// the others run in place (a plain copy when the set is empty)
 template <int CM, typename C>
 __device__ __forceinline__ void apply_messages(const C* __restrict__ T, C* W, const C* sM, int d, int chi, size_t NT,
                                                int k0, int k1, int skip) {
-    for (size_t i = threadIdx.x; i < NT; i += blockDim.x) W[i] = T[i];
-    __syncthreads();
+    bool first = true;
     for (int k = k0; k < k1; ++k) {
         if (k == skip) continue;
-        mode_product_inplace<CM>(W, sM + k * chi * chi, ipow(chi, k), chi, ipow(chi, d - 1 - k));
+        const C* M = sM + k * chi * chi;
+        if (first) mode_product<CM>(T, W, M, M, ipow(chi, k), chi, chi, ipow(chi, d - 1 - k));
+        else mode_product_inplace<CM>(W, M, ipow(chi, k), chi, ipow(chi, d - 1 - k));
+        first = false;
+        __syncthreads();
+    }
+    if (first) {
+        for (size_t i = threadIdx.x; i < NT; i += blockDim.x) W[i] = T[i];
         __syncthreads();
     }
 }
