@@ -470,38 +470,60 @@ def serving_stream(jobs: int, rate: float, seed: int = 0):
 
 
 def run_serve_mode(args) -> None:
-    """p50/p99 job latency and jobs/s of a Poisson job stream through the continuous-batching
-    server, next to the same jobs run one at a time (each job's latency then includes its
-    wait behind the earlier ones)."""
+    """p50/p99 job latency and jobs/s of Poisson job streams (one per rate in --rates) through
+    the continuous-batching server, next to the same jobs run one at a time in arrival order
+    (each job's latency then includes its wait behind the earlier ones).  Both sides start
+    from configs already compiled into contexts, so both time device state set-up, the
+    anneal and the read-out."""
     import torch
     import bqa_gb300
+    from bqa_gb300 import config as cfg
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
     from bqa_gb300.serve import JobServer
-    stream = serving_stream(args.jobs, args.rate, seed=1)
-    # warm-up: compile paths and allocator
-    bqa_gb300.run_qa(dict(stream[0][1]))
-    torch.cuda.synchronize()
-    srv = JobServer()
-    for t, conf in stream:
-        srv.submit(dict(conf), arrival=t)
-    srv._t0 = time.perf_counter()
-    srv.run(timeout=1800)
-    served = srv.stats()
-    # one at a time, same arrivals
-    t0 = time.perf_counter()
-    lat = []
-    clock = 0.0
-    for t, conf in stream:
-        now = time.perf_counter() - t0
-        if now < t:
-            time.sleep(t - now)
-        bqa_gb300.run_qa(dict(conf))
+
+    def run_one(ctx):
+        job = Annealer(ctx)
+        out = []
+        for ins in ctx.instructions:
+            if isinstance(ins, dict):
+                job.run_layer(ins["xtime"], ins["ztime"])
+            elif ins == cfg.MEASURE:
+                out.append(job.measure())
+            else:
+                out.append(job.bloch_vectors())
         torch.cuda.synchronize()
-        lat.append(time.perf_counter() - t0 - t)
-    seq_span = time.perf_counter() - t0 - stream[0][0]
-    print(json.dumps({"mode": "serve", "jobs": args.jobs, "rate_per_s": args.rate, "served": served,
-                      "one_at_a_time": {"p50_s": float(np.percentile(lat, 50)),
-                                        "p99_s": float(np.percentile(lat, 99)),
-                                        "jobs_per_s": args.jobs / seq_span}}))
+        return out
+
+    rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+    results = []
+    for rate in rates:
+        stream = serving_stream(args.jobs, rate, seed=1)
+        bqa_gb300.run_qa(dict(stream[0][1]))              # warm-up: compile paths and allocator
+        torch.cuda.synchronize()
+        srv = JobServer()
+        for t, conf in stream:
+            srv.submit(dict(conf), arrival=t)
+        srv._t0 = time.perf_counter()
+        srv.run(timeout=1800)
+        served = srv.stats()
+        ctxs = [(t, build_context(dict(conf))) for t, conf in stream]
+        t0 = time.perf_counter()
+        lat = []
+        for t, ctx in ctxs:
+            now = time.perf_counter() - t0
+            if now < t:
+                time.sleep(t - now)
+            run_one(ctx)
+            lat.append(time.perf_counter() - t0 - t)
+        seq_span = time.perf_counter() - t0 - ctxs[0][0]
+        results.append({"rate_per_s": rate, "served": served,
+                        "one_at_a_time": {"p50_s": float(np.percentile(lat, 50)),
+                                          "p99_s": float(np.percentile(lat, 99)),
+                                          "jobs_per_s": args.jobs / seq_span}})
+    print(json.dumps({"mode": "serve", "jobs": args.jobs,
+                      "stream": "random d-regular, d in {3,4}, n log-uniform in [100, 20000], chi in {4, 8}, "
+                                "20 or 50 steps", "rates": results}))
 
 
 def run_layout_mode(args) -> None:
@@ -649,6 +671,7 @@ def main() -> None:
     ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout", "small", "mixed"])
     ap.add_argument("--jobs", type=int, default=32)
     ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--rates", default="", help="serve mode: comma-separated arrival rates (jobs/s)")
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     args = ap.parse_args()
     logging.basicConfig(level=logging.ERROR)

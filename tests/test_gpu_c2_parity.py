@@ -1,0 +1,44 @@
+"""Parity at the headline shape: a 10,000-node instance of the 100k-qubit workload's generator
+(random 3-regular, J = +-1, h ~ U(-0.5, 0.5), chi 16), first 66 steps of the 200-step schedule
+(past bond-dim saturation), against the REFERENCE run at FP64 (fixture written by
+tests/golden/make_golden_c2.py).  complex128 to round-off; complex64 within the complex64 bar
+(the pinv_eps threshold moves ~1e-3 of amplitude under complex64 rounding)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+import bqa_gb300  # noqa: E402
+from tests.golden.make_golden_c2 import config_from_fixture  # noqa: E402
+
+FIXTURE = Path(__file__).resolve().parent / "golden" / "c2_rr3_n10k_chi16.npz"
+
+
+@pytest.fixture(scope="module")
+def case():
+    if not FIXTURE.exists():
+        pytest.skip("fixture not generated")
+    return config_from_fixture(FIXTURE), np.load(FIXTURE)["bloch"]
+
+
+def _bloch(conf, precision, monkeypatch):
+    monkeypatch.setenv("BQA_PRECISION", precision)
+    out = bqa_gb300.run_qa(dict(conf), as_arrays=True)
+    return out[0][1]
+
+
+def test_complex128_matches_reference(case, monkeypatch):
+    conf, want = case
+    got = _bloch(conf, "double", monkeypatch)
+    assert got.shape == want.shape
+    assert np.abs(got - want).max() < 1e-8
+
+
+def test_complex64_within_bar(case, monkeypatch):
+    conf, want = case
+    got = _bloch(conf, "single", monkeypatch)
+    err = np.abs(got - want).max()
+    assert err < 5e-3, err
