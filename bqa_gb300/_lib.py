@@ -9,7 +9,7 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 6
+ABI_VERSION = 7
 BQA_C64 = 0
 BQA_C128 = 1
 
@@ -35,6 +35,26 @@ class BqaClass(ctypes.Structure):
         ("scratch", c_void_p),
         ("scratch_elems", c_int64),
     ]
+
+
+class BqaJob(ctypes.Structure):
+    """Mirror of ``struct bqa_job``."""
+    _fields_ = [
+        ("dtype", c_int32), ("n_classes", c_int32), ("classes", POINTER(BqaClass)),
+        ("edges", c_int32), ("max_bond_dim", c_int32), ("max_bp_iters", c_int32), ("bp_check_every", c_int32),
+        ("pad_bonds", c_int32), ("split_sweeps", c_int32), ("colmax_elems", c_int32),
+        ("chi", c_int32), ("chis", c_int32), ("lam_stride", c_int32), ("mcur", c_int32), ("tcur", c_int32),
+        ("bp_eps", c_double), ("pinv_eps", c_double), ("damping", c_double),
+        ("msgs", c_void_p * 2), ("ext", c_void_p), ("lu", c_void_p), ("ul", c_void_p), ("lmbds", c_void_p),
+        ("colmax", c_void_p), ("dist_parts", c_void_p), ("loop_state", c_void_p), ("status", c_void_p),
+        ("edge_j", c_void_p),
+    ]
+
+
+class BqaLayerInfo(ctypes.Structure):
+    """Mirror of ``struct bqa_layer_info``."""
+    _fields_ = [("bond_dim", c_int32), ("sweeps", c_int32), ("bp_exhausted", c_int32),
+                ("svd_not_converged", c_int32), ("trunc_err", c_double), ("best_dist", c_double)]
 
 
 # name -> (restype, argtypes); every exported symbol of the header
@@ -68,6 +88,7 @@ SIGNATURES = {
     "bqa_canonicalize_noalloc": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_void_p]),
     "bqa_fp32_fma_probe": (c_int32, [c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_run_layer": (c_int32, [POINTER(BqaJob), c_double, c_double, POINTER(BqaLayerInfo), c_void_p]),
     "bqa_layout_degrees": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
                                      c_void_p, c_void_p, c_void_p, c_void_p]),
     "bqa_layout_class": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_void_p,

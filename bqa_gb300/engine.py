@@ -24,6 +24,8 @@ PyTorch only allocates device memory and supplies the stream; all arithmetic run
 """
 from __future__ import annotations
 
+import ctypes
+
 import logging
 from dataclasses import dataclass
 
@@ -71,7 +73,7 @@ class Annealer:
     """One annealing job resident on one GPU."""
 
     def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4,
-                 pad_bonds: bool | None = None):
+                 pad_bonds: bool | None = None, native: bool = True):
         import torch
         self.torch = torch
         if not torch.cuda.is_available():
@@ -83,6 +85,9 @@ class Annealer:
         real = torch.float32 if self.precision == "single" else torch.float64
         self.real_np = np.float32 if self.precision == "single" else np.float64
         self.ctx = ctx
+        # steps through bqa_run_layer (one library call per step, no interpreter lock held);
+        # per-kernel timing runs the same launches from Python
+        self.native = bool(native)
         self.device = torch.device(device if device is not None else "cuda")
         self.bp_check_every = max(1, int(bp_check_every))
         E = ctx.edges_number
@@ -346,9 +351,46 @@ class Annealer:
 
     def run_layer(self, xtime: float, ztime: float) -> dict:
         """One annealing step (src/bqa/state.py:315-321)."""
+        if self.native and self._events is None:
+            return self._run_layer_native(float(xtime), float(ztime))
         dim, err = self.gate_layer(xtime, ztime)
         sweeps = self.run_bp()
         info = {"bond_dim": dim, "trunc_err": err, "sweeps": sweeps}
+        self.stats.append(info)
+        return info
+
+    def _job_struct(self):
+        ctx = self.ctx
+        cls = self._class_array(out=True)          # tensor = current buffer, tensor_out = the other
+        j = _lib.BqaJob()
+        j.dtype, j.n_classes = self.dtype, len(self.classes)
+        j.classes = ctypes.cast(cls, ctypes.POINTER(_lib.BqaClass))
+        j.edges, j.max_bond_dim = self.E, int(ctx.max_bond_dim)
+        j.max_bp_iters, j.bp_check_every = int(ctx.max_bp_iters_number), self.bp_check_every
+        j.pad_bonds, j.split_sweeps = int(self.pad_bonds), int(self.split_sweeps)
+        j.colmax_elems = int(self.colmax.numel())
+        j.chi, j.chis, j.lam_stride, j.mcur, j.tcur = self.chi, self.chis, self.lam_stride, self.mcur, self.tcur
+        j.bp_eps, j.pinv_eps, j.damping = float(ctx.bp_eps), float(ctx.pinv_eps), float(ctx.damping)
+        j.msgs[0], j.msgs[1] = _ptr(self.msgs[0]), _ptr(self.msgs[1])
+        j.ext, j.lu, j.ul, j.lmbds = _ptr(self.ext), _ptr(self.lu), _ptr(self.ul), _ptr(self.lmbds)
+        j.colmax, j.dist_parts = _ptr(self.colmax), _ptr(self.dist_parts)
+        j.loop_state, j.status, j.edge_j = _ptr(self.loop_state), _ptr(self.status), _ptr(self.edge_j)
+        return j, cls
+
+    def _run_layer_native(self, xtime: float, ztime: float) -> dict:
+        if self.ctx.max_bp_iters_number < 1:
+            raise ValueError("max_bp_iter_number must be >= 1 to run belief propagation")
+        j, cls = self._job_struct()
+        res = _lib.BqaLayerInfo()
+        self.lib.call("bqa_run_layer", ctypes.byref(j), xtime, ztime, ctypes.byref(res), self.stream)
+        self.chi, self.chis, self.lam_stride, self.mcur, self.tcur = j.chi, j.chis, j.lam_stride, j.mcur, j.tcur
+        if res.svd_not_converged:
+            log.warning("a Jacobi SVD of the truncation step hit its sweep cap")
+        log.info(f"Truncation performed, per edge error upper bound: {res.trunc_err}")
+        if res.bp_exhausted:
+            log.warning(f"BP algorithm exceeds iterations limit set to {self.ctx.max_bp_iters_number}, "
+                        f"obtained bp_eps {res.best_dist}")
+        info = {"bond_dim": int(res.bond_dim), "trunc_err": float(res.trunc_err), "sweeps": int(res.sweeps)}
         self.stats.append(info)
         return info
 

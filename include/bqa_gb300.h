@@ -69,6 +69,55 @@ typedef struct bqa_class {
     int64_t scratch_elems;     /* its size in complex elements; see bqa_node_scratch_elems */
 } bqa_class;
 
+/* One annealing job's device state and parameters, for bqa_run_layer.  Buffers as for the
+ * entry points below; the fields marked "state" are read and updated by each step. */
+typedef struct bqa_job {
+    int32_t dtype;             /* BQA_C64 / BQA_C128 */
+    int32_t n_classes;
+    bqa_class* classes;        /* tensor = current buffer, tensor_out = the other (swapped by a step) */
+    int32_t edges;             /* E directed edges */
+    int32_t max_bond_dim;
+    int32_t max_bp_iters;      /* reference max_bp_iter_number (>= 1) */
+    int32_t bp_check_every;    /* BP sweeps launched between host reads of the loop state */
+    int32_t pad_bonds;         /* bond dims > 4 stored rounded up to a multiple of 4 */
+    int32_t split_sweeps;      /* BP sweeps and extended messages in two stages (pm in lu) */
+    int32_t colmax_elems;      /* entries of colmax (>= 2 chi) */
+    int32_t chi, chis;         /* state: logical and storage bond dim */
+    int32_t lam_stride;        /* state: row stride of lmbds */
+    int32_t mcur, tcur;        /* state: current message buffer, tensor ping-pong parity */
+    double bp_eps, pinv_eps, damping;
+    void* msgs[2];             /* [E][chis][chis] each */
+    void* ext;                 /* [E][2chi][2chi]: extended messages, then canonicalisers */
+    void* lu;                  /* [E][2chi][2chi]; also the blocks of the two-stage passes */
+    void* ul;                  /* [E][2chi][2chi] */
+    void* lmbds;               /* [E/2][2chi] real */
+    void* colmax;              /* [colmax_elems] real bit patterns */
+    void* dist_parts;          /* 2 x int64 */
+    int32_t* loop_state;       /* 8 x int32 */
+    int32_t* status;           /* 1 x int32 */
+    const double* edge_j;      /* [E/2] couplings (two-stage extended messages) */
+} bqa_job;
+
+/* What one step did. */
+typedef struct bqa_layer_info {
+    int32_t bond_dim;          /* bond dim after the truncation */
+    int32_t sweeps;            /* BP sweeps run */
+    int32_t bp_exhausted;      /* the BP loop hit max_bp_iters */
+    int32_t svd_not_converged; /* a Jacobi SVD hit its sweep cap (status word reset) */
+    double trunc_err;          /* per-edge truncation error bound */
+    double best_dist;          /* last BP distance when exhausted */
+} bqa_layer_info;
+
+/*
+ * One annealing step (src/bqa/state.py:315-321): the gate layer with BP-gauged truncation
+ * (bqa_ext_msgs[_split], bqa_env_factor, bqa_bond_canon, the global truncation decision,
+ * bqa_lmbds_truncate, bqa_apply_update, bqa_msgs_from_lmbds) and loopy BP to tolerance
+ * (bqa_bp_sweep[_split] + bqa_bp_finalize in groups, the loop state read every
+ * bp_check_every sweeps), the same launches and decisions a host would make calling those
+ * entry points.  Blocks the calling thread at the two reads of a step.
+ */
+int32_t bqa_run_layer(bqa_job* job, double xtime, double ztime, bqa_layer_info* info, void* stream);
+
 /* ABI version of this header (bumped on any signature change). */
 int32_t bqa_abi_version(void);
 

@@ -150,3 +150,23 @@ def test_snapshot_restore_replays_identically():
     for ins in steps[3:6]:
         job.run_layer(ins["xtime"], ins["ztime"])
     assert np.array_equal(job.bloch_vectors(), first)
+
+
+@pytest.mark.parametrize("name,precision", [("rr3_n16_chi4", "single"), ("grid3x4_chi4_damped", "single"),
+                                            ("mixed_n18_chi3", "double"), ("tree9", "single")])
+def test_native_step_equals_python_step(name, precision):
+    """bqa_run_layer issues the same launches and decisions as the Python step: identical state."""
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
+    ctx = build_context(gc.config(name))
+    steps = [i for i in ctx.instructions if isinstance(i, dict)][:8]
+    jobs = [Annealer(ctx, precision=precision, native=nat) for nat in (True, False)]
+    for job in jobs:
+        for ins in steps:
+            job.run_layer(ins["xtime"], ins["ztime"])
+    (t1, m1, l1), (t2, m2, l2) = (j.get_state() for j in jobs)
+    assert jobs[0].stats == jobs[1].stats
+    assert np.array_equal(m1, m2) and np.array_equal(l1, l2)
+    for d in t1:
+        assert np.array_equal(t1[d], t2[d])
+    assert np.array_equal(jobs[0].bloch_vectors(), jobs[1].bloch_vectors())
