@@ -43,7 +43,7 @@ static int cuda_rc(cudaError_t e, const char* what) {
 }
 
 static int store_dim(const bqa_job* j, int chi) {
-    return (j->pad_bonds && chi > 4 && chi % 4) ? chi + 4 - chi % 4 : chi;
+    return (j->pad_bonds && chi > 4 && chi <= 16 && chi % 4) ? chi + 4 - chi % 4 : chi;
 }
 
 static int gate_layer(bqa_job* j, double xtime, double ztime, bqa_layer_info* info, cudaStream_t st) {

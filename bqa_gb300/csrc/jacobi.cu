@@ -312,6 +312,236 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
     }
 }
 
+// ---- matrices of size 33..64 (bond dims 17..32): columns in shared memory ----------------------
+//
+// One warp per matrix.  A and V are kept column-major in shared memory at an odd stride
+// (NS = 65 complex elements), so the 32 lanes reading one row of 32 different columns fall in
+// distinct 8-byte bank slots two by two.  The xor round-robin ordering is the same (round r
+// pairs j with j ^ r, r = 1..63); lane k takes the k-th pair of the round, forms its Gram
+// entries, decides and applies the rotation to both columns of A and V, and updates the two
+// cached column norms.  Pairs of a round are disjoint, so lanes never touch the same column.
+// Decisions, rotation formula, relative test and stopping rule are those of jacobi_columns.
+constexpr int kWide = 64;
+constexpr int kWideNS = 65;
+
+template <typename R>
+__device__ __forceinline__ bool jacobi_wide(typename Cx<R>::T* A, typename Cx<R>::T* V, R* nrm, int lane) {
+    using C = typename Cx<R>::T;
+    constexpr int W = kWide, NS = kWideNS;
+    for (int j = lane; j < W; j += 32) {
+        C* v = V + j * NS;
+        for (int i = 0; i < W; ++i) v[i] = c_make(i == j ? R(1) : R(0), R(0));
+        const C* a = A + j * NS;
+        R p[NP] = {};
+        for (int i = 0; i < W; ++i) p[i % NP] = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, p[i % NP]));
+        nrm[j] = sum_parts<NP>(p);
+    }
+    __syncwarp();
+    R fro2 = nrm[lane] + nrm[lane + 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fro2 += __shfl_xor_sync(BQA_FULL_MASK, fro2, o);
+    const R tol = (R)W * jacobi_eps<R>();
+    const R col_floor = fmax((R)W * jacobi_eps<R>() * jacobi_eps<R>() * fro2, sizeof(R) == 4 ? R(1e-30) : R(1e-280));
+    for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
+        int rotated = 0;
+        for (int r = 1; r < W; ++r) {
+            const int h = 31 - __clz(r);
+            const int pc = ((lane >> h) << (h + 1)) | (lane & ((1 << h) - 1));   // bit h clear
+            const int qc = pc ^ r;
+            C* ap = A + pc * NS;
+            C* aq = A + qc * NS;
+            const R alpha = nrm[pc], beta = nrm[qc];
+            R sx[NP] = {}, sy[NP] = {};
+            for (int i = 0; i < W; ++i) {
+                const C x = ap[i], y = aq[i];
+                sx[i % NP] = fma(x.x, y.x, fma(x.y, y.y, sx[i % NP]));
+                sy[i % NP] = fma(x.x, y.y, fma(-x.y, y.x, sy[i % NP]));
+            }
+            const C g = c_make(sum_parts<NP>(sx), sum_parts<NP>(sy));
+            const R gabs = sqrt(c_abs2(g));
+            const bool rot = alpha > R(0) && beta > R(0) && gabs > tol * sqrt(alpha) * sqrt(beta);
+            if (rot) {
+                const R zeta = (beta - alpha) / (R(2) * gabs);
+                const R t = copysign(R(1), zeta) / (fabs(zeta) + hypot(R(1), zeta));
+                const R c = R(1) / sqrt(fma(t, t, R(1)));
+                const R sn = c * t;
+                const R ex = g.x / gabs, ey = g.y / gabs;
+                const C wp = c_make(-sn * ex, sn * ey), wq = c_make(sn * ex, sn * ey);
+                R np_[NP] = {}, nq_[NP] = {};
+                for (int i = 0; i < W; ++i) {
+                    const C x = ap[i], y = aq[i];
+                    const C nx = c_fma(wp, y, c_scale(x, c)), ny = c_fma(wq, x, c_scale(y, c));
+                    ap[i] = nx;
+                    aq[i] = ny;
+                    np_[i % NP] = fma(nx.x, nx.x, fma(nx.y, nx.y, np_[i % NP]));
+                    nq_[i % NP] = fma(ny.x, ny.x, fma(ny.y, ny.y, nq_[i % NP]));
+                }
+                nrm[pc] = sum_parts<NP>(np_);
+                nrm[qc] = sum_parts<NP>(nq_);
+                C* vp = V + pc * NS;
+                C* vq = V + qc * NS;
+                for (int i = 0; i < W; ++i) {
+                    const C x = vp[i], y = vq[i];
+                    vp[i] = c_fma(wp, y, c_scale(x, c));
+                    vq[i] = c_fma(wq, x, c_scale(y, c));
+                }
+                rotated |= (alpha > col_floor && beta > col_floor);
+            }
+            __syncwarp();
+        }
+        if (!__any_sync(BQA_FULL_MASK, rotated)) return true;
+    }
+    return false;
+}
+
+template <typename R>
+__host__ __device__ constexpr size_t wide_smem_elems() { return 2 * (size_t)kWide * kWideNS + kWide; }
+
+// bqa_env_factor for 32 < n <= 64: one warp per matrix (mirrors env_factor_kernel)
+template <typename R>
+__global__ void __launch_bounds__(32) env_factor_wide_kernel(const typename Cx<R>::T* __restrict__ mats, int count,
+                                                             int n, R eps, typename Cx<R>::T* __restrict__ lu,
+                                                             typename Cx<R>::T* __restrict__ ul, int32_t* status) {
+    using C = typename Cx<R>::T;
+    constexpr int NS = kWideNS;
+    extern __shared__ double4 smem_raw[];
+    C* A = reinterpret_cast<C*>(smem_raw);
+    C* V = A + kWide * NS;
+    R* nrm = reinterpret_cast<R*>(V + kWide * NS);
+    const int lane = threadIdx.x;
+    const int mat = blockIdx.x;
+    const size_t base = (size_t)mat * n * n;
+    // column j of A = column j of m (zero-padded to 64)
+    for (int e = lane; e < kWide * kWide; e += 32) {
+        const int j = e / kWide, i = e - j * kWide;
+        A[j * NS + i] = (i < n && j < n) ? mats[base + (size_t)i * n + j] : c_zero<C>();
+    }
+    __syncwarp();
+    const bool ok = jacobi_wide<R>(A, V, nrm, lane);
+    if (!ok && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
+    // sigma_j = |a_j|; nrm[j] <- sqrt(sigma_j) if kept, else 0
+    for (int j = lane; j < kWide; j += 32) {
+        const C* a = A + j * NS;
+        R s2 = 0;
+        for (int i = 0; i < kWide; ++i) s2 += c_abs2(a[i]);
+        const R sig = sqrt(s2);
+        nrm[j] = sig > eps ? sqrt(sig) : R(0);
+    }
+    __syncwarp();
+    // lu[j][k] = sqrt(sigma_j) conj(V[k][j]), ul[k][j] = V[k][j] / sqrt(sigma_j)
+    for (int e = lane; e < n * n; e += 32) {
+        const int j = e / n, k = e - j * n;
+        const R sq = nrm[j];
+        const C vkj = V[j * NS + k];
+        lu[base + (size_t)j * n + k] = c_make(sq * vkj.x, -sq * vkj.y);
+    }
+    for (int e = lane; e < n * n; e += 32) {
+        const int k = e / n, j = e - k * n;
+        const R inv = nrm[j] > R(0) ? R(1) / nrm[j] : R(0);
+        ul[base + (size_t)k * n + j] = c_scale(V[j * NS + k], inv);
+    }
+}
+
+// bqa_bond_canon for 32 < n <= 64: one warp per undirected edge (mirrors bond_canon_kernel)
+template <typename R>
+__global__ void __launch_bounds__(32) bond_canon_wide_kernel(const typename Cx<R>::T* __restrict__ lu,
+                                                             const typename Cx<R>::T* __restrict__ ul, int edges, int n,
+                                                             R eps, typename Cx<R>::T* __restrict__ canon,
+                                                             R* __restrict__ lmbds, typename Cx<R>::Bits* colmax,
+                                                             int32_t* status) {
+    using C = typename Cx<R>::T;
+    constexpr int NS = kWideNS;
+    extern __shared__ double4 smem_raw[];
+    C* A = reinterpret_cast<C*>(smem_raw);
+    C* V = A + kWide * NS;
+    R* nrm = reinterpret_cast<R*>(V + kWide * NS);
+    __shared__ R s_sig[kWide];
+    __shared__ int s_rank[kWide];
+    const int lane = threadIdx.x;
+    const int half = edges / 2;
+    const int pf = blockIdx.x, pb = pf + half;
+    const size_t nn = (size_t)n * n;
+    const C* luf = lu + (size_t)pf * nn;
+    const C* lub = lu + (size_t)pb * nn;
+    // ker[i][j] = sum_k lu_f[i][k] lu_b[j][k]; column j of A = column j of ker
+    for (int e = lane; e < kWide * kWide; e += 32) {
+        const int j = e / kWide, i = e - j * kWide;
+        C acc = c_zero<C>();
+        if (i < n && j < n)
+            for (int k = 0; k < n; ++k) acc = c_fma(luf[(size_t)i * n + k], lub[(size_t)j * n + k], acc);
+        A[j * NS + i] = acc;
+    }
+    __syncwarp();
+    const bool ok = jacobi_wide<R>(A, V, nrm, lane);
+    if (!ok && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
+    for (int j = lane; j < kWide; j += 32) {
+        const C* a = A + j * NS;
+        R s2 = 0;
+        for (int i = 0; i < kWide; ++i) s2 += c_abs2(a[i]);
+        const R sig = sqrt(s2);
+        s_sig[j] = (j < n && sig > eps) ? sig : R(0);
+        nrm[j] = s_sig[j] > R(0) ? R(1) / sig : R(0);      // 1 / sigma_j of the kept columns
+    }
+    __syncwarp();
+    R ss = 0;
+    for (int j = lane; j < kWide; j += 32) ss += s_sig[j] * s_sig[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(BQA_FULL_MASK, ss, o);
+    const R norm = sqrt(ss);
+    for (int j = lane; j < kWide; j += 32) {
+        const R sk = s_sig[j];
+        int rank = 0;
+        for (int k = 0; k < kWide; ++k) rank += (s_sig[k] > sk) || (s_sig[k] == sk && k < j);
+        s_rank[j] = rank;
+        if (j < n) {
+            lmbds[(size_t)pf * n + rank] = norm > R(0) ? sk / norm : R(0);
+            if (norm > R(0)) atomic_max_nonneg(colmax + rank, sk / norm);
+        }
+    }
+    __syncwarp();
+    // canon[pb][i][rank_j] = ul_f[i] . a_j / sigma_j ; canon[pf][i][rank_j] = ul_b[i] . conj(v_j)
+    const C* ulf = ul + (size_t)pf * nn;
+    const C* ulb = ul + (size_t)pb * nn;
+    for (int e = lane; e < n * n; e += 32) {
+        const int i = e / n, j = e - i * n;
+        const R sk = s_sig[j];
+        const C* a = A + j * NS;
+        const C* v = V + j * NS;
+        C acc = c_zero<C>(), accv = c_zero<C>();
+        for (int k = 0; k < n; ++k) {
+            acc = c_fma(ulf[(size_t)i * n + k], a[k], acc);
+            accv = c_fma(ulb[(size_t)i * n + k], c_conj(v[k]), accv);
+        }
+        canon[(size_t)pb * nn + (size_t)i * n + s_rank[j]] = c_scale(acc, nrm[j]);
+        canon[(size_t)pf * nn + (size_t)i * n + s_rank[j]] = c_scale(accv, sk > R(0) ? R(1) : R(0));
+    }
+}
+
+template <typename R>
+static int launch_env_wide(const void* m, int count, int n, double eps, void* lu, void* ul, int32_t* status,
+                           cudaStream_t st) {
+    using C = typename Cx<R>::T;
+    const size_t smem = wide_smem_elems<R>() * sizeof(C);
+    int rc = ensure_smem((const void*)env_factor_wide_kernel<R>, smem, "env_factor (64)");
+    if (rc) return rc;
+    env_factor_wide_kernel<R><<<count, 32, smem, st>>>(static_cast<const C*>(m), count, n, (R)eps, static_cast<C*>(lu),
+                                                        static_cast<C*>(ul), status);
+    return check_launch("env_factor (64)");
+}
+
+template <typename R>
+static int launch_canon_wide(const void* lu, const void* ul, int edges, int n, double eps, void* canon, void* lmbds,
+                             void* colmax, int32_t* status, cudaStream_t st) {
+    using C = typename Cx<R>::T;
+    const size_t smem = wide_smem_elems<R>() * sizeof(C);
+    int rc = ensure_smem((const void*)bond_canon_wide_kernel<R>, smem, "bond_canon (64)");
+    if (rc) return rc;
+    bond_canon_wide_kernel<R><<<edges / 2, 32, smem, st>>>(static_cast<const C*>(lu), static_cast<const C*>(ul), edges,
+                                                            n, (R)eps, static_cast<C*>(canon), static_cast<R*>(lmbds),
+                                                            static_cast<typename Cx<R>::Bits*>(colmax), status);
+    return check_launch("bond_canon (64)");
+}
+
 template <int W, typename R>
 static int launch_env(const void* m, int count, int n, double eps, void* lu, void* ul, int32_t* status, cudaStream_t st) {
     using C = typename Cx<R>::T;
@@ -347,7 +577,8 @@ static int env_dispatch(const void* m, int count, int n, double eps, void* lu, v
     if (n <= 8) return launch_env<8, R>(m, count, n, eps, lu, ul, status, st);
     if (n <= 16) return launch_env<16, R>(m, count, n, eps, lu, ul, status, st);
     if (n <= 32) return launch_env<32, R>(m, count, n, eps, lu, ul, status, st);
-    return set_error(BQA_ERR_UNSUPPORTED, "bqa_env_factor: matrix size %d > 32", n);
+    if (n <= kWide) return launch_env_wide<R>(m, count, n, eps, lu, ul, status, st);
+    return set_error(BQA_ERR_UNSUPPORTED, "bqa_env_factor: matrix size %d > %d", n, kWide);
 }
 
 template <typename R>
@@ -356,7 +587,8 @@ static int canon_dispatch(const void* lu, const void* ul, int edges, int n, doub
     if (n <= 8) return launch_canon<8, R>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
     if (n <= 16) return launch_canon<16, R>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
     if (n <= 32) return launch_canon<32, R>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
-    return set_error(BQA_ERR_UNSUPPORTED, "bqa_bond_canon: matrix size %d > 32", n);
+    if (n <= kWide) return launch_canon_wide<R>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    return set_error(BQA_ERR_UNSUPPORTED, "bqa_bond_canon: matrix size %d > %d", n, kWide);
 }
 
 }  // namespace bqa

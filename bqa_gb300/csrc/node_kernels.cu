@@ -482,7 +482,8 @@ static int launch_node_global(const NodeArgs<R>& args, int count, void* scratch,
     if (chi <= 4) kern = node_kernel_global<4, MODE, R>;
     else if (chi <= 8) kern = node_kernel_global<8, MODE, R>;
     else if (chi <= 16) kern = node_kernel_global<16, MODE, R>;
-    else return set_error(BQA_ERR_UNSUPPORTED, "node kernel: bond dim %d > 16", chi);
+    else if (chi <= 32) kern = node_kernel_global<32, MODE, R>;
+    else return set_error(BQA_ERR_UNSUPPORTED, "node kernel: bond dim %d > 32", chi);
     int rc = ensure_smem((const void*)kern, smem, "node kernel (global)");
     if (rc) return rc;
     kern<<<(int)ctas, threads, smem, st>>>(args, count, static_cast<C*>(scratch));
@@ -842,7 +843,8 @@ static int launch_node_mode(const NodeArgs<R>& args, int count, cudaStream_t st)
     else if (chi <= 4) kern = node_kernel<4, MODE, R>;
     else if (chi <= 8) kern = node_kernel<8, MODE, R>;
     else if (chi <= 16) kern = node_kernel<16, MODE, R>;
-    else return set_error(BQA_ERR_UNSUPPORTED, "node kernel: bond dim %d > 16", chi);
+    else if (chi <= 32) kern = node_kernel<32, MODE, R>;
+    else return set_error(BQA_ERR_UNSUPPORTED, "node kernel: bond dim %d > 32", chi);
     int rc = ensure_smem((const void*)kern, smem, "node kernel");
     if (rc) return rc;
     kern<<<count, threads, smem, st>>>(args);
@@ -1015,9 +1017,10 @@ int32_t bqa_max_bond_dim(int32_t degree, int32_t dtype) {
     if (degree < 0 || (dtype != BQA_C64 && dtype != BQA_C128)) return 0;
     const size_t el = dtype == BQA_C64 ? 8 : 16;
     int best = 0;
-    // message kernels stage a node in shared memory; the simple update's Jacobi SVDs are
-    // 2chi x 2chi with 2chi <= 32
-    for (int chi = 1; chi <= 16; ++chi)
+    // the largest bond dim whose node tensors the message kernels hold in shared memory
+    // (beyond it they run on caller scratch, see bqa_node_scratch_elems; the simple update's
+    // Jacobi SVDs take 2chi <= 64)
+    for (int chi = 1; chi <= 32; ++chi)
         if (node_smem_elems(degree, chi) * el <= kMaxSmem) best = chi;
     return best;
 }

@@ -327,7 +327,8 @@ static int apply_classes(const bqa_class* classes, int n_classes, int chi, int d
             if (chi <= 4) gk = apply_kernel_global<4, R>;
             else if (chi <= 8) gk = apply_kernel_global<8, R>;
             else if (chi <= 16) gk = apply_kernel_global<16, R>;
-            else return set_error(BQA_ERR_UNSUPPORTED, "apply: bond dim %d > 16", chi);
+            else if (chi <= 32) gk = apply_kernel_global<32, R>;
+            else return set_error(BQA_ERR_UNSUPPORTED, "apply: bond dim %d > 32", chi);
             int rc = ensure_smem((const void*)gk, gsmem, "apply (global)");
             if (rc) return rc;
             gk<<<(int)ctas, 256, gsmem, st>>>(a, k.count, static_cast<C*>(k.scratch));
@@ -351,7 +352,8 @@ static int apply_classes(const bqa_class* classes, int n_classes, int chi, int d
         else if (chi <= 4) kern = apply_kernel<4, R>;
         else if (chi <= 8) kern = apply_kernel<8, R>;
         else if (chi <= 16) kern = apply_kernel<16, R>;
-        else return set_error(BQA_ERR_UNSUPPORTED, "apply: bond dim %d > 16", chi);
+        else if (chi <= 32) kern = apply_kernel<32, R>;
+        else return set_error(BQA_ERR_UNSUPPORTED, "apply: bond dim %d > 32", chi);
         int rc = ensure_smem((const void*)kern, smem, "apply");
         if (rc) return rc;
         kern<<<k.count, threads, smem, st>>>(a);

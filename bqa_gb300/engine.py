@@ -93,9 +93,9 @@ class Annealer:
         E = ctx.edges_number
         self.E = E
         self.half = E // 2
-        # Storage bond dim: a bond dim above 4 that is not a multiple of 4 is stored zero-padded
+        # Storage bond dim: a bond dim in 5..15 that is not a multiple of 4 is stored zero-padded
         # to the next multiple of 4, so the register-tiled complex64 message kernels (built for
-        # degrees 2-4 and chi % 4 == 0) serve every step.  Padding is exact: padded rows and
+        # degrees 2-4 and chi in {4, 8, 12, 16}) serve every step.  Padding is exact: padded rows and
         # columns of tensors and messages stay zero, their singular values are 0 (masked and
         # sorted last, never counted by the truncation rank), and the truncation zeroes the
         # spectrum columns it drops.
@@ -105,9 +105,9 @@ class Annealer:
         # BP sweeps in two stages (half-node message kernels + combine) on the complex64 path
         self.split_sweeps = self.precision == "single"
         chimax = self._store(ctx.max_bond_dim)
-        if chimax > 16:
+        if chimax > 32:
             raise NotImplementedError(
-                f"max_bond_dim={chimax}: the truncation's Jacobi SVDs take 2*chi <= 32 (chi <= 16)")
+                f"max_bond_dim={chimax}: the truncation's Jacobi SVDs take 2*chi <= 64 (chi <= 32)")
         dev = self.device
         # classes whose node tensors exceed shared memory run on up to 8 CTAs per SM with work
         # tensors in this scratch (one buffer, shared: classes run one after another on the stream)
@@ -196,7 +196,7 @@ class Annealer:
     # ---- helpers -------------------------------------------------------------------------
     def _store(self, chi: int) -> int:
         """Storage bond dim of logical bond dim ``chi``."""
-        if self.pad_bonds and chi > 4 and chi % 4:
+        if self.pad_bonds and 4 < chi <= 16 and chi % 4:
             return chi + 4 - chi % 4
         return chi
 

@@ -36,7 +36,7 @@ def job_footprint(ctx: Context, precision: str | None = None) -> int:
     rs = es // 2
     pad = p == "single" and all(d <= 4 for d in ctx.degree_to_layout)
     chi = ctx.max_bond_dim
-    if pad and chi > 4 and chi % 4:
+    if pad and 4 < chi <= 16 and chi % 4:
         chi += 4 - chi % 4
     E, half, n = ctx.edges_number, ctx.edges_number // 2, ctx.nodes_number
     nmax = 2 * chi

@@ -27,7 +27,9 @@ CASES = [("rr3_n16_chi4", 4), ("rr3_n24_chi8", 8), ("mixed_n18_chi3", 3), ("rr4_
          ("rr3_n16_chi4", 16), ("grid3x4_chi4_damped", 5), ("tree9", 2), ("grid3x4_chi4_damped", 8),
          ("rr3_n24_chi8", 12), ("grid3x4_chi4_damped", 4),
          # degree-7 node tensors beyond shared memory: the global-memory kernels
-         ("mixed_n18_chi3", 4)]
+         ("mixed_n18_chi3", 4),
+         # bond dim 32: global-memory kernels and the 64-column Jacobi
+         ("rr3_n16_chi4", 32)]
 RTOL = 2e-5
 
 
@@ -226,7 +228,7 @@ def test_bp_loop_matches_oracle(name, chi):
 
 
 @pytest.mark.parametrize("name,chi", [("rr3_n16_chi4", 4), ("mixed_n18_chi3", 3), ("tree9", 2),
-                                      ("mixed_n18_chi3", 4)])
+                                      ("mixed_n18_chi3", 4), ("rr3_n16_chi4", 20)])
 def test_double_precision_kernels_match_oracle_to_roundoff(name, chi):
     """The complex128 build of the same kernels agrees with the FP64 oracle to ~1e-12."""
     octx, st, job = random_state(name, chi, seed=7, precision="double")
