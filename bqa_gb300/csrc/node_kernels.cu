@@ -279,13 +279,15 @@ __device__ __forceinline__ void mode_product_inplace(C* X, const C* M, int L, in
 // once; rows padded to NP = n rounded up to 4, zero beyond n); thread (s, 4x4 tile of (a, b),
 // K-slice sl) accumulates its tile over the slice (8 shared loads per 16 complex FMAs); the
 // slices meet in `red` (4096 complex elements).
-constexpr int kCloseKC = 64;
 constexpr int kCloseRed = 4096;
+// positions per staged chunk: 64, or 32 above bond dim 16 (keeps complex128 at chi 32 within
+// shared memory)
+__host__ __device__ inline int close_kc(int n) { return n <= 16 ? 64 : 32; }
 
 template <typename C>
 __device__ __forceinline__ void close_global(const C* __restrict__ X, const C* __restrict__ Y, C* __restrict__ P,
                                              C* __restrict__ stage, C* __restrict__ red, int L, int n, int Rr) {
-    constexpr int KC = kCloseKC, KP = KC + 1;
+    const int KC = close_kc(n), KP = KC + 1;
     const int K = L * Rr;
     const int NPd = (n + 3) & ~3;
     const int ntile = NPd / 4;
@@ -357,22 +359,23 @@ __device__ __forceinline__ void close_global(const C* __restrict__ X, const C* _
 
 // shared memory of the global kernel: messages, P, the close's staging and slice partials, the
 // block reductions' scratch (block_sum<8>: 8 x 32 reals fit 128 complex elements)
+// (+ d message pointers); messages themselves are read from global memory (L1/L2)
 __host__ __device__ inline size_t node_global_smem_elems(int d, int chi, int threads) {
     (void)threads;
     const int n2 = chi * chi;
     const int NPd = (chi + 3) & ~3;
-    return (size_t)d * n2 + 2 * (size_t)n2 + 4 * (size_t)NPd * (kCloseKC + 1) + kCloseRed + 128;
+    return 2 * (size_t)n2 + 4 * (size_t)NPd * (close_kc(chi) + 1) + kCloseRed + 128 + (size_t)d;
 }
 
 // T x_k M_k for k in [k0, k1) except `skip`, into W: the first product reads T and writes W,
 // the others run in place (a plain copy when the set is empty)
 template <int CM, typename C>
-__device__ __forceinline__ void apply_messages(const C* __restrict__ T, C* W, const C* sM, int d, int chi, size_t NT,
-                                               int k0, int k1, int skip) {
+__device__ __forceinline__ void apply_messages(const C* __restrict__ T, C* W, const C* const* mp, int d, int chi,
+                                               size_t NT, int k0, int k1, int skip) {
     bool first = true;
     for (int k = k0; k < k1; ++k) {
         if (k == skip) continue;
-        const C* M = sM + k * chi * chi;
+        const C* M = mp[k];
         if (first) mode_product<CM>(T, W, M, M, ipow(chi, k), chi, chi, ipow(chi, d - 1 - k));
         else mode_product_inplace<CM>(W, M, ipow(chi, k), chi, ipow(chi, d - 1 - k));
         first = false;
@@ -397,11 +400,11 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
     const int per_s = ipow(chi, d);
     const size_t NT = 2 * (size_t)per_s;
     const int NPd = (chi + 3) & ~3;
-    C* sM = sm;
-    C* sP = sM + (size_t)d * n2;
+    C* sP = sm;
     C* stage = sP + 2 * n2;
-    C* red = stage + 4 * (size_t)NPd * (kCloseKC + 1);
+    C* red = stage + 4 * (size_t)NPd * (close_kc(chi) + 1);
     R* sRed = reinterpret_cast<R*>(red + kCloseRed);
+    const C** mp = reinterpret_cast<const C**>(red + kCloseRed + 128);   // d message pointers
     C* Wa = scratch + (size_t)blockIdx.x * 2 * NT;
     C* Wb = Wa + NT;
     const int h = d / 2;
@@ -415,15 +418,12 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
     R num2 = 0, den2 = 0;
     for (int node = blockIdx.x; node < count; node += gridDim.x) {
         const C* T = a.tensors + (size_t)node * NT;
-        for (int k = 0; k < d; ++k) {
-            const C* mg = msgs_in + (size_t)a.in_pos[node * d + k] * n2;
-            for (int i = threadIdx.x; i < n2; i += blockDim.x) sM[k * n2 + i] = mg[i];
-        }
+        for (int k = threadIdx.x; k < d; k += blockDim.x) mp[k] = msgs_in + (size_t)a.in_pos[node * d + k] * n2;
         __syncthreads();
         if (MODE == MODE_DENS) {
             // rho[s][s'] = sum (T x_all M)[s, ..] conj(T[s', ..]) = sum (T x_B)[s, ..] conj((T x_A)[s', ..])
-            apply_messages<CM>(T, Wa, sM, d, chi, NT, 0, h, -1);
-            apply_messages<CM>(T, Wb, sM, d, chi, NT, h, d, -1);
+            apply_messages<CM>(T, Wa, mp, d, chi, NT, 0, h, -1);
+            apply_messages<CM>(T, Wb, mp, d, chi, NT, h, d, -1);
             R v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             for (int o = threadIdx.x; o < per_s; o += blockDim.x) {
                 const C x0 = Wb[o], x1 = Wb[per_s + o];
@@ -443,11 +443,11 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
             continue;
         }
         // idx in A: Wb = T x_B once
-        apply_messages<CM>(T, Wb, sM, d, chi, NT, h, d, -1);
+        apply_messages<CM>(T, Wb, mp, d, chi, NT, h, d, -1);
         for (int idx = 0; idx < d; ++idx) {
-            if (idx == h) apply_messages<CM>(T, Wa, sM, d, chi, NT, 0, h, -1);   // Wa = T x_A for idx in B
-            if (idx < h) apply_messages<CM>(T, Wa, sM, d, chi, NT, 0, h, idx);
-            else apply_messages<CM>(T, Wb, sM, d, chi, NT, h, d, idx);
+            if (idx == h) apply_messages<CM>(T, Wa, mp, d, chi, NT, 0, h, -1);   // Wa = T x_A for idx in B
+            if (idx < h) apply_messages<CM>(T, Wa, mp, d, chi, NT, 0, h, idx);
+            else apply_messages<CM>(T, Wb, mp, d, chi, NT, h, d, idx);
             close_global(Wa, Wb, sP, stage, red, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
             __syncthreads();
             write_outputs<MODE, R>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
