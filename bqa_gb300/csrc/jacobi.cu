@@ -394,8 +394,9 @@ __device__ __forceinline__ bool jacobi_wide(typename Cx<R>::T* A, typename Cx<R>
     return false;
 }
 
+// A, V, column norms, and (bond canonicalisation) kept singular values and their ranks
 template <typename R>
-__host__ __device__ constexpr size_t wide_smem_elems() { return 2 * (size_t)kWide * kWideNS + kWide; }
+__host__ __device__ constexpr size_t wide_smem_elems() { return 2 * (size_t)kWide * kWideNS + 3 * kWide; }
 
 // bqa_env_factor for 32 < n <= 64: one warp per matrix (mirrors env_factor_kernel)
 template <typename R>
@@ -455,8 +456,8 @@ __global__ void __launch_bounds__(32) bond_canon_wide_kernel(const typename Cx<R
     C* A = reinterpret_cast<C*>(smem_raw);
     C* V = A + kWide * NS;
     R* nrm = reinterpret_cast<R*>(V + kWide * NS);
-    __shared__ R s_sig[kWide];
-    __shared__ int s_rank[kWide];
+    R* s_sig = reinterpret_cast<R*>(V + kWide * NS + kWide);
+    int* s_rank = reinterpret_cast<int*>(V + kWide * NS + 2 * kWide);
     const int lane = threadIdx.x;
     const int half = edges / 2;
     const int pf = blockIdx.x, pb = pf + half;
