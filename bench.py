@@ -355,7 +355,7 @@ def run_sweep_mode(args) -> None:
     from bqa_gb300 import instances
     from bqa_gb300.engine import Annealer, _ptr
     from bqa_gb300.layout import build_context
-    conf = instances.headline_gpu_job(n=args.n, seed=0, chi=args.chi)
+    conf = instances.headline_gpu_job(n=args.n, seed=0, chi=args.chi, degree=args.degree)
     ctx = build_context(conf)
     job = Annealer(ctx, precision=args.precision)
     chi = args.chi
@@ -390,7 +390,8 @@ def run_sweep_mode(args) -> None:
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in evs]
     mean = float(np.mean(ms))
-    print(json.dumps({"mode": "sweep", "n": args.n, "chi": chi, "precision": args.precision, "sweeps": args.steps,
+    print(json.dumps({"mode": "sweep", "n": args.n, "degree": args.degree, "chi": chi, "precision": args.precision,
+                      "sweeps": args.steps,
                       "ms_per_sweep": mean, "ms_min": float(np.min(ms)),
                       "tflops": flops / (mean / 1000) / 1e12, "algorithmic_gbs": nbytes / (mean / 1000) / 1e9,
                       "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": nbytes,
@@ -409,14 +410,26 @@ def run_svd_mode(args) -> None:
     steps = [i for i in ctx.instructions if isinstance(i, dict)]
     job = Annealer(ctx, precision=args.precision)
     s = 0
-    while job.bond_dim < args.chi and s < len(steps) - 1:
-        job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
-        s += 1
-    chi = job.chis
-    n = 2 * chi
     lib, st, E = job.lib, job.stream, ctx.edges_number
-    lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job._msgs_cur()),
-             _ptr(job.ext), float(steps[s]["ztime"]), st)
+    if args.synthetic:
+        # random Hermitian PSD 2chi x 2chi matrices with a graded spectrum (no anneal)
+        chi = n_chi = args.chi
+        n = 2 * chi
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.randn(E, n, n, dtype=job.ext.dtype, device="cuda", generator=g)
+        x = x * torch.logspace(0, -4, n, device="cuda").to(x.dtype)
+        m = x @ x.conj().transpose(1, 2)
+        m = m / torch.diagonal(m, dim1=1, dim2=2).sum(-1).view(E, 1, 1)
+        job.ext[: E * n * n].copy_(m.reshape(-1))
+        job.chi = job.chis = chi
+    else:
+        while job.bond_dim < args.chi and s < len(steps) - 1:
+            job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
+            s += 1
+        chi = job.chis
+        n = 2 * chi
+        lib.call("bqa_ext_msgs", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job._msgs_cur()),
+                 _ptr(job.ext), float(steps[s]["ztime"]), st)
     ext = job.ext.clone()
     canon = torch.empty_like(job.ext)
     eps = float(ctx.pinv_eps)
@@ -673,6 +686,9 @@ def main() -> None:
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--rates", default="", help="serve mode: comma-separated arrival rates (jobs/s)")
     ap.add_argument("--precision", default="single", choices=["single", "double"])
+    ap.add_argument("--degree", type=int, default=3, help="sweep mode: degree of the random regular graph")
+    ap.add_argument("--synthetic", action="store_true",
+                    help="svd mode: random graded Hermitian PSD matrices instead of an annealed state")
     args = ap.parse_args()
     logging.basicConfig(level=logging.ERROR)
     logging.getLogger("bqa_gb300").setLevel(logging.ERROR)

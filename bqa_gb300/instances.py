@@ -103,11 +103,11 @@ def headline_cpu_job(n: int = 1000, seed: int = 0) -> dict:
 
 
 def headline_gpu_job(n: int = 100_000, seed: int = 0, chi: int = 16, steps: int = 200,
-                     total_time: float = 20.0) -> dict:
+                     total_time: float = 20.0, degree: int = 3) -> dict:
     """Random 3-regular, J in {-1,+1}, h ~ U(-0.5, 0.5), chi 16, 200 steps, T 20, tol 1e-5,
-    <= 50 sweeps (the 100k-qubit FP32 configuration)."""
+    <= 50 sweeps (the 100k-qubit FP32 configuration); `degree` changes the regular degree."""
     rng = np.random.default_rng(seed)
-    e = random_regular_edges(n, 3, seed)
+    e = random_regular_edges(n, degree, seed)
     J = 2.0 * rng.integers(0, 2, size=len(e)) - 1.0
     h = rng.uniform(-0.5, 0.5, size=n)
     return qubo_config(e, J, h, max_bond_dim=chi, bp_eps=1e-5, pinv_eps=1e-6, max_bp_iter_number=50,
