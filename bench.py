@@ -413,7 +413,7 @@ def run_svd_mode(args) -> None:
     lib, st, E = job.lib, job.stream, ctx.edges_number
     if args.synthetic:
         # random Hermitian PSD 2chi x 2chi matrices with a graded spectrum (no anneal)
-        chi = n_chi = args.chi
+        chi = args.chi
         n = 2 * chi
         g = torch.Generator(device="cuda").manual_seed(0)
         x = torch.randn(E, n, n, dtype=job.ext.dtype, device="cuda", generator=g)

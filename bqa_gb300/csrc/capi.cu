@@ -2,6 +2,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <unordered_map>
 
@@ -28,15 +29,19 @@ int check_launch(const char* what) {
 
 int ensure_smem(const void* kernel, size_t bytes, const char* what) {
     static std::mutex mu;
-    static std::unordered_map<const void*, size_t> granted;
+    static std::map<std::pair<int, const void*>, size_t> granted;   // (device, kernel) -> bytes
     if (bytes <= 48 * 1024) return BQA_OK;
     if (bytes > kMaxSmem) return set_error(BQA_ERR_UNSUPPORTED, "%s: needs %zu B of shared memory", what, bytes);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "%s: cudaGetDevice: %s", what, cudaGetErrorString(e));
     std::lock_guard<std::mutex> lock(mu);
-    auto it = granted.find(kernel);
+    const auto key = std::make_pair(dev, kernel);
+    auto it = granted.find(key);
     if (it != granted.end() && it->second >= bytes) return BQA_OK;
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "%s: cudaFuncSetAttribute: %s", what, cudaGetErrorString(e));
-    granted[kernel] = kMaxSmem;
+    granted[key] = kMaxSmem;
     return BQA_OK;
 }
 
