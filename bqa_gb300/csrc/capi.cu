@@ -39,9 +39,17 @@ int ensure_smem(const void* kernel, size_t bytes, const char* what) {
     const auto key = std::make_pair(dev, kernel);
     auto it = granted.find(key);
     if (it != granted.end() && it->second >= bytes) return BQA_OK;
-    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    // the per-block limit covers static and dynamic shared memory together
+    cudaFuncAttributes attr;
+    e = cudaFuncGetAttributes(&attr, kernel);
+    if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "%s: cudaFuncGetAttributes: %s", what, cudaGetErrorString(e));
+    const size_t room = kMaxSmem > attr.sharedSizeBytes ? kMaxSmem - attr.sharedSizeBytes : 0;
+    if (bytes > room)
+        return set_error(BQA_ERR_UNSUPPORTED, "%s: needs %zu B of dynamic shared memory next to %zu B static",
+                         what, bytes, (size_t)attr.sharedSizeBytes);
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room);
     if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "%s: cudaFuncSetAttribute: %s", what, cudaGetErrorString(e));
-    granted[key] = kMaxSmem;
+    granted[key] = room;
     return BQA_OK;
 }
 

@@ -142,6 +142,27 @@ __device__ __forceinline__ HalfZZ<R> half_zz(double c) {
     return out;
 }
 
+// half_zz / sincos computed once per warp (lane 0, double precision) and broadcast: the FP64
+// pipe is narrow, so per-thread evaluation of the same value dominated the kernels that need
+// it.  Every lane of the warp must call these.
+template <typename R>
+__device__ __forceinline__ HalfZZ<R> half_zz_warp(double c) {
+    HalfZZ<R> h;
+    if ((threadIdx.x & 31) == 0) h = half_zz<R>(c);
+    h.a0.x = __shfl_sync(BQA_FULL_MASK, h.a0.x, 0);
+    h.a0.y = __shfl_sync(BQA_FULL_MASK, h.a0.y, 0);
+    h.a1.x = __shfl_sync(BQA_FULL_MASK, h.a1.x, 0);
+    h.a1.y = __shfl_sync(BQA_FULL_MASK, h.a1.y, 0);
+    return h;
+}
+
+__device__ __forceinline__ void sincos_warp(double x, double* s, double* c) {
+    double sv = 0.0, cv = 0.0;
+    if ((threadIdx.x & 31) == 0) sincos(x, &sv, &cv);
+    *s = __shfl_sync(BQA_FULL_MASK, sv, 0);
+    *c = __shfl_sync(BQA_FULL_MASK, cv, 0);
+}
+
 __host__ __device__ __forceinline__ int ipow(int b, int e) {
     int r = 1;
     for (int i = 0; i < e; ++i) r *= b;

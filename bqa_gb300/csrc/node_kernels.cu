@@ -137,7 +137,7 @@ __device__ __forceinline__ void write_outputs(const NodeArgs<R>& a, int node, in
                 den2 = fmax(den2, c_abs2(c_add(m, o)));
             }
         } else {  // MODE_EXT
-            const HalfZZ<R> h = half_zz<R>(a.edge_ampl[node * d + idx] * a.ztime);
+            const HalfZZ<R> h = half_zz_warp<R>(a.edge_ampl[node * d + idx] * a.ztime);
             const R scale = c_abs2(h.a0) + c_abs2(h.a1);
             const C trx = c_scale(tr, scale);
             const int n = 2 * chi;
@@ -766,7 +766,7 @@ __global__ void __launch_bounds__(256) ext_combine_kernel(const typename Cx<R>::
     const C* p1 = p0 + n2;
     C tr = c_zero<C>();
     for (int q = 0; q < chi; ++q) tr = c_add(tr, c_add(p0[q * chi + q], p1[q * chi + q]));
-    const HalfZZ<R> h = half_zz<R>(edge_j[slot % (E / 2)] * ztime);
+    const HalfZZ<R> h = half_zz_warp<R>(edge_j[slot % (E / 2)] * ztime);
     const R scale = c_abs2(h.a0) + c_abs2(h.a1);
     const C trx = c_scale(tr, scale);
     C* og = ext + (size_t)slot * n * n;

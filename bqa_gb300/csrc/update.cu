@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyArgs<R> a) {
     const C* tg = a.t_in + (size_t)node * nin;
     for (int i = threadIdx.x; i < nin; i += blockDim.x) sX[i] = tg[i];
     for (int k = 0; k < d; ++k) {
-        const HalfZZ<R> h = half_zz<R>(a.edge_ampl[node * d + k] * a.ztime);
+        const HalfZZ<R> h = half_zz_warp<R>(a.edge_ampl[node * d + k] * a.ztime);
         const C* Cc = a.canon + (size_t)a.in_pos[node * d + k] * n * n;
         const R* lam = a.lmbds + (size_t)a.lmbd_pos[node * d + k] * a.lam_stride;
         for (int o = threadIdx.x; o < 2 * dim * chi; o += blockDim.x) {
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyArgs<R> a) {
 
     // Rz, Rx, norm
     double sz, cz;
-    sincos(a.node_ampl[node] * a.ztime, &sz, &cz);
+    sincos_warp(a.node_ampl[node] * a.ztime, &sz, &cz);
     const C z0 = c_make((R)cz, (R)-sz), z1 = c_make((R)cz, (R)sz);
     const int per_s = ipow(dim, d);
     R acc[1] = {0};
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int c
         const C* tg = a.t_in + (size_t)node * nin;
         for (int i = threadIdx.x; i < nin; i += blockDim.x) X0[i] = tg[i];
         for (int k = 0; k < d; ++k) {
-            const HalfZZ<R> h = half_zz<R>(a.edge_ampl[node * d + k] * a.ztime);
+            const HalfZZ<R> h = half_zz_warp<R>(a.edge_ampl[node * d + k] * a.ztime);
             const C* Cc = a.canon + (size_t)a.in_pos[node * d + k] * n * n;
             const R* lam = a.lmbds + (size_t)a.lmbd_pos[node * d + k] * a.lam_stride;
             for (int o = threadIdx.x; o < 2 * dim * chi; o += blockDim.x) {
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int c
             C* t = cur; cur = nxt; nxt = t;
         }
         double sz, cz;
-        sincos(a.node_ampl[node] * a.ztime, &sz, &cz);
+        sincos_warp(a.node_ampl[node] * a.ztime, &sz, &cz);
         const C z0 = c_make((R)cz, (R)-sz), z1 = c_make((R)cz, (R)sz);
         R acc[1] = {0};
         for (int o = threadIdx.x; o < per_s; o += blockDim.x) {
@@ -215,11 +215,11 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_apply
             *reinterpret_cast<float4*>(sX + tiled::swz<SW>(2 * i)) = tg[i];
     }
     double sz, cz;
-    sincos(a.node_ampl[node] * a.ztime, &sz, &cz);
+    sincos_warp(a.node_ampl[node] * a.ztime, &sz, &cz);
     const float2 zs = make_float2((float)cz, s ? (float)sz : (float)-sz);
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        const HalfZZ<float> h = half_zz<float>(a.edge_ampl[node * D + k] * a.ztime);
+        const HalfZZ<float> h = half_zz_warp<float>(a.edge_ampl[node * D + k] * a.ztime);
         const float2* Cc = a.canon + (size_t)a.in_pos[node * D + k] * n * n;
         const float* lam = a.lmbds + (size_t)a.lmbd_pos[node * D + k] * a.lam_stride;
         for (int o = threadIdx.x; o < N2; o += TH) {
