@@ -62,9 +62,27 @@ __device__ __forceinline__ void bond_product(const C* __restrict__ X, C* __restr
     }
 }
 
+// X, Y, the bond matrices, the block reduction's scratch (64), the node's half-ZZ
+// coefficients and Rz phase (2d + 1)
 __host__ __device__ inline size_t apply_smem_elems(int d, int chi, int dim) {
     const int m = chi > dim ? chi : dim;
-    return 2 * (2 * (size_t)ipow(m, d)) + (size_t)d * 2 * dim * chi + 64;
+    return 2 * (2 * (size_t)ipow(m, d)) + (size_t)d * 2 * dim * chi + 64 + 2 * (size_t)d + 1;
+}
+
+// warp 0 evaluates the node's d half-ZZ coefficient pairs and its Rz phase in double precision,
+// one lane each, into sC (2d + 1 complex); the caller synchronises before reading them
+template <typename R>
+__device__ __forceinline__ void node_coefficients(const ApplyArgs<R>& a, int node, typename Cx<R>::T* sC) {
+    const int d = a.d;
+    if ((int)threadIdx.x < d) {
+        const HalfZZ<R> h = half_zz<R>(a.edge_ampl[node * d + threadIdx.x] * a.ztime);
+        sC[2 * threadIdx.x] = h.a0;
+        sC[2 * threadIdx.x + 1] = h.a1;
+    } else if ((int)threadIdx.x == d) {
+        double sz, cz;
+        sincos(a.node_ampl[node] * a.ztime, &sz, &cz);
+        sC[2 * d] = c_make((R)cz, (R)sz);
+    }
 }
 
 template <int CM, typename R>
@@ -79,13 +97,18 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyArgs<R> a) {
     C* sY = sX + buf;
     C* sW = sY + buf;
     R* sRed = reinterpret_cast<R*>(sW + (size_t)d * 2 * dim * chi);
+    C* sC = sW + (size_t)d * 2 * dim * chi + 64;
 
     const int node = blockIdx.x;
     const int nin = 2 * ipow(chi, d);
     const C* tg = a.t_in + (size_t)node * nin;
     for (int i = threadIdx.x; i < nin; i += blockDim.x) sX[i] = tg[i];
+    node_coefficients<R>(a, node, sC);
+    __syncthreads();
     for (int k = 0; k < d; ++k) {
-        const HalfZZ<R> h = half_zz_warp<R>(a.edge_ampl[node * d + k] * a.ztime);
+        HalfZZ<R> h;
+        h.a0 = sC[2 * k];
+        h.a1 = sC[2 * k + 1];
         const C* Cc = a.canon + (size_t)a.in_pos[node * d + k] * n * n;
         const R* lam = a.lmbds + (size_t)a.lmbd_pos[node * d + k] * a.lam_stride;
         for (int o = threadIdx.x; o < 2 * dim * chi; o += blockDim.x) {
@@ -110,9 +133,7 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyArgs<R> a) {
     }
 
     // Rz, Rx, norm
-    double sz, cz;
-    sincos_warp(a.node_ampl[node] * a.ztime, &sz, &cz);
-    const C z0 = c_make((R)cz, (R)-sz), z1 = c_make((R)cz, (R)sz);
+    const C z1 = sC[2 * d], z0 = c_conj(z1);
     const int per_s = ipow(dim, d);
     R acc[1] = {0};
     for (int o = threadIdx.x; o < per_s; o += blockDim.x) {
@@ -145,6 +166,7 @@ __global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int c
     const int m = chi > dim ? chi : dim;
     const size_t buf = 2 * (size_t)ipow(m, d);
     R* sRed = reinterpret_cast<R*>(sW + (size_t)d * 2 * dim * chi);
+    C* sC = sW + (size_t)d * 2 * dim * chi + 64;
     C* X0 = scratch + (size_t)blockIdx.x * 2 * buf;
     C* Y0 = X0 + buf;
     const int nin = 2 * ipow(chi, d);
@@ -152,8 +174,12 @@ __global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int c
     for (int node = blockIdx.x; node < count; node += gridDim.x) {
         const C* tg = a.t_in + (size_t)node * nin;
         for (int i = threadIdx.x; i < nin; i += blockDim.x) X0[i] = tg[i];
+        node_coefficients<R>(a, node, sC);
+        __syncthreads();
         for (int k = 0; k < d; ++k) {
-            const HalfZZ<R> h = half_zz_warp<R>(a.edge_ampl[node * d + k] * a.ztime);
+            HalfZZ<R> h;
+            h.a0 = sC[2 * k];
+            h.a1 = sC[2 * k + 1];
             const C* Cc = a.canon + (size_t)a.in_pos[node * d + k] * n * n;
             const R* lam = a.lmbds + (size_t)a.lmbd_pos[node * d + k] * a.lam_stride;
             for (int o = threadIdx.x; o < 2 * dim * chi; o += blockDim.x) {
@@ -175,9 +201,7 @@ __global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int c
             __syncthreads();
             C* t = cur; cur = nxt; nxt = t;
         }
-        double sz, cz;
-        sincos_warp(a.node_ampl[node] * a.ztime, &sz, &cz);
-        const C z0 = c_make((R)cz, (R)-sz), z1 = c_make((R)cz, (R)sz);
+        const C z1 = sC[2 * d], z0 = c_conj(z1);
         R acc[1] = {0};
         for (int o = threadIdx.x; o < per_s; o += blockDim.x) {
             const C y0 = c_mul(z0, cur[o]), y1 = c_mul(z1, cur[per_s + o]);
@@ -208,18 +232,30 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_apply
     float2* sX = reinterpret_cast<float2*>(smem_raw);
     float2* sY = sX + PS;
     float2* sW = sY + PS;           // D blocks of [j][c], CHI x CHI
+    float2* sC = sW + D * N2;       // half-ZZ coefficients a0, a1 of each bond, then (cos, sin) of Rz
     const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
     {
         const float4* tg = reinterpret_cast<const float4*>(a.t_in + (size_t)node * 2 * PS + (size_t)s * PS);
         for (int i = threadIdx.x; i < PS / 2; i += TH)
             *reinterpret_cast<float4*>(sX + tiled::swz<SW>(2 * i)) = tg[i];
     }
-    double sz, cz;
-    sincos_warp(a.node_ampl[node] * a.ztime, &sz, &cz);
-    const float2 zs = make_float2((float)cz, s ? (float)sz : (float)-sz);
+    // the node's D + 1 double-precision trig evaluations, one lane each (one FP64 stream per CTA)
+    if (threadIdx.x < D) {
+        const HalfZZ<float> h = half_zz<float>(a.edge_ampl[node * D + threadIdx.x] * a.ztime);
+        sC[2 * threadIdx.x] = h.a0;
+        sC[2 * threadIdx.x + 1] = h.a1;
+    } else if (threadIdx.x == D) {
+        double sz, cz;
+        sincos(a.node_ampl[node] * a.ztime, &sz, &cz);
+        sC[2 * D] = make_float2((float)cz, (float)sz);
+    }
+    __syncthreads();
+    const float2 zs = make_float2(sC[2 * D].x, s ? sC[2 * D].y : -sC[2 * D].y);
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        const HalfZZ<float> h = half_zz_warp<float>(a.edge_ampl[node * D + k] * a.ztime);
+        HalfZZ<float> h;
+        h.a0 = sC[2 * k];
+        h.a1 = sC[2 * k + 1];
         const float2* Cc = a.canon + (size_t)a.in_pos[node * D + k] * n * n;
         const float* lam = a.lmbds + (size_t)a.lmbd_pos[node * D + k] * a.lam_stride;
         for (int o = threadIdx.x; o < N2; o += TH) {
@@ -265,7 +301,7 @@ __global__ void __launch_bounds__(256) apply_rx_norm_kernel(float2* t, int per_s
 template <int D, int CHI>
 static int launch_apply_half(const ApplyArgs<float>& a, int count, cudaStream_t st) {
     using S = tiled::HalfShape<D, CHI>;
-    const size_t smem = ((size_t)2 * S::PER_S + (size_t)D * S::N2) * sizeof(float2);
+    const size_t smem = ((size_t)2 * S::PER_S + (size_t)D * S::N2 + 2 * D + 2) * sizeof(float2);
     int rc = ensure_smem((const void*)tiled_apply_half_kernel<D, CHI>, smem, "tiled apply");
     if (rc) return rc;
     tiled_apply_half_kernel<D, CHI><<<2 * count, S::THREADS, smem, st>>>(a);
@@ -322,7 +358,7 @@ static int apply_classes(const bqa_class* classes, int n_classes, int chi, int d
                                  "of the %lld scratch elements a CTA needs (bqa_node_scratch_elems)",
                                  k.degree, chi, dim, (long long)k.scratch_elems, (long long)need);
             const int64_t ctas = std::min<int64_t>((int64_t)k.count, k.scratch_elems / need);
-            const size_t gsmem = ((size_t)k.degree * 2 * dim * chi + 64) * sizeof(C);
+            const size_t gsmem = ((size_t)k.degree * 2 * dim * chi + 64 + 2 * (size_t)k.degree + 1) * sizeof(C);
             void (*gk)(ApplyArgs<R>, int, C*) = nullptr;
             if (chi <= 4) gk = apply_kernel_global<4, R>;
             else if (chi <= 8) gk = apply_kernel_global<8, R>;
