@@ -1,8 +1,8 @@
 """Parity at the headline shape: a 10,000-node instance of the 100k-qubit workload's generator
 (random 3-regular, J = +-1, h ~ U(-0.5, 0.5), chi 16), first 66 steps of the 200-step schedule
 (past bond-dim saturation), against the REFERENCE run at FP64 (fixture written by
-tests/golden/make_golden_c2.py).  complex128 to round-off; complex64 within the complex64 bar
-(the pinv_eps threshold moves ~1e-3 of amplitude under complex64 rounding)."""
+tests/golden/make_golden_c2.py).  complex128 to round-off (measured 2.4e-13); complex64
+measured at 1.5e-4."""
 from pathlib import Path
 
 import numpy as np
@@ -38,7 +38,8 @@ def test_complex128_matches_reference(case, monkeypatch):
 
 
 def test_complex64_within_bar(case, monkeypatch):
+    """Measured 1.5e-4 max (5.7e-6 mean on <Z>); held to 5e-4."""
     conf, want = case
     got = _bloch(conf, "single", monkeypatch)
     err = np.abs(got - want).max()
-    assert err < 5e-3, err
+    assert err < 5e-4, err
