@@ -170,3 +170,18 @@ def test_native_step_equals_python_step(name, precision):
     for d in t1:
         assert np.array_equal(t1[d], t2[d])
     assert np.array_equal(jobs[0].bloch_vectors(), jobs[1].bloch_vectors())
+
+
+def test_known_answer_config_end_to_end(monkeypatch):
+    """The reference's known-answer config through run_qa: isolated nodes (degree-0 class), a zero
+    coupling, a default field, damping, a measurement between two evolution actions (the second
+    of type imag_time_evolution, which the reference runs as the same layer), Bloch vectors at
+    the end; complex128 against the oracle."""
+    from oracle import bqa_oracle as orc
+    from tests.test_config_layout import KNOWN_CONFIG
+    monkeypatch.setenv("BQA_PRECISION", "double")
+    got = bqa_gb300.run_qa(dict(KNOWN_CONFIG))
+    want = orc.run_qa(dict(KNOWN_CONFIG))
+    assert [k for k, _ in got] == [k for k, _ in want] == ["measurement_outcomes", "bloch_vectors"]
+    assert got[0][1] == want[0][1]
+    assert np.abs(np.array(got[1][1]) - np.array(want[1][1])).max() < 1e-9
