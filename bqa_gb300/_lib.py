@@ -9,9 +9,10 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 7
+ABI_VERSION = 8
 BQA_C64 = 0
 BQA_C128 = 1
+BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC = 0, 1, 2
 
 BQA_OK = 0
 BQA_STATUS_SVD_NOT_CONVERGED = 1
@@ -47,7 +48,7 @@ class BqaJob(ctypes.Structure):
         ("bp_eps", c_double), ("pinv_eps", c_double), ("damping", c_double),
         ("msgs", c_void_p * 2), ("ext", c_void_p), ("lu", c_void_p), ("ul", c_void_p), ("lmbds", c_void_p),
         ("colmax", c_void_p), ("dist_parts", c_void_p), ("loop_state", c_void_p), ("status", c_void_p),
-        ("edge_j", c_void_p),
+        ("edge_j", c_void_p), ("sweep_variants", POINTER(c_int32)),
     ]
 
 
@@ -67,6 +68,8 @@ SIGNATURES = {
                                c_void_p]),
     "bqa_bp_sweep_split": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                      c_int32, c_void_p, c_void_p, c_void_p]),
+    "bqa_bp_sweep_plan": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, POINTER(c_int32), c_void_p,
+                                    c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p]),
     "bqa_bp_finalize": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_double, c_double,
                                   c_int32, c_void_p]),
     "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),
@@ -89,6 +92,11 @@ SIGNATURES = {
                                            c_void_p, c_void_p, c_void_p]),
     "bqa_fp32_fma_probe": (c_int32, [c_int32, c_int32, c_void_p, c_void_p]),
     "bqa_run_layer": (c_int32, [POINTER(BqaJob), c_double, c_double, POINTER(BqaLayerInfo), c_void_p]),
+    "bqa_graph_cache_create": (c_int32, [POINTER(c_void_p)]),
+    "bqa_graph_cache_destroy": (c_int32, [c_void_p]),
+    "bqa_run_layer_graph": (c_int32, [POINTER(BqaJob), c_void_p, c_double, c_double, POINTER(BqaLayerInfo),
+                                      c_void_p]),
+    "bqa_run_bp_graph": (c_int32, [POINTER(BqaJob), c_void_p, POINTER(BqaLayerInfo), c_void_p]),
     "bqa_layout_degrees": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
                                      c_void_p, c_void_p, c_void_p, c_void_p]),
     "bqa_layout_class": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_void_p,

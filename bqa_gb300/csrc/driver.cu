@@ -7,6 +7,7 @@
 // Mirrors src/bqa/state.py:315-321 (run_layer), :230-247 (_simple_update), :97-124 (_run_bp).
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <vector>
 
 #include "common.cuh"
@@ -34,6 +35,9 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes, int32_t n_classes, int32_t 
                            void* stream);
 int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, int32_t dtype, void* dist_parts,
                         int32_t* loop_state, double eps, double damping, int32_t max_iters, void* stream);
+int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype,
+                          const int32_t* variants, void* msgs_a, void* msgs_b, void* pm, int32_t edges,
+                          void* dist_parts, const int32_t* loop_state, void* stream);
 }
 
 namespace bqa {
@@ -100,6 +104,18 @@ static int gate_layer(bqa_job* j, double xtime, double ztime, bqa_layer_info* in
     return bqa_msgs_from_lmbds(j->lmbds, n, E, dims, dt, j->msgs[j->mcur], s);
 }
 
+// One sweep of the job's BP loop: the tuned per-class kernels when the job carries a plan.
+static int job_sweep(bqa_job* j, void* a, void* b, void* s) {
+    if (j->sweep_variants)
+        return bqa_bp_sweep_plan(j->classes, j->n_classes, j->chis, j->dtype,
+                                 j->sweep_variants + (size_t)j->chis * j->n_classes, a, b,
+                                 j->split_sweeps ? j->lu : nullptr, j->edges, j->dist_parts, j->loop_state, s);
+    if (j->split_sweeps)
+        return bqa_bp_sweep_split(j->classes, j->n_classes, j->chis, j->dtype, a, b, j->lu, j->edges, j->dist_parts,
+                                  j->loop_state, s);
+    return bqa_bp_sweep(j->classes, j->n_classes, j->chis, j->dtype, a, b, j->dist_parts, j->loop_state, s);
+}
+
 static int run_bp(bqa_job* j, bqa_layer_info* info, cudaStream_t st) {
     if (j->max_bp_iters < 1) return set_error(BQA_ERR_ARG, "max_bp_iter_number must be >= 1 to run BP");
     void* s = reinterpret_cast<void*>(st);
@@ -115,12 +131,7 @@ static int run_bp(bqa_job* j, bqa_layer_info* info, cudaStream_t st) {
     while (true) {
         const int group = (j->max_bp_iters - launched) < every ? (j->max_bp_iters - launched) : every;
         for (int g = 0; g < group; ++g) {
-            if (j->split_sweeps)
-                rc = bqa_bp_sweep_split(j->classes, j->n_classes, j->chis, j->dtype, a, b, j->lu, j->edges,
-                                        j->dist_parts, j->loop_state, s);
-            else
-                rc = bqa_bp_sweep(j->classes, j->n_classes, j->chis, j->dtype, a, b, j->dist_parts, j->loop_state, s);
-            if (rc) return rc;
+            if ((rc = job_sweep(j, a, b, s))) return rc;
             if ((rc = bqa_bp_finalize(a, b, elems, j->dtype, j->dist_parts, j->loop_state, j->bp_eps, j->damping,
                                       j->max_bp_iters, s)))
                 return rc;
@@ -155,4 +166,255 @@ extern "C" int32_t bqa_run_layer(bqa_job* job, double xtime, double ztime, bqa_l
     int rc = gate_layer(job, xtime, ztime, info, st);
     if (rc) return rc;
     return run_bp(job, info, st);
+}
+
+// ---- BP to tolerance as one CUDA graph ----------------------------------------------------
+//
+// The device-driven BP loop launches the same kernels with the same arguments every sweep
+// (which message buffer is read, whether the run is done and whether to damp all live in
+// loop_state on the device), so a whole run -- zero the loop state, then sweep + decision +
+// damping while the decision kernel has not marked the run done, then copy the loop state to
+// the host -- is captured once per (buffers, bond dim, loop parameters) as a graph with a
+// WHILE node.  A BP run is then one graph launch and one host read, instead of 3-4 launches
+// per sweep, a host read every bp_check_every sweeps and up to bp_check_every - 1 sweeps
+// queued after convergence that return at once.  Same kernels in the same order as run_bp:
+// the state after a step is bit-identical.
+
+namespace bqa {
+
+// Repeats the WHILE body while the run is not done.  loop_state[7] counts the body passes;
+// the loop also ends after max_iters passes whatever the decision says, so it cannot run on.
+__global__ void bp_graph_cond_kernel(cudaGraphConditionalHandle handle, int32_t* ls, int max_iters) {
+    const int passes = ls[7] + 1;
+    ls[7] = passes;
+    cudaGraphSetConditional(handle, (ls[0] == 0 && passes < max_iters) ? 1u : 0u);
+}
+
+struct GraphEntry {
+    std::vector<uint64_t> key;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+}  // namespace bqa
+
+struct bqa_graph_cache {
+    int device = 0;
+    cudaStream_t capture[2] = {nullptr, nullptr};   // private streams: capture cannot use the legacy stream
+    int32_t* host_ls = nullptr;                      // pinned: target of the graph's loop-state copy
+    std::vector<bqa::GraphEntry> entries;            // oldest first
+};
+
+namespace bqa {
+
+constexpr size_t kGraphCacheEntries = 16;
+
+static void release(GraphEntry& e) {
+    if (e.exec) cudaGraphExecDestroy(e.exec);
+    if (e.graph) cudaGraphDestroy(e.graph);
+    e.exec = nullptr;
+    e.graph = nullptr;
+}
+
+static uint64_t bits_of(double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    return u;
+}
+
+// Everything a captured BP run bakes into its launches.
+static std::vector<uint64_t> bp_graph_key(const bqa_job* j) {
+    std::vector<uint64_t> k = {(uint64_t)j->dtype, (uint64_t)j->chis, (uint64_t)j->mcur, (uint64_t)j->edges,
+                               (uint64_t)j->split_sweeps, (uint64_t)j->max_bp_iters, bits_of(j->bp_eps),
+                               bits_of(j->damping), (uint64_t)(uintptr_t)j->msgs[0], (uint64_t)(uintptr_t)j->msgs[1],
+                               (uint64_t)(uintptr_t)j->lu, (uint64_t)(uintptr_t)j->dist_parts,
+                               (uint64_t)(uintptr_t)j->loop_state, (uint64_t)j->n_classes};
+    for (int c = 0; c < j->n_classes; ++c) {
+        const bqa_class& x = j->classes[c];
+        const void* p[] = {x.node_ids, x.in_pos, x.out_pos, x.lmbd_pos, x.edge_ampl, x.node_ampl, x.tensor, x.scratch};
+        k.push_back(j->sweep_variants ? (uint64_t)(1 + j->sweep_variants[j->chis * j->n_classes + c]) : 0);
+        k.push_back((uint64_t)x.degree);
+        k.push_back((uint64_t)x.count);
+        k.push_back((uint64_t)x.scratch_elems);
+        for (const void* q : p) k.push_back((uint64_t)(uintptr_t)q);
+    }
+    return k;
+}
+
+// One sweep, the decision and the damping, then the loop condition: the WHILE body.
+static int bp_body(bqa_job* j, cudaGraphConditionalHandle h, cudaStream_t st) {
+    void* s = reinterpret_cast<void*>(st);
+    void* a = j->msgs[j->mcur];
+    void* b = j->msgs[1 - j->mcur];
+    int rc = job_sweep(j, a, b, s);
+    if (rc) return rc;
+    const int64_t elems = (int64_t)j->edges * j->chis * j->chis;
+    if ((rc = bqa_bp_finalize(a, b, elems, j->dtype, j->dist_parts, j->loop_state, j->bp_eps, j->damping,
+                              j->max_bp_iters, s)))
+        return rc;
+    bp_graph_cond_kernel<<<1, 1, 0, st>>>(h, j->loop_state, j->max_bp_iters);
+    return check_launch("bp_graph_cond");
+}
+
+static int capture_bp_graph(bqa_job* j, bqa_graph_cache* cache, GraphEntry* out) {
+    cudaStream_t s0 = cache->capture[0], s1 = cache->capture[1];
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return cuda_rc(e, "cudaGraphCreate");
+    int rc = BQA_OK;
+    bool cap0 = false, cap1 = false;
+    do {
+        cudaGraphConditionalHandle h;
+        // default 1 at every launch: the body runs at least once (max_bp_iters >= 1)
+        if ((rc = cuda_rc(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault), "handle"))) break;
+        if ((rc = cuda_rc(cudaStreamBeginCaptureToGraph(s0, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                          "capture")))
+            break;
+        cap0 = true;
+        if ((rc = cuda_rc(cudaMemsetAsync(j->loop_state, 0, 8 * sizeof(int32_t), s0), "loop state"))) break;
+        if ((rc = cuda_rc(cudaMemsetAsync(j->dist_parts, 0, 2 * sizeof(int64_t), s0), "dist"))) break;
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        const cudaGraphEdgeData* edata = nullptr;
+        size_t ndeps = 0;
+        if ((rc = cuda_rc(cudaStreamGetCaptureInfo(s0, &cs, nullptr, nullptr, &deps, &edata, &ndeps), "capture info")))
+            break;
+        cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        if ((rc = cuda_rc(cudaGraphAddNode(&node, g, deps, edata, ndeps, &p), "while node"))) break;
+        if ((rc = cuda_rc(cudaStreamUpdateCaptureDependencies(s0, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+                          "capture dependencies")))
+            break;
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        if ((rc = cuda_rc(cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                          "body capture")))
+            break;
+        cap1 = true;
+        rc = bp_body(j, h, s1);
+        cudaGraph_t tmp = nullptr;
+        cap1 = false;
+        const int rc_end = cuda_rc(cudaStreamEndCapture(s1, &tmp), "body capture end");
+        if (rc || (rc = rc_end)) break;
+        if ((rc = cuda_rc(cudaMemcpyAsync(cache->host_ls, j->loop_state, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                          s0),
+                          "loop read")))
+            break;
+    } while (false);
+    if (cap1) {
+        cudaGraph_t tmp = nullptr;
+        cudaStreamEndCapture(s1, &tmp);
+    }
+    if (cap0) {
+        cudaGraph_t tmp = nullptr;
+        const int rc_end = cuda_rc(cudaStreamEndCapture(s0, &tmp), "capture end");
+        if (!rc) rc = rc_end;
+    }
+    cudaGetLastError();   // a failed capture leaves its error pending; it is reported through rc
+    if (rc) {
+        cudaGraphDestroy(g);
+        return rc;
+    }
+    cudaGraphExec_t exec = nullptr;
+    if ((rc = cuda_rc(cudaGraphInstantiate(&exec, g, 0), "cudaGraphInstantiate"))) {
+        cudaGraphDestroy(g);
+        return rc;
+    }
+    out->graph = g;
+    out->exec = exec;
+    return BQA_OK;
+}
+
+static int run_bp_graph(bqa_job* j, bqa_graph_cache* cache, bqa_layer_info* info, cudaStream_t st) {
+    if (j->max_bp_iters < 1) return set_error(BQA_ERR_ARG, "max_bp_iter_number must be >= 1 to run BP");
+    int dev = 0;
+    int rc;
+    if ((rc = cuda_rc(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
+    if (dev != cache->device) return set_error(BQA_ERR_ARG, "bqa graph cache belongs to device %d, not %d",
+                                               cache->device, dev);
+    std::vector<uint64_t> key = bp_graph_key(j);
+    GraphEntry* hit = nullptr;
+    for (auto& e : cache->entries)
+        if (e.key == key) hit = &e;
+    if (!hit) {
+        GraphEntry fresh;
+        fresh.key = std::move(key);
+        if ((rc = capture_bp_graph(j, cache, &fresh))) return rc;
+        if (cache->entries.size() >= kGraphCacheEntries) {
+            release(cache->entries.front());
+            cache->entries.erase(cache->entries.begin());
+        }
+        cache->entries.push_back(std::move(fresh));
+        hit = &cache->entries.back();
+    }
+    if ((rc = cuda_rc(cudaGraphLaunch(hit->exec, st), "cudaGraphLaunch"))) return rc;
+    if ((rc = cuda_rc(cudaStreamSynchronize(st), "sync"))) return rc;
+    int32_t ls[8];
+    std::memcpy(ls, cache->host_ls, sizeof(ls));
+    if (!ls[0]) return set_error(BQA_ERR_UNSUPPORTED, "BP graph ended without a decision after %d sweeps", ls[1]);
+    if (ls[2]) j->mcur = 1 - j->mcur;
+    info->sweeps = ls[1];
+    info->bp_exhausted = ls[3];
+    float best;
+    std::memcpy(&best, &ls[6], 4);
+    info->best_dist = best;
+    return BQA_OK;
+}
+
+static int check_job(const bqa_job* job) {
+    if (!job || !job->classes || job->n_classes < 0 || job->edges < 2 || job->chis < 1 ||
+        2 * job->chis > job->colmax_elems || 2 * job->chis > 64)
+        return set_error(BQA_ERR_ARG, "bad job");
+    return BQA_OK;
+}
+
+}  // namespace bqa
+
+extern "C" int32_t bqa_graph_cache_create(bqa_graph_cache** out) {
+    if (!out) return set_error(BQA_ERR_ARG, "bqa_graph_cache_create: null output");
+    *out = nullptr;
+    auto* c = new (std::nothrow) bqa_graph_cache();
+    if (!c) return set_error(BQA_ERR_ARG, "bqa_graph_cache_create: out of host memory");
+    int rc = cuda_rc(cudaGetDevice(&c->device), "cudaGetDevice");
+    for (int i = 0; i < 2 && !rc; ++i)
+        rc = cuda_rc(cudaStreamCreateWithFlags(&c->capture[i], cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!rc) rc = cuda_rc(cudaHostAlloc((void**)&c->host_ls, 8 * sizeof(int32_t), cudaHostAllocDefault), "cudaHostAlloc");
+    if (rc) {
+        bqa_graph_cache_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return BQA_OK;
+}
+
+extern "C" int32_t bqa_graph_cache_destroy(bqa_graph_cache* cache) {
+    if (!cache) return BQA_OK;
+    for (auto& e : cache->entries) release(e);
+    for (cudaStream_t s : cache->capture)
+        if (s) cudaStreamDestroy(s);
+    if (cache->host_ls) cudaFreeHost(cache->host_ls);
+    delete cache;
+    return BQA_OK;
+}
+
+extern "C" int32_t bqa_run_bp_graph(bqa_job* job, bqa_graph_cache* cache, bqa_layer_info* info, void* stream) {
+    if (!cache || !info) return set_error(BQA_ERR_ARG, "bqa_run_bp_graph: bad argument");
+    int rc = check_job(job);
+    if (rc) return rc;
+    std::memset(info, 0, sizeof(*info));
+    info->bond_dim = job->chi;
+    return run_bp_graph(job, cache, info, as_stream(stream));
+}
+
+extern "C" int32_t bqa_run_layer_graph(bqa_job* job, bqa_graph_cache* cache, double xtime, double ztime,
+                                       bqa_layer_info* info, void* stream) {
+    if (!cache || !info) return set_error(BQA_ERR_ARG, "bqa_run_layer_graph: bad argument");
+    int rc = check_job(job);
+    if (rc) return rc;
+    std::memset(info, 0, sizeof(*info));
+    cudaStream_t st = as_stream(stream);
+    if ((rc = gate_layer(job, xtime, ztime, info, st))) return rc;
+    return run_bp_graph(job, cache, info, st);
 }

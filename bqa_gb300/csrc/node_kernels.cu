@@ -824,15 +824,10 @@ __global__ void __launch_bounds__(256) bp_combine_kernel(const typename Cx<R>::T
     }
 }
 
+// The generic shared-memory node kernel (any degree and bond dim <= 32 whose node fits).
 template <int MODE, typename R>
-static int launch_node_mode(const NodeArgs<R>& args, int count, cudaStream_t st) {
+static int launch_node_generic(const NodeArgs<R>& args, int count, cudaStream_t st) {
     const int chi = args.chi, d = args.d;
-    if constexpr (sizeof(R) == 4 && (MODE == MODE_BP || MODE == MODE_EXT || MODE == MODE_DENS)) {
-        if (g_use_tiled) {
-            int rc = BQA_OK;
-            if (try_tiled<MODE>(args, count, st, &rc)) return rc;
-        }
-    }
     const size_t smem = node_smem_elems(d, chi) * sizeof(typename Cx<R>::T);
     const int fib = 2 * ipow(chi, d > 0 ? d - 1 : 0);
     int threads = ((max(fib, 2 * chi * chi) + 31) / 32) * 32;
@@ -849,6 +844,17 @@ static int launch_node_mode(const NodeArgs<R>& args, int count, cudaStream_t st)
     if (rc) return rc;
     kern<<<count, threads, smem, st>>>(args);
     return check_launch("node kernel");
+}
+
+template <int MODE, typename R>
+static int launch_node_mode(const NodeArgs<R>& args, int count, cudaStream_t st) {
+    if constexpr (sizeof(R) == 4 && (MODE == MODE_BP || MODE == MODE_EXT || MODE == MODE_DENS)) {
+        if (g_use_tiled) {
+            int rc = BQA_OK;
+            if (try_tiled<MODE>(args, count, st, &rc)) return rc;
+        }
+    }
+    return launch_node_generic<MODE, R>(args, count, st);
 }
 
 template <typename R>
@@ -1007,6 +1013,57 @@ static int finalize(void* a, void* b, int64_t n, void* parts, int32_t* ls, doubl
     return check_launch("bp_damp");
 }
 
+template <typename R>
+static NodeArgs<R> class_args(const bqa_class& k, int chi, const void* msgs_a, void* msgs_b, void* out,
+                              void* dist_parts, const int32_t* loop_state) {
+    using C = typename Cx<R>::T;
+    NodeArgs<R> a;
+    a.tensors = static_cast<const C*>(k.tensor);
+    a.in_pos = k.in_pos;
+    a.out_pos = k.out_pos;
+    a.node_ids = k.node_ids;
+    a.edge_ampl = k.edge_ampl;
+    a.d = k.degree;
+    a.chi = chi;
+    a.msgs_a = static_cast<const C*>(msgs_a);
+    a.msgs_b = static_cast<C*>(msgs_b);
+    a.out = static_cast<C*>(out);
+    a.loop_state = loop_state;
+    a.dist_parts = static_cast<typename Cx<R>::Bits*>(dist_parts);
+    a.ztime = 0.0;
+    return a;
+}
+
+// BP sweep of one class with the generic shared-memory kernel (MODE_BP: messages and
+// convergence maxima; MODE_PSPLIT: open-bond blocks into pm).  Classes whose nodes exceed
+// shared memory have only the global-memory form, which run_classes picks.
+template <int MODE, typename R>
+static int sweep_class_generic(const bqa_class& k, int chi, const void* msgs_a, void* msgs_b, void* out,
+                               void* dist_parts, const int32_t* loop_state, cudaStream_t st) {
+    using C = typename Cx<R>::T;
+    if (node_smem_elems(k.degree, chi) * sizeof(C) > kMaxSmem) {
+        bqa_class one = k;
+        return run_classes<R>(MODE, &one, 1, chi, msgs_a, msgs_b, out, dist_parts, loop_state, 0.0, st);
+    }
+    return launch_node_generic<MODE, R>(class_args<R>(k, chi, msgs_a, msgs_b, out, dist_parts, loop_state), k.count,
+                                        st);
+}
+
+static int launch_bp_combine(int dtype, const void* pm, int edges, int chi, void* msgs_a, void* msgs_b,
+                             const int32_t* loop_state, void* dist_parts, cudaStream_t st) {
+    const int blocks = (int)(((int64_t)edges * 32 + 255) / 256);
+    if (dtype == BQA_C64)
+        bp_combine_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float2*>(pm), edges, chi,
+                                                          static_cast<const float2*>(msgs_a), static_cast<float2*>(msgs_b),
+                                                          loop_state, static_cast<uint32_t*>(dist_parts));
+    else
+        bp_combine_kernel<double><<<blocks, 256, 0, st>>>(static_cast<const double2*>(pm), edges, chi,
+                                                           static_cast<const double2*>(msgs_a),
+                                                           static_cast<double2*>(msgs_b), loop_state,
+                                                           static_cast<unsigned long long*>(dist_parts));
+    return check_launch("bp_combine");
+}
+
 }  // namespace bqa
 
 using namespace bqa;
@@ -1080,6 +1137,60 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes, int32_t n_classes, int32_t 
                                                            static_cast<double2*>(msgs_b), loop_state,
                                                            static_cast<unsigned long long*>(dist_parts));
     return check_launch("bp_combine");
+}
+
+int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype,
+                          const int32_t* variants, void* msgs_a, void* msgs_b, void* pm, int32_t edges,
+                          void* dist_parts, const int32_t* loop_state, void* stream) {
+    if (!variants)
+        return pm ? bqa_bp_sweep_split(classes, n_classes, chi, dtype, msgs_a, msgs_b, pm, edges, dist_parts,
+                                       loop_state, stream)
+                  : bqa_bp_sweep(classes, n_classes, chi, dtype, msgs_a, msgs_b, dist_parts, loop_state, stream);
+    if (!classes || n_classes < 0 || chi < 1 || !msgs_a || !msgs_b || !dist_parts || (pm && edges < 2))
+        return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: bad argument");
+    if (dtype != BQA_C64 && dtype != BQA_C128) return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: unknown dtype %d", dtype);
+    cudaStream_t st = as_stream(stream);
+    for (int c = 0; c < n_classes; ++c) {
+        const bqa_class& k = classes[c];
+        if (k.count <= 0 || k.degree == 0) continue;
+        const int v = variants[c];
+        if (v < BQA_VARIANT_DEFAULT || v > BQA_VARIANT_GENERIC)
+            return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: unknown variant %d", v);
+        int rc = BQA_OK;
+        if (v == BQA_VARIANT_DEFAULT) {
+            // the kernel bqa_bp_sweep_split / bqa_bp_sweep would launch for this class
+            bqa_class one = k;
+            if (pm) {
+                int hit = 0;
+                if (dtype == BQA_C64 && g_use_tiled) {
+                    NodeArgs<float> a = class_args<float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state);
+                    hit = try_half(a, k.count, st, &rc);
+                }
+                if (!hit)
+                    rc = run_classes_dt(dtype, MODE_PSPLIT, &one, 1, chi, msgs_a, msgs_b, pm, nullptr, loop_state, 0.0,
+                                        st);
+            } else {
+                rc = run_classes_dt(dtype, MODE_BP, &one, 1, chi, msgs_a, msgs_b, nullptr, dist_parts, loop_state, 0.0,
+                                    st);
+            }
+        } else if (v == BQA_VARIANT_TILED) {
+            if (dtype != BQA_C64)
+                return set_error(BQA_ERR_UNSUPPORTED, "bqa_bp_sweep_plan: no register-tiled complex128 kernel");
+            NodeArgs<float> a = class_args<float>(k, chi, msgs_a, msgs_b, pm, pm ? nullptr : dist_parts, loop_state);
+            const int hit = pm ? try_half(a, k.count, st, &rc) : try_tiled<MODE_BP>(a, k.count, st, &rc);
+            if (!hit)
+                return set_error(BQA_ERR_UNSUPPORTED, "bqa_bp_sweep_plan: no register-tiled kernel for degree %d, "
+                                 "bond dim %d", k.degree, chi);
+        } else if (dtype == BQA_C64) {
+            rc = pm ? sweep_class_generic<MODE_PSPLIT, float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state, st)
+                    : sweep_class_generic<MODE_BP, float>(k, chi, msgs_a, msgs_b, nullptr, dist_parts, loop_state, st);
+        } else {
+            rc = pm ? sweep_class_generic<MODE_PSPLIT, double>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state, st)
+                    : sweep_class_generic<MODE_BP, double>(k, chi, msgs_a, msgs_b, nullptr, dist_parts, loop_state, st);
+        }
+        if (rc) return rc;
+    }
+    return pm ? launch_bp_combine(dtype, pm, edges, chi, msgs_a, msgs_b, loop_state, dist_parts, st) : BQA_OK;
 }
 
 int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, int32_t dtype, void* dist_parts,

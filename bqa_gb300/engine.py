@@ -73,7 +73,7 @@ class Annealer:
     """One annealing job resident on one GPU."""
 
     def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4,
-                 pad_bonds: bool | None = None, native: bool = True):
+                 pad_bonds: bool | None = None, native: bool = True, graphs: bool | None = None):
         import torch
         self.torch = torch
         if not torch.cuda.is_available():
@@ -88,6 +88,13 @@ class Annealer:
         # steps through bqa_run_layer (one library call per step, no interpreter lock held);
         # per-kernel timing runs the same launches from Python
         self.native = bool(native)
+        # BP runs replayed as captured CUDA graphs (one launch and one host read per run) unless
+        # graphs=False or the environment variable BQA_GB300_GRAPHS=0
+        if graphs is None:
+            import os
+            graphs = os.environ.get("BQA_GB300_GRAPHS", "1") != "0"
+        self.graphs = bool(graphs)
+        self._graph_cache = None
         self.device = torch.device(device if device is not None else "cuda")
         self.bp_check_every = max(1, int(bp_check_every))
         E = ctx.edges_number
@@ -155,6 +162,23 @@ class Annealer:
         self.stats: list[dict] = []
         self._events: list | None = None
         self.reset()
+
+    def __del__(self):
+        cache, self._graph_cache = getattr(self, "_graph_cache", None), None
+        if cache is not None:
+            try:
+                self.lib.dll.bqa_graph_cache_destroy(cache)
+            except Exception:
+                pass
+
+    def _graphs(self):
+        """The job's BP graph cache (created on first use, with the job's device current)."""
+        if self._graph_cache is None:
+            h = ctypes.c_void_p()
+            with self.torch.cuda.device(self.device):
+                self.lib.call("bqa_graph_cache_create", ctypes.byref(h))
+            self._graph_cache = h
+        return self._graph_cache
 
     # ---- kernel timing (CUDA events on the launch stream) ----------------------------------
     def enable_kernel_timing(self, on: bool = True) -> None:
@@ -382,7 +406,11 @@ class Annealer:
             raise ValueError("max_bp_iter_number must be >= 1 to run belief propagation")
         j, cls = self._job_struct()
         res = _lib.BqaLayerInfo()
-        self.lib.call("bqa_run_layer", ctypes.byref(j), xtime, ztime, ctypes.byref(res), self.stream)
+        if self.graphs:
+            self.lib.call("bqa_run_layer_graph", ctypes.byref(j), self._graphs(), xtime, ztime, ctypes.byref(res),
+                          self.stream)
+        else:
+            self.lib.call("bqa_run_layer", ctypes.byref(j), xtime, ztime, ctypes.byref(res), self.stream)
         self.chi, self.chis, self.lam_stride, self.mcur, self.tcur = j.chi, j.chis, j.lam_stride, j.mcur, j.tcur
         if res.svd_not_converged:
             log.warning("a Jacobi SVD of the truncation step hit its sweep cap")
@@ -401,6 +429,8 @@ class Annealer:
         ctx = self.ctx
         if ctx.max_bp_iters_number < 1:
             raise ValueError("max_bp_iter_number must be >= 1 to run belief propagation")
+        if self.native and self.graphs and self._events is None:
+            return self._run_bp_graph()
         lib, st = self.lib, self.stream
         cls = self._class_array()
         a, b = self.msgs[self.mcur], self.msgs[1 - self.mcur]
@@ -442,6 +472,16 @@ class Annealer:
             log.warning(f"BP algorithm exceeds iterations limit set to {ctx.max_bp_iters_number}, "
                         f"obtained bp_eps {best}")
         return int(ls[1])
+
+    def _run_bp_graph(self) -> int:
+        j, cls = self._job_struct()
+        res = _lib.BqaLayerInfo()
+        self.lib.call("bqa_run_bp_graph", ctypes.byref(j), self._graphs(), ctypes.byref(res), self.stream)
+        self.mcur = j.mcur
+        if res.bp_exhausted:
+            log.warning(f"BP algorithm exceeds iterations limit set to {self.ctx.max_bp_iters_number}, "
+                        f"obtained bp_eps {res.best_dist}")
+        return int(res.sweeps)
 
     # ---- read-out ------------------------------------------------------------------------
     def density_matrices(self) -> np.ndarray:

@@ -44,6 +44,13 @@ enum {
 
 enum { BQA_C64 = 0, BQA_C128 = 1 };
 
+/* message-kernel form of one degree class in a BP sweep (bqa_bp_sweep_plan) */
+enum {
+    BQA_VARIANT_DEFAULT = 0,  /* the kernel bqa_bp_sweep / bqa_bp_sweep_split launch */
+    BQA_VARIANT_TILED = 1,    /* register-tiled: half-node (two-stage sweep) or whole-node (one stage) */
+    BQA_VARIANT_GENERIC = 2   /* generic shared-memory kernel (global-memory form beyond shared memory) */
+};
+
 /* device status word bits (written by kernels into a caller int32) */
 enum {
     BQA_STATUS_SVD_NOT_CONVERGED = 1, /* a Jacobi SVD hit its sweep cap */
@@ -96,6 +103,8 @@ typedef struct bqa_job {
     int32_t* loop_state;       /* 8 x int32 */
     int32_t* status;           /* 1 x int32 */
     const double* edge_j;      /* [E/2] couplings (two-stage extended messages) */
+    const int32_t* sweep_variants; /* host [33][n_classes] or NULL: row chis holds each class's BQA_VARIANT_*
+                                      for BP sweeps at storage bond dim chis (bqa_bp_sweep_plan) */
 } bqa_job;
 
 /* What one step did. */
@@ -117,6 +126,35 @@ typedef struct bqa_layer_info {
  * entry points.  Blocks the calling thread at the two reads of a step.
  */
 int32_t bqa_run_layer(bqa_job* job, double xtime, double ztime, bqa_layer_info* info, void* stream);
+
+/*
+ * Captured CUDA graphs of BP runs, one cache per job (opaque).  The BP loop of
+ * src/bqa/state.py:97-124 launches the same kernels with the same arguments every sweep (the
+ * loop state lives on the device), so a whole run -- zero the loop state, sweep + decision +
+ * damping under a WHILE node that repeats until the decision kernel marks the run done (at the
+ * latest after max_bp_iters sweeps), copy the loop state to the host -- is captured once per
+ * (buffers, bond dim, current message buffer, loop parameters) and replayed as ONE graph launch
+ * and one host read per BP run.  Create the cache with the job's device current; it owns two
+ * non-blocking capture streams, a pinned 32-byte host buffer and up to 16 executable graphs
+ * (oldest evicted).  One host thread at a time per cache.
+ */
+typedef struct bqa_graph_cache bqa_graph_cache;
+int32_t bqa_graph_cache_create(bqa_graph_cache** out /* host */);
+int32_t bqa_graph_cache_destroy(bqa_graph_cache* cache);
+
+/*
+ * bqa_run_layer with its BP run replayed from the cache (captured on first use): the gate
+ * layer is launched as in bqa_run_layer (its gate angles change every step), then the BP run
+ * is one graph launch.  Same kernels in the same order as bqa_run_layer, minus the sweeps it
+ * queues after convergence (those return at once), so the state after the step is
+ * bit-identical.  Blocks the calling thread at the two reads of a step.
+ */
+int32_t bqa_run_layer_graph(bqa_job* job, bqa_graph_cache* cache, double xtime, double ztime, bqa_layer_info* info,
+                            void* stream);
+
+/* The BP run alone (src/bqa/state.py:97-124) from the cache; info->sweeps, bp_exhausted and
+ * best_dist are filled in, bond_dim is the job's current bond dim. */
+int32_t bqa_run_bp_graph(bqa_job* job, bqa_graph_cache* cache, bqa_layer_info* info, void* stream);
 
 /* ABI version of this header (bumped on any signature change). */
 int32_t bqa_abi_version(void);
@@ -161,6 +199,21 @@ int32_t bqa_bp_sweep(const bqa_class* classes /* host array */, int32_t n_classe
 int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi, int32_t dtype,
                            void* msgs_a, void* msgs_b, void* pm, int32_t edges, void* dist_parts,
                            const int32_t* loop_state, void* stream);
+
+/*
+ * One BP sweep with the message kernel of every class chosen by the caller: variants[c]
+ * (host int32 [n_classes], BQA_VARIANT_*) for classes[c]; pm != NULL runs the two-stage form
+ * of bqa_bp_sweep_split (TILED = half-node kernels, GENERIC = generic open-bond blocks, then one
+ * combine pass over all `edges` slots), pm == NULL the one-stage form of bqa_bp_sweep (TILED =
+ * whole-node kernels).  TILED is BQA_ERR_UNSUPPORTED where no register-tiled kernel exists
+ * (complex64, degree 2-4, chi in {4, 8, 12, 16} minus (2, 4) and (4, 12+)).  variants == NULL is
+ * bqa_bp_sweep_split (pm != NULL) or bqa_bp_sweep.  The choices are the search space of the
+ * host-side autotuner (bqa_gb300/autotune.py); every variant computes the same messages up to
+ * rounding.  Same loop_state and dist_parts behaviour as bqa_bp_sweep.
+ */
+int32_t bqa_bp_sweep_plan(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi, int32_t dtype,
+                          const int32_t* variants /* host */, void* msgs_a, void* msgs_b, void* pm, int32_t edges,
+                          void* dist_parts, const int32_t* loop_state, void* stream);
 
 /*
  * BP convergence decision and damping after one sweep (src/bqa/state.py:113-124,

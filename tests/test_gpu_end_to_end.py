@@ -172,6 +172,47 @@ def test_native_step_equals_python_step(name, precision):
     assert np.array_equal(jobs[0].bloch_vectors(), jobs[1].bloch_vectors())
 
 
+@pytest.mark.parametrize("name,precision", [("rr3_n16_chi4", "single"), ("grid3x4_chi4_damped", "single"),
+                                            ("mixed_n18_chi3", "double"), ("rr3_n24_chi8", "single"),
+                                            ("tree9", "double")])
+def test_graph_bp_equals_native_step(name, precision):
+    """BP runs replayed from captured CUDA graphs (WHILE node, device-side stop) run the same kernels
+    in the same order as the launch-by-launch native driver: identical state, sweep counts and
+    exhaustion flags after every step, including damped runs that hit the sweep cap."""
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
+    ctx = build_context(gc.config(name))
+    steps = [i for i in ctx.instructions if isinstance(i, dict)][:10]
+    jobs = [Annealer(ctx, precision=precision, graphs=g) for g in (True, False)]
+    for ins in steps:
+        for job in jobs:
+            job.run_layer(ins["xtime"], ins["ztime"])
+        (t1, m1, l1), (t2, m2, l2) = (j.get_state() for j in jobs)
+        assert np.array_equal(m1, m2) and np.array_equal(l1, l2)
+        for d in t1:
+            assert np.array_equal(t1[d], t2[d])
+    assert jobs[0].stats == jobs[1].stats
+    assert jobs[0]._graph_cache is not None and jobs[1]._graph_cache is None
+    # a BP run on its own (the measurement loop's call) from the same cache
+    assert jobs[0].run_bp() == jobs[1].run_bp()
+    assert np.array_equal(jobs[0].bloch_vectors(), jobs[1].bloch_vectors())
+
+
+def test_graph_measurement_matches_oracle():
+    """The measurement loop (two BP runs per draw) on graph-replayed BP: outcomes equal the
+    reference's recorded ones."""
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
+    name = "rr3_n12_measure"
+    ctx = build_context(gc.config(name))
+    a = [Annealer(ctx, precision="double", graphs=g) for g in (True, False)]
+    for job in a:
+        for ins in ctx.instructions:
+            if isinstance(ins, dict):
+                job.run_layer(ins["xtime"], ins["ztime"])
+    assert a[0].measure() == a[1].measure()
+
+
 def test_known_answer_config_end_to_end(monkeypatch):
     """The reference's known-answer config through run_qa: isolated nodes (degree-0 class), a zero
     coupling, a default field, damping, a measurement between two evolution actions (the second
