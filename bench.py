@@ -341,6 +341,7 @@ def run_gpu_arm(args) -> None:
                      "where": "complex64 path vs the reference at FP64 on a 10,000-node instance of this "
                               "generator (chi 16, first 66 steps, past saturation); tests/test_gpu_c2_parity.py "
                               "holds it to 5e-4 (complex128: 2.4e-13)"},
+        "autotune": ([job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off"),
         "gpu_launches": gpu_launches(job, kt, args.steps),
         "clocks": clocks.summary(),
         "prep": {"steps": prep_steps, "seconds": round(prep_s, 1)},
@@ -685,6 +686,8 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="1: BP message kernels chosen per (degree, bond dim) by the autotuner; 0: built-in choice")
     ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout", "small", "mixed"])
     ap.add_argument("--jobs", type=int, default=32)
     ap.add_argument("--rate", type=float, default=20.0)
@@ -694,6 +697,9 @@ def main() -> None:
     ap.add_argument("--synthetic", action="store_true",
                     help="svd mode: random graded Hermitian PSD matrices instead of an annealed state")
     args = ap.parse_args()
+    # every Annealer of this process (run_qa, the job server, the modes below) tunes its BP
+    # message kernels unless --autotune 0
+    os.environ["BQA_GB300_AUTOTUNE"] = "1" if args.autotune else "0"
     logging.basicConfig(level=logging.ERROR)
     logging.getLogger("bqa_gb300").setLevel(logging.ERROR)
     if args.impl == "reference":

@@ -1,0 +1,213 @@
+"""Autotuner of the BP message kernels, per (degree, storage bond dim, precision, class size).
+
+A BP sweep (reference ``_run_bp``, src/bqa/state.py:105-113 with ``Tensor.pass_msgs``,
+src/bqa/backends.py:381-408) runs one message kernel per degree class.  Several kernels
+compute the same messages (up to rounding), and which is fastest depends on the degree, the
+bond dim and the number of nodes:
+
+* the sweep's form: two-stage (every node writes its open-bond blocks P_0, P_1 to scratch,
+  then one pass forms the messages) or one-stage (every node writes its messages);
+* per class, within a form: the register-tiled kernel (half-node CTAs in the two-stage form,
+  whole-node CTAs in the one-stage form; complex64, degree 2-4, bond dims 4/8/12/16) or the
+  generic shared-memory kernel (global-memory form for nodes beyond shared memory).
+
+``tune(annealer)`` times every candidate of every class on the job's live state (CUDA events
+on the job's stream, a warm-up launch then ``reps`` timed launches, each reading the current
+messages and writing the idle message buffer, so the job's state is untouched), keeps the
+fastest per class and form, then times the two complete sweeps and keeps the faster form.
+Results are cached per process by (device, precision, degree, bond dim, class size rounded up
+to a power of two), and optionally in a JSON file named by the environment variable
+BQA_GB300_TUNE_CACHE, so a job pays for tuning only at (degree, bond dim) pairs no earlier job
+of its size class has seen.  The engine applies a plan through ``bqa_job.sweep_variants``
+(one row per bond dim) and ``bqa_bp_sweep_plan``.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import threading
+from dataclasses import dataclass, field
+
+from . import _lib
+
+VARIANT_NAMES = {_lib.BQA_VARIANT_DEFAULT: "default", _lib.BQA_VARIANT_TILED: "tiled",
+                 _lib.BQA_VARIANT_GENERIC: "generic"}
+
+_LOCK = threading.Lock()
+_CLASS_CACHE: dict[tuple, dict] = {}     # class key -> {"best": variant, "ms": {variant: ms}}
+_FORM_CACHE: dict[tuple, dict] = {}      # job key -> {"split": bool, "ms": {"split": ms, "whole": ms}}
+_LOADED = False
+
+
+@dataclass
+class Plan:
+    """What the tuner chose for one job at one storage bond dim."""
+    chis: int
+    split: bool                                   # two-stage sweeps
+    variants: list[int]                           # per engine class
+    class_ms: list[dict] = field(default_factory=list)
+    form_ms: dict = field(default_factory=dict)
+
+    def describe(self) -> dict:
+        return {"chi": self.chis, "form": "two-stage" if self.split else "one-stage",
+                "variants": [VARIANT_NAMES[v] for v in self.variants],
+                "class_ms": [{VARIANT_NAMES[int(k)]: round(v, 4) for k, v in m.items()} for m in self.class_ms],
+                "form_ms": {k: (round(v, 4) if v is not None else None) for k, v in self.form_ms.items()}}
+
+
+def _tuplify(x):
+    return tuple(_tuplify(y) for y in x) if isinstance(x, (list, tuple)) else x
+
+
+def _bucket(count: int) -> int:
+    return 1 << max(0, int(count - 1).bit_length())
+
+
+def _cache_path() -> str | None:
+    return os.environ.get("BQA_GB300_TUNE_CACHE") or None
+
+
+def _load() -> None:
+    global _LOADED
+    if _LOADED:
+        return
+    _LOADED = True
+    path = _cache_path()
+    if not path or not os.path.exists(path):
+        return
+    try:
+        with open(path) as f:
+            data = json.load(f)
+        for k, v in data.get("classes", []):
+            _CLASS_CACHE[_tuplify(k)] = {"best": int(v["best"]), "ms": {int(a): float(b) for a, b in v["ms"].items()}}
+        for k, v in data.get("forms", []):
+            _FORM_CACHE[_tuplify(k)] = {"split": bool(v["split"]), "ms": dict(v["ms"])}
+    except (OSError, ValueError, KeyError, TypeError):
+        pass   # a stale or foreign cache file is ignored, never fatal
+
+
+def _save() -> None:
+    path = _cache_path()
+    if not path:
+        return
+    data = {"classes": [[k, {"best": v["best"], "ms": {str(a): b for a, b in v["ms"].items()}}]
+                        for k, v in _CLASS_CACHE.items()],
+            "forms": [[k, v] for k, v in _FORM_CACHE.items()]}
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f)
+    os.replace(tmp, path)
+
+
+def clear_cache() -> None:
+    """Forget every tuning result of this process (the JSON file is left as it is)."""
+    with _LOCK:
+        _CLASS_CACHE.clear()
+        _FORM_CACHE.clear()
+        _PLAN_CACHE.clear()
+
+
+class _Timer:
+    """Times launches of one job's sweeps with CUDA events on the job's stream."""
+
+    def __init__(self, job, reps: int):
+        self.job = job
+        self.reps = max(1, int(reps))
+        torch = job.torch
+        self.dist = torch.zeros(2, dtype=torch.int64, device=job.device)
+
+    def sweep(self, classes, variants, split: bool) -> None:
+        job = self.job
+        arr = (ctypes.c_int32 * len(variants))(*variants)
+        job.lib.call("bqa_bp_sweep_plan", classes, len(variants), job.chis, job.dtype, arr,
+                     job.msgs[job.mcur].data_ptr(), job.msgs[1 - job.mcur].data_ptr(),
+                     job.lu.data_ptr() if split else None, job.E, self.dist.data_ptr(), None, job.stream)
+
+    def time(self, classes, variants, split: bool) -> float | None:
+        """Mean milliseconds of one sweep, or None when a variant does not exist for a class."""
+        torch = self.job.torch
+        try:
+            self.sweep(classes, variants, split)       # warm-up (also opts kernels into shared memory)
+        except _lib.BqaError:
+            return None
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(self.reps):
+            self.sweep(classes, variants, split)
+        ev1.record()
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / self.reps
+
+
+_DEVICE_NAMES: dict = {}
+_PLAN_CACHE: dict[tuple, Plan] = {}      # job key -> finished plan (fast path for repeated jobs)
+
+
+def _device_name(job) -> str:
+    idx = job.device.index if job.device.index is not None else job.torch.cuda.current_device()
+    name = _DEVICE_NAMES.get(idx)
+    if name is None:
+        name = _DEVICE_NAMES[idx] = job.torch.cuda.get_device_name(idx)
+    return name
+
+
+def tune(job, reps: int = 3) -> Plan:
+    """Choose the sweep form and each class's message kernel for ``job`` at its current storage
+    bond dim (``job.chis``), timing candidates on its live state.  The job's tensors, current
+    messages and loop state are not modified."""
+    with _LOCK:
+        _load()
+    dev = _device_name(job)
+    chis = job.chis
+    jkey = (dev, job.precision, chis, tuple((c.degree, _bucket(c.count)) for c in job.classes))
+    with _LOCK:
+        done = _PLAN_CACHE.get(jkey)
+    if done is not None:
+        return Plan(chis=chis, split=done.split, variants=list(done.variants), class_ms=done.class_ms,
+                    form_ms=done.form_ms)
+    torch = job.torch
+    classes = job._class_array()
+    active = [i for i, c in enumerate(job.classes) if c.degree > 0 and c.count > 0]
+    timer = None
+    best: dict[bool, list[int]] = {}
+    class_ms: list[dict] = [dict() for _ in job.classes]
+    with torch.cuda.device(job.device):
+        for split in (True, False):
+            picks = [_lib.BQA_VARIANT_DEFAULT] * len(job.classes)
+            for i in active:
+                c = job.classes[i]
+                key = (dev, job.precision, c.degree, chis, _bucket(c.count), split)
+                with _LOCK:
+                    hit = _CLASS_CACHE.get(key)
+                if hit is None:
+                    timer = timer or _Timer(job, reps)
+                    one = (_lib.BqaClass * 1)(classes[i])
+                    ms = {}
+                    for v in (_lib.BQA_VARIANT_TILED, _lib.BQA_VARIANT_GENERIC):
+                        t = timer.time(one, [v], split)
+                        if t is not None:
+                            ms[v] = t
+                    hit = {"best": min(ms, key=ms.get) if ms else _lib.BQA_VARIANT_DEFAULT, "ms": ms}
+                    with _LOCK:
+                        _CLASS_CACHE[key] = hit
+                picks[i] = hit["best"]
+                class_ms[i].update({(v if not split else v + 10): t for v, t in hit["ms"].items()})
+            best[split] = picks
+        with _LOCK:
+            form = _FORM_CACHE.get(jkey)
+        if form is None:
+            timer = timer or _Timer(job, reps)
+            ms = {"split": timer.time(classes, best[True], True), "whole": timer.time(classes, best[False], False)}
+            inf = float("inf")
+            form = {"split": (ms["split"] or inf) <= (ms["whole"] or inf), "ms": ms}
+            with _LOCK:
+                _FORM_CACHE[jkey] = form
+                _save()
+    split = bool(form["split"])
+    per_class = [{k % 10: v for k, v in m.items() if (k >= 10) == split} for m in class_ms]
+    plan = Plan(chis=chis, split=split, variants=best[split], class_ms=per_class, form_ms=dict(form["ms"]))
+    with _LOCK:
+        _PLAN_CACHE[jkey] = plan
+    return plan

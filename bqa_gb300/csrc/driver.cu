@@ -106,10 +106,12 @@ static int gate_layer(bqa_job* j, double xtime, double ztime, bqa_layer_info* in
 
 // One sweep of the job's BP loop: the tuned per-class kernels when the job carries a plan.
 static int job_sweep(bqa_job* j, void* a, void* b, void* s) {
-    if (j->sweep_variants)
-        return bqa_bp_sweep_plan(j->classes, j->n_classes, j->chis, j->dtype,
-                                 j->sweep_variants + (size_t)j->chis * j->n_classes, a, b,
-                                 j->split_sweeps ? j->lu : nullptr, j->edges, j->dist_parts, j->loop_state, s);
+    if (j->sweep_variants) {
+        const int32_t* row = j->sweep_variants + (size_t)j->chis * (j->n_classes + 1);
+        const bool two_stage = row[0] == 0 ? j->split_sweeps != 0 : row[0] == 1;
+        return bqa_bp_sweep_plan(j->classes, j->n_classes, j->chis, j->dtype, row + 1, a, b,
+                                 two_stage ? j->lu : nullptr, j->edges, j->dist_parts, j->loop_state, s);
+    }
     if (j->split_sweeps)
         return bqa_bp_sweep_split(j->classes, j->n_classes, j->chis, j->dtype, a, b, j->lu, j->edges, j->dist_parts,
                                   j->loop_state, s);
@@ -229,10 +231,12 @@ static std::vector<uint64_t> bp_graph_key(const bqa_job* j) {
                                bits_of(j->damping), (uint64_t)(uintptr_t)j->msgs[0], (uint64_t)(uintptr_t)j->msgs[1],
                                (uint64_t)(uintptr_t)j->lu, (uint64_t)(uintptr_t)j->dist_parts,
                                (uint64_t)(uintptr_t)j->loop_state, (uint64_t)j->n_classes};
+    if (j->sweep_variants)
+        for (int c = 0; c <= j->n_classes; ++c)
+            k.push_back((uint64_t)(1 + j->sweep_variants[(size_t)j->chis * (j->n_classes + 1) + c]));
     for (int c = 0; c < j->n_classes; ++c) {
         const bqa_class& x = j->classes[c];
         const void* p[] = {x.node_ids, x.in_pos, x.out_pos, x.lmbd_pos, x.edge_ampl, x.node_ampl, x.tensor, x.scratch};
-        k.push_back(j->sweep_variants ? (uint64_t)(1 + j->sweep_variants[j->chis * j->n_classes + c]) : 0);
         k.push_back((uint64_t)x.degree);
         k.push_back((uint64_t)x.count);
         k.push_back((uint64_t)x.scratch_elems);

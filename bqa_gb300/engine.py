@@ -73,7 +73,8 @@ class Annealer:
     """One annealing job resident on one GPU."""
 
     def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4,
-                 pad_bonds: bool | None = None, native: bool = True, graphs: bool | None = None):
+                 pad_bonds: bool | None = None, native: bool = True, graphs: bool | None = None,
+                 autotune: bool | None = None):
         import torch
         self.torch = torch
         if not torch.cuda.is_available():
@@ -95,6 +96,14 @@ class Annealer:
             graphs = os.environ.get("BQA_GB300_GRAPHS", "1") != "0"
         self.graphs = bool(graphs)
         self._graph_cache = None
+        # per-(degree, bond dim) choice of the BP message kernels (autotune.py) when autotune=True or
+        # the environment variable BQA_GB300_AUTOTUNE=1; the plan of bond dim chis is row chis of
+        # the table handed to the native driver (entry 0 the sweep form, then one entry per class)
+        if autotune is None:
+            import os
+            autotune = os.environ.get("BQA_GB300_AUTOTUNE", "0") == "1"
+        self.autotune = bool(autotune)
+        self.plans: dict = {}
         self.device = torch.device(device if device is not None else "cuda")
         self.bp_check_every = max(1, int(bp_check_every))
         E = ctx.edges_number
@@ -158,6 +167,7 @@ class Annealer:
         self.rho = torch.empty(ctx.nodes_number * 4, dtype=cplx, device=dev)
         self.zz = torch.empty(self.half, dtype=torch.float64, device=dev)
         self.norm2 = torch.zeros(1, dtype=torch.float64, device=dev)
+        self._plan_table = (ctypes.c_int32 * (33 * (len(self.classes) + 1)))()
         self.rng = np.random.default_rng(ctx.seed)
         self.stats: list[dict] = []
         self._events: list | None = None
@@ -376,12 +386,35 @@ class Annealer:
     def run_layer(self, xtime: float, ztime: float) -> dict:
         """One annealing step (src/bqa/state.py:315-321)."""
         if self.native and self._events is None:
-            return self._run_layer_native(float(xtime), float(ztime))
-        dim, err = self.gate_layer(xtime, ztime)
-        sweeps = self.run_bp()
-        info = {"bond_dim": dim, "trunc_err": err, "sweeps": sweeps}
-        self.stats.append(info)
+            info = self._run_layer_native(float(xtime), float(ztime))
+        else:
+            dim, err = self.gate_layer(xtime, ztime)
+            sweeps = self.run_bp()
+            info = {"bond_dim": dim, "trunc_err": err, "sweeps": sweeps}
+            self.stats.append(info)
+        if self.autotune and self.chis not in self.plans:
+            self.tune()
         return info
+
+    def tune(self):
+        """Time the BP message-kernel candidates at the current bond dim on the live state and
+        use the fastest from the next sweep on (autotune.tune); returns the plan."""
+        from . import autotune
+        plan = autotune.tune(self)
+        self.plans[self.chis] = plan
+        row = self.chis * (len(self.classes) + 1)
+        self._plan_table[row] = 1 if plan.split else 2
+        for i, v in enumerate(plan.variants):
+            self._plan_table[row + 1 + i] = int(v)
+        return plan
+
+    def _plan_row(self):
+        """(two-stage?, variants array) of the current bond dim's plan, or None."""
+        if self.chis not in self.plans:
+            return None
+        row = self.chis * (len(self.classes) + 1)
+        arr = (ctypes.c_int32 * len(self.classes)).from_buffer(self._plan_table, 4 * (row + 1))
+        return self._plan_table[row] == 1, arr
 
     def _job_struct(self):
         ctx = self.ctx
@@ -399,6 +432,8 @@ class Annealer:
         j.ext, j.lu, j.ul, j.lmbds = _ptr(self.ext), _ptr(self.lu), _ptr(self.ul), _ptr(self.lmbds)
         j.colmax, j.dist_parts = _ptr(self.colmax), _ptr(self.dist_parts)
         j.loop_state, j.status, j.edge_j = _ptr(self.loop_state), _ptr(self.status), _ptr(self.edge_j)
+        if self.plans:
+            j.sweep_variants = ctypes.cast(self._plan_table, ctypes.POINTER(ctypes.c_int32))
         return j, cls
 
     def _run_layer_native(self, xtime: float, ztime: float) -> dict:
@@ -441,9 +476,14 @@ class Annealer:
         eps, damp = float(ctx.bp_eps), float(ctx.damping)
         flops, nbytes = self.bp_sweep_cost()
         first = len(self._events) if self._events is not None else 0
+        plan = self._plan_row()
         while True:
             for _ in range(min(self.bp_check_every, ctx.max_bp_iters_number - launched)):
-                if self.split_sweeps:
+                if plan is not None:
+                    self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep_plan", cls, len(self.classes),
+                                 self.chis, self.dtype, plan[1], _ptr(a), _ptr(b), _ptr(self.lu) if plan[0] else None,
+                                 self.E, _ptr(self.dist_parts), _ptr(self.loop_state), st)
+                elif self.split_sweeps:
                     # open-bond blocks into the idle simple-update scratch, then the messages
                     self._launch("bp_sweep", flops, nbytes, lib.call, "bqa_bp_sweep_split", cls, len(self.classes),
                                  self.chis, self.dtype, _ptr(a), _ptr(b), _ptr(self.lu), self.E,

@@ -103,8 +103,10 @@ typedef struct bqa_job {
     int32_t* loop_state;       /* 8 x int32 */
     int32_t* status;           /* 1 x int32 */
     const double* edge_j;      /* [E/2] couplings (two-stage extended messages) */
-    const int32_t* sweep_variants; /* host [33][n_classes] or NULL: row chis holds each class's BQA_VARIANT_*
-                                      for BP sweeps at storage bond dim chis (bqa_bp_sweep_plan) */
+    const int32_t* sweep_variants; /* host [33][n_classes + 1] or NULL (sweeps as split_sweeps says).  Row chis
+                                      plans the BP sweeps at storage bond dim chis (bqa_bp_sweep_plan): entry 0
+                                      the form (0: as split_sweeps, 1: two-stage, 2: one-stage), entry 1 + c
+                                      class c's BQA_VARIANT_*.  Extended messages keep split_sweeps. */
 } bqa_job;
 
 /* What one step did. */
