@@ -44,7 +44,10 @@ SAMPLE_N = 200
 
 # executed / algorithmic FLOPs of the degree-3 message kernels: the shape-specialised schedule
 # (3 products + 3 closing contractions) against the reference order (6 + 3)
-EXECUTED_FRACTION = {4: 6 / 9, 8: 6 / 9, 12: 6 / 9, 16: 6 / 9}
+# Executed share of the reference order's FLOPs in the degree-3 half-node sweep: 3 bond products
+# and 3 closing contractions (Hermitian split) instead of 6 + 3, each closing contraction forming
+# only the NG (NG + 1) / 2 upper 4x4 tiles of its NG x NG tile grid (NG = chi / 4).
+EXECUTED_FRACTION = {c: (3 + 3 * ((c // 4) * (c // 4 + 1) / 2) / (c // 4) ** 2) / 9 for c in (4, 8, 12, 16)}
 
 # DRAM bytes one chi-16 degree-3 BP sweep moves per node: ncu capture of a 10k-node sweep,
 # tiled_half_kernel<3,16> 829.2 MB + bp_combine_kernel 224.9 MB (the work is per node).
@@ -327,7 +330,7 @@ def run_gpu_arm(args) -> None:
                      "algorithmic_bytes_per_launch": bp_bytes / max(len(sweep_ev), 1),
                      "algorithmic_flops_per_launch": bp_flops / max(len(sweep_ev), 1),
                      "note": "complex64 SIMT contraction: 16 d^2 chi^(d+1) FLOP per node per sweep "
-                             "(reference order; the kernel executes 2/3 of them at degree 3); the FP32 "
+                             "(reference order; the kernel executes 54% of them at degree 3, chi 16); the FP32 "
                              "CUDA-core peak, measured below, is the ceiling of this kernel",
                      "fp32_simt": {"peak_measured": fp32_peak, "unit": "TFLOP/s",
                                    "achieved_executed": achieved * EXECUTED_FRACTION.get(args.chi, 1.0),

@@ -199,6 +199,10 @@ template <int W> struct QrStride {
     static constexpr int BLOCK = VStride<W>::BLOCK + H + W;
 };
 template <int W> __device__ __forceinline__ int qr_off(int k) { return k * W - (k * (k - 1)) / 2; }
+// Column remainders at or below this norm count as zero (|x| (|x| + |x_k|) stays a normal number).
+template <typename R> __device__ __forceinline__ R qr_tiny();
+template <> __device__ __forceinline__ float qr_tiny<float>() { return 1e-18f; }
+template <> __device__ __forceinline__ double qr_tiny<double>() { return 1e-150; }
 
 // a_k = this lane's element k (k a runtime index)
 template <int W, typename C>
@@ -237,22 +241,26 @@ __device__ __forceinline__ void qr_precondition(typename Cx<R>::T (&a)[W], typen
         }
         C* u = sH + qr_off<W>(k);     // u[i - k], i = k..W-1
         if (lane == bl) {
-            // x = column rows k..: alpha = -phase(x_k) |x|, u = x - alpha e_k, tau = 2 / |u|^2
+            // x = column rows k..: alpha = -phase(x_k) |x|, u = (x - alpha e_k) / sqrt(|x| (|x| + |x_k|)),
+            // so |u|^2 = 2 and H = I - u u^H (tau = 1).  A remainder below qr_tiny is dropped (tau = 0,
+            // the column zeroed): the Jacobi would treat it as noise, and its reflector scale would
+            // overflow.
             const R xn = sqrt(t);
             const C xk = pick<W>(a, k);
             const R ak = sqrt(c_abs2(xk));
             const C ph = ak > R(0) ? c_scale(xk, R(1) / ak) : c_make(R(1), R(0));
-            const R tau = xn > R(0) ? R(1) / (xn * (xn + ak)) : R(0);
+            const bool keep = xn > qr_tiny<R>();
+            const R scale = keep ? R(1) / sqrt(xn * (xn + ak)) : R(0);
 #pragma unroll
             for (int i = 0; i < W; ++i)
-                if (i > k) u[i - k] = a[i];
-            u[0] = c_scale(ph, ak + xn);
-            sTau[k] = tau;
+                if (i > k) u[i - k] = c_scale(a[i], scale);
+            u[0] = c_scale(ph, (ak + xn) * scale);
+            sTau[k] = keep ? R(1) : R(0);
             // the pivot column becomes alpha e_k
 #pragma unroll
             for (int i = 0; i < W; ++i)
                 if (i > k) a[i] = c_zero<C>();
-            const C alpha = c_scale(ph, -xn);
+            const C alpha = keep ? c_scale(ph, -xn) : c_zero<C>();
 #pragma unroll
             for (int i = 0; i < W; ++i)
                 if (i == k) a[i] = alpha;

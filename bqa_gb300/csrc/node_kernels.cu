@@ -669,11 +669,10 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         __syncthreads();
     };
     auto emit = [&](int idx, const float2* X, const float2* R) {
-        tiled::close_tiled<CHI, TH, S::KS, PS, SW, 1>(X, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
+        tiled::close_tiled<CHI, TH, S::KS, PS, SW, 1, true>(X, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
         __syncthreads();
         float4* og = reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2);
-        const float4* sp = reinterpret_cast<const float4*>(sP);
-        for (int i = threadIdx.x; i < N2 / 2; i += TH) og[i] = sp[i];
+        tiled::write_half_block<CHI, TH>(sP, og);
         __syncthreads();
     };
     if constexpr (SPEC) {
@@ -683,8 +682,7 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
             q::close<IDX>(X, R, sP);
             __syncthreads();
             float4* og = reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + IDX] * 2 + s) * N2);
-            const float4* sp = reinterpret_cast<const float4*>(sP);
-            for (int i = threadIdx.x; i < N2 / 2; i += TH) og[i] = sp[i];
+            tiled::write_half_block<CHI, TH>(sP, og);
             __syncthreads();
         };
         q::prod1(sT, sA, sMt + N2);

@@ -142,13 +142,17 @@ __device__ __forceinline__ void prod0_inplace(float2* X, const float2* __restric
     }
 }
 
-// P[a][b] = sum conj(X[..]) R[..] over every index but bond IDX; thread = (tile (ag, bg), K-slice ks)
+// P[a][b] = sum conj(X[..]) R[..] over every index but bond IDX; thread = (tile (ag, bg), K-slice ks).
+// P is Hermitian: the 10 tiles with ag <= bg (tiled::upper_tile order) run on warps 0-4, warps 5-7
+// have no closing work (the block's lower tiles are written as conjugates).
 template <int IDX>
 __device__ __forceinline__ void close(const float2* __restrict__ X, const float2* __restrict__ R,
                                       float2* __restrict__ P) {
     const int t = threadIdx.x;
     const int ks = t & 15, tile = t >> 4;
-    const int ag = tile >> 2, bg = tile & 3;
+    if (tile >= 10) return;
+    const int ag = tile < 4 ? 0 : (tile < 7 ? 1 : (tile < 9 ? 2 : 3));
+    const int bg = ag + tile - (ag == 0 ? 0 : (ag == 1 ? 4 : (ag == 2 ? 7 : 9)));
     const int b3 = ks >> 3;
     float2 acc[4][4];
     zero(acc);

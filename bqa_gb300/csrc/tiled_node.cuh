@@ -55,6 +55,9 @@ struct Shape {
 
 // One CTA per (node, physical index s): the two values of s never mix inside a message
 // contraction, so a node splits into two independent halves of half the shared memory.
+// The half-node blocks P_s are Hermitian (the message of one physical index), so the closing
+// contractions form only the 4x4 tiles on and above the diagonal (NG (NG + 1) / 2 of NG^2) and
+// the written block takes the tiles below it as conjugate transposes (write_half_block).
 template <int D, int CHI>
 struct HalfShape {
     static constexpr int PER_S = cpow(CHI, D);
@@ -62,7 +65,7 @@ struct HalfShape {
     static constexpr int PROD_TILES = (CHI / 4) * (cpow(CHI, D - 1) / 4 > 0 ? cpow(CHI, D - 1) / 4 : 1);
     static constexpr int R32 = ((PROD_TILES + 31) / 32) * 32;
     static constexpr int THREADS = R32 > 512 ? 512 : R32;
-    static constexpr int CLOSE_TILES = (CHI / 4) * (CHI / 4);
+    static constexpr int CLOSE_TILES = (CHI / 4) * (CHI / 4 + 1) / 2;
     static constexpr int KS_RAW = THREADS / CLOSE_TILES;
     static constexpr int KS = KS_RAW >= 32 ? 32 : (KS_RAW >= 16 ? 16 : (KS_RAW >= 8 ? 8 : (KS_RAW >= 4 ? 4 : (KS_RAW >= 2 ? 2 : 1))));
     static constexpr int SW = CHI == 16 ? 7 : (CHI == 8 ? 3 : 0);
@@ -257,17 +260,32 @@ __device__ __forceinline__ void reduce_tile(float2 (&acc)[4][4], int ks, bool ac
     }
 }
 
-template <int CHI, int THREADS, int KS, int PER_S, int SW, int NS = 2>
+// Tile k of the upper triangle (row-major, diagonal included) of an NG x NG tile grid.
+__device__ __forceinline__ void upper_tile(int k, int NG, int& ag, int& bg) {
+    ag = 0;
+    int rem = k;
+#pragma unroll 1
+    while (ag < NG - 1 && rem >= NG - ag) {
+        rem -= NG - ag;
+        ++ag;
+    }
+    bg = ag + rem;
+}
+
+// HERM (one physical index, NS = 1): only the tiles on and above the diagonal.
+template <int CHI, int THREADS, int KS, int PER_S, int SW, int NS = 2, bool HERM = false>
 __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const float2* __restrict__ Rt,
                                             float2* __restrict__ P, int Ax, int B) {
+    static_assert(!HERM || NS == 1, "Hermitian closing contractions are per physical index");
     constexpr int NG = CHI / 4;
-    constexpr int TILES = NS * NG * NG;
+    constexpr int TILES = HERM ? NG * (NG + 1) / 2 : NS * NG * NG;
     const int t = threadIdx.x;
     const int ks = t % KS;
     const int tile = t / KS;
     const bool active = tile < TILES;
-    const int s = active ? tile / (NG * NG) : 0;
-    const int ag = (tile / NG) % NG, bg = tile % NG;
+    const int s = (active && !HERM) ? tile / (NG * NG) : 0;
+    int ag = (tile / NG) % NG, bg = tile % NG;
+    if (HERM) upper_tile(active ? tile : 0, NG, ag, bg);
     float2 acc[4][4];
 #pragma unroll
     for (int u = 0; u < 4; ++u)
@@ -313,6 +331,22 @@ __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const 
     }
     // sum the KS slices (adjacent lanes)
     reduce_tile<KS, CHI>(acc, ks, active, P + (size_t)s * CHI * CHI, ag, bg);
+}
+
+// Copy a half-node block P (CHI x CHI, row-major, upper tiles valid) to global memory, the
+// tiles below the diagonal as conjugate transposes of those above.
+template <int CHI, int TH>
+__device__ __forceinline__ void write_half_block(const float2* __restrict__ P, float4* __restrict__ og) {
+    const float4* sp = reinterpret_cast<const float4*>(P);
+    for (int i = threadIdx.x; i < CHI * CHI / 2; i += TH) {
+        const int r = (2 * i) / CHI, c = (2 * i) % CHI;
+        if ((r >> 2) > (c >> 2)) {
+            const float2 x = P[c * CHI + r], y = P[(c + 1) * CHI + r];
+            og[i] = make_float4(x.x, -x.y, y.x, -y.y);
+        } else {
+            og[i] = sp[i];
+        }
+    }
 }
 
 }  // namespace tiled
