@@ -261,11 +261,14 @@ def run_gpu_arm(args) -> None:
     stream = torch.cuda.current_stream(dev)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clocks:
+        # profilers select the timed steps by this range (ncu --nvtx --nvtx-include "timed_steps/")
+        torch.cuda.nvtx.range_push("timed_steps")
         ev0.record(stream)
         for i in range(args.steps):
             job.run_layer(*step_at(s + i))
         ev1.record(stream)
         torch.cuda.synchronize(dev)
+        torch.cuda.nvtx.range_pop()
     barrier()
     ms = ev0.elapsed_time(ev1)
     s += args.steps

@@ -124,15 +124,23 @@ class _Timer:
                      job.msgs[job.mcur].data_ptr(), job.msgs[1 - job.mcur].data_ptr(),
                      job.lu.data_ptr() if split else None, job.E, self.dist.data_ptr(), None, job.stream)
 
-    def time(self, classes, variants, split: bool) -> float | None:
-        """Mean milliseconds of one sweep, or None when a variant does not exist for a class."""
+    def time(self, classes, variants, split: bool, best: float | None = None) -> float | None:
+        """Mean milliseconds of one sweep, or None when a variant does not exist for a class.  A
+        candidate whose warm-up launch already takes over 4x ``best`` is not timed further (its
+        warm-up time is returned)."""
         torch = self.job.torch
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
         try:
             self.sweep(classes, variants, split)       # warm-up (also opts kernels into shared memory)
         except _lib.BqaError:
             return None
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
+        ev1.record()
+        ev1.synchronize()
+        warm = ev0.elapsed_time(ev1)
+        if best is not None and warm > 4.0 * best:
+            return warm
         ev0.record()
         for _ in range(self.reps):
             self.sweep(classes, variants, split)
@@ -186,7 +194,7 @@ def tune(job, reps: int = 3) -> Plan:
                     one = (_lib.BqaClass * 1)(classes[i])
                     ms = {}
                     for v in (_lib.BQA_VARIANT_TILED, _lib.BQA_VARIANT_GENERIC):
-                        t = timer.time(one, [v], split)
+                        t = timer.time(one, [v], split, min(ms.values()) if ms else None)
                         if t is not None:
                             ms[v] = t
                     hit = {"best": min(ms, key=ms.get) if ms else _lib.BQA_VARIANT_DEFAULT, "ms": ms}
