@@ -83,6 +83,27 @@ def fp32_peak_tflops(lib, dev) -> float:
     return flops / (float(np.median(ts)) / 1e3) / 1e12
 
 
+def mma_peak_tflops(lib, dev, kind: int) -> float:
+    """Warp-level mma.sync throughput (bqa_mma_probe; kind 0 bf16 m16n8k16, 1 tf32 m16n8k8), 8
+    CTAs of 256 per SM, best of 5 timed launches after 1 untimed."""
+    import torch
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = 8 * sms, 2000
+    out = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    ts = []
+    for i in range(6):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        lib.call("bqa_mma_probe", kind, blocks, iters, out.data_ptr(), st.cuda_stream)
+        b.record(st)
+        torch.cuda.synchronize(dev)
+        if i >= 1:
+            ts.append(a.elapsed_time(b))
+    flops = 2.0 * 16 * 8 * (16 if kind == 0 else 8) * 8 * iters * blocks * 8
+    return flops / (min(ts) / 1e3) / 1e12
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling while the timed region runs."""
 
@@ -338,7 +359,10 @@ def run_gpu_arm(args) -> None:
                      "fp32_simt": {"peak_measured": fp32_peak, "unit": "TFLOP/s",
                                    "achieved_executed": achieved * EXECUTED_FRACTION.get(args.chi, 1.0),
                                    "frac": achieved * EXECUTED_FRACTION.get(args.chi, 1.0) / fp32_peak,
-                                   "probe": "bqa_fp32_fma_probe, 16 independent FMA chains per thread"}},
+                                   "probe": "bqa_fp32_fma_probe, 16 independent FMA chains per thread"},
+                     "legacy_mma_peaks_measured": {"bf16_m16n8k16": mma_peak_tflops(job.lib, dev, 0),
+                                                   "tf32_m16n8k8": mma_peak_tflops(job.lib, dev, 1),
+                                                   "unit": "TFLOP/s", "probe": "bqa_mma_probe"}},
         "e2e": {"value": world * args.steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 16,
                 "d2h_bytes_per_step": int(n_el * 4 * 8 + 2 * args.chi * 4 + 64),
                 "what": "Annealer.run_layer + bloch_vectors per step (host scalars in, all marginals out), "

@@ -91,6 +91,7 @@ SIGNATURES = {
     "bqa_canonicalize_noalloc": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_void_p]),
     "bqa_fp32_fma_probe": (c_int32, [c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_mma_probe": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p]),
     "bqa_run_layer": (c_int32, [POINTER(BqaJob), c_double, c_double, POINTER(BqaLayerInfo), c_void_p]),
     "bqa_graph_cache_create": (c_int32, [POINTER(c_void_p)]),
     "bqa_graph_cache_destroy": (c_int32, [c_void_p]),

@@ -85,8 +85,12 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) fro2 += __shfl_xor_sync(BQA_FULL_MASK, fro2, o, W);
     const R col_floor = fmax((R)W * jacobi_eps<R>() * jacobi_eps<R>() * fro2, sizeof(R) == 4 ? R(1e-30) : R(1e-280));
+    // a sweep whose significant rotations all had |gamma| < sqrt(tol) sqrt(alpha beta) leaves the
+    // pairs orthogonal to ~tol relative (the coupling it reintroduces is second order), so the
+    // loop also ends after such a sweep instead of running one more sweep that rotates nothing
+    const R big_tol = sqrt(tol);
     for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
-        int rotated = 0;
+        int rotated = 0, big = 0;
 #pragma unroll 1
         for (int r = 1; r < W; ++r) {
             const int partner = lane ^ r;
@@ -126,7 +130,9 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                     const R ex = g.x / gabs, ey = g.y / gabs;
                     wp = c_make(-sn * ex, sn * ey);
                     wq = c_make(sn * ex, sn * ey);
-                    rotated |= (alpha > col_floor && beta > col_floor);
+                    const bool sig = alpha > col_floor && beta > col_floor;
+                    rotated |= sig;
+                    big |= sig && gabs >= big_tol * sqrt(alpha) * sqrt(beta);
                 }
                 const C wown = low ? wp : wq;
 #pragma unroll
@@ -166,7 +172,7 @@ __device__ __forceinline__ bool jacobi_columns(typename Cx<R>::T (&a)[W], typena
                 __syncwarp();
             }
         }
-        if (!__any_sync(BQA_FULL_MASK, rotated)) return true;
+        if (!__any_sync(BQA_FULL_MASK, rotated) || !__any_sync(BQA_FULL_MASK, big)) return true;
     }
     return false;
 }
@@ -369,12 +375,18 @@ __global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>
 
 // Per undirected edge p: ker = lu[p] lu[p+h]^T = us s vhs; lambdas; canonicalisers
 // (src/bqa/state.py:171-200).
-template <int W, typename R>
+// QR: the Jacobi runs on the pivoted triangular factor of ker^H (qr_precondition): with
+// ker^H = Q R', R'^H = ker Q, and R'^H V_r = A (orthogonal columns) gives ker (Q V_r) = A, so
+// Q V_r are ker's right singular vectors and A = us s, the same roles as the direct form.  The
+// Householder vectors sit in the segment's staging block, idle between the ker product and
+// the canonicaliser products.
+template <int W, typename R, bool QR>
 __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>::T* __restrict__ lu,
                                                          const typename Cx<R>::T* __restrict__ ul, int edges, int n,
                                                          R eps, typename Cx<R>::T* __restrict__ canon,
                                                          R* __restrict__ lmbds, typename Cx<R>::Bits* colmax,
                                                          int32_t* status) {
+    static_assert(!QR || QrStride<W>::H + W <= W * W, "Householder vectors fit the staging block");
     using C = typename Cx<R>::T;
     extern __shared__ double4 smem_raw[];
     constexpr int VS = VStride<W>::VS;
@@ -387,15 +399,17 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
     const bool live = p < half;
     const int pf = live ? p : 0, pb = pf + half;
     const size_t nn = (size_t)n * n;
-    // stage lu_f, then ker[:, lane] = lu_f . lu_b[lane, :]^T
-    for (int i = lane; i < n * n; i += W) sm[i] = live ? lu[(size_t)pf * nn + i] : c_zero<C>();
+    // direct: stage lu_f, then ker[:, lane] = lu_f . lu_b[lane, :]^T
+    // QR: stage lu_b, then ker^H[:, lane] = conj(lu_b . lu_f[lane, :]^T)
+    const size_t staged = QR ? (size_t)pb : (size_t)pf, other = QR ? (size_t)pf : (size_t)pb;
+    for (int i = lane; i < n * n; i += W) sm[i] = live ? lu[staged * nn + i] : c_zero<C>();
     __syncwarp();
     C a[W];
     {
         C brow[W];
 #pragma unroll
         for (int k = 0; k < W; ++k)
-            brow[k] = (live && lane < n && k < n) ? lu[(size_t)pb * nn + (size_t)lane * n + k] : c_zero<C>();
+            brow[k] = (live && lane < n && k < n) ? lu[other * nn + (size_t)lane * n + k] : c_zero<C>();
 #pragma unroll
         for (int i = 0; i < W; ++i) {
             C acc = c_zero<C>();
@@ -404,8 +418,14 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
                 for (int k = 0; k < W; ++k)
                     if (k < n) acc = c_fma(sm[i * n + k], brow[k], acc);
             }
-            a[i] = acc;
+            a[i] = QR ? c_conj(acc) : acc;
         }
+    }
+    C* sH = sm;
+    R* sTau = reinterpret_cast<R*>(sm + QrStride<W>::H);
+    if constexpr (QR) {
+        __syncwarp();   // every lane has read the staged factor before the Householder vectors land there
+        qr_precondition<W, R>(a, sV, sH, sTau, lane);
     }
     const bool ok = jacobi_columns<W, R>(a, sV, lane);
     const C* v = sV + lane * VS;
@@ -414,6 +434,7 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
 #pragma unroll
     for (int i = 0; i < W; ++i) nrm2 += c_abs2(a[i]);
     const R sig = sqrt(nrm2);
+    if constexpr (QR) qr_apply_q<W, R>(sV, sH, sTau, lane);
     const R sk = (lane < n && sig > eps) ? sig : R(0);
     // descending rank among the segment's columns, ties by column index
     int rank = 0;
@@ -721,20 +742,38 @@ static int launch_env(const void* m, int count, int n, double eps, void* lu, voi
     return launch_env_k<W, R, false>(m, count, n, eps, lu, ul, status, st);
 }
 
-template <int W, typename R>
-static int launch_canon(const void* lu, const void* ul, int edges, int n, double eps, void* canon, void* lmbds,
-                        void* colmax, int32_t* status, cudaStream_t st) {
+template <int W, typename R, bool QR>
+static int launch_canon_k(const void* lu, const void* ul, int edges, int n, double eps, void* canon, void* lmbds,
+                          void* colmax, int32_t* status, cudaStream_t st) {
     using C = typename Cx<R>::T;
     const int per_block = 128 / W;
     const int half = edges / 2;
     const int blocks = (half + per_block - 1) / per_block;
     const size_t smem = ((size_t)128 * W + (size_t)(128 / W) * VStride<W>::BLOCK) * sizeof(C);
-    int rc = ensure_smem((const void*)bond_canon_kernel<W, R>, smem, "bond_canon");
+    int rc = ensure_smem((const void*)bond_canon_kernel<W, R, QR>, smem, "bond_canon");
     if (rc) return rc;
-    bond_canon_kernel<W, R><<<blocks, 128, smem, st>>>(static_cast<const C*>(lu), static_cast<const C*>(ul), edges, n,
-                                                       (R)eps, static_cast<C*>(canon), static_cast<R*>(lmbds),
-                                                       static_cast<typename Cx<R>::Bits*>(colmax), status);
+    bond_canon_kernel<W, R, QR><<<blocks, 128, smem, st>>>(static_cast<const C*>(lu), static_cast<const C*>(ul),
+                                                           edges, n, (R)eps, static_cast<C*>(canon),
+                                                           static_cast<R*>(lmbds),
+                                                           static_cast<typename Cx<R>::Bits*>(colmax), status);
     return check_launch("bond_canon");
+}
+
+// The bond canonicalisation's Jacobi works on ker^H's pivoted triangular factor when
+// BQA_GB300_CANON_QR=1 is set when the library loads (complex64, and complex128 up to 16
+// columns); by default it works on ker directly.
+static const bool g_canon_qr = [] {
+    const char* v = getenv("BQA_GB300_CANON_QR");
+    return v && v[0] == '1';
+}();
+
+template <int W, typename R>
+static int launch_canon(const void* lu, const void* ul, int edges, int n, double eps, void* canon, void* lmbds,
+                        void* colmax, int32_t* status, cudaStream_t st) {
+    if constexpr (sizeof(R) == 4 || W <= 16) {
+        if (g_canon_qr) return launch_canon_k<W, R, true>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
+    }
+    return launch_canon_k<W, R, false>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
 }
 
 template <typename R>

@@ -374,6 +374,16 @@ int32_t bqa_layout_class(int32_t degree, int32_t count, const int32_t* deg, cons
  */
 int32_t bqa_fp32_fma_probe(int32_t blocks, int32_t iters, float* out, void* stream);
 
+/*
+ * Warp-level tensor-core throughput probe (no reference counterpart; measurement only):
+ * `blocks` CTAs of 256 threads, every warp running 8 independent mma.sync accumulator chains
+ * for `iters` iterations on register operands -- kind 0: m16n8k16 bf16 inputs, f32
+ * accumulate (4096 FLOP per instruction); kind 1: m16n8k8 tf32 (2048 FLOP).  FLOPs =
+ * per-instruction FLOP * 8 * iters * blocks * 8; one float per thread goes to
+ * out[blocks * 256].  The legacy tensor path's ceiling, next to the FP32 one.
+ */
+int32_t bqa_mma_probe(int32_t kind, int32_t blocks, int32_t iters, float* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

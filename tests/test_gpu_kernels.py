@@ -314,3 +314,18 @@ def test_fp32_fma_probe_runs():
     assert torch.isfinite(out).all()
     tf = bench.fp32_peak_tflops(lib, torch.device("cuda"))
     assert 5.0 < tf < 500.0
+
+
+def test_mma_probe_runs():
+    """The warp-level MMA probe launches both kinds, writes every output, gives plausible rates."""
+    import bench
+    lib = _lib.load()
+    out = torch.full((152 * 256,), float("nan"), device="cuda")
+    for kind in (0, 1):
+        lib.call("bqa_mma_probe", kind, 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert torch.isfinite(out).all()
+    with pytest.raises(_lib.BqaError):
+        lib.call("bqa_mma_probe", 2, 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream)
+    for kind in (0, 1):
+        assert 10.0 < bench.mma_peak_tflops(lib, torch.device("cuda"), kind) < 5000.0
