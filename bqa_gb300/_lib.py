@@ -9,7 +9,7 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 8
+ABI_VERSION = 9
 BQA_C64 = 0
 BQA_C128 = 1
 BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC = 0, 1, 2
@@ -48,7 +48,7 @@ class BqaJob(ctypes.Structure):
         ("bp_eps", c_double), ("pinv_eps", c_double), ("damping", c_double),
         ("msgs", c_void_p * 2), ("ext", c_void_p), ("lu", c_void_p), ("ul", c_void_p), ("lmbds", c_void_p),
         ("colmax", c_void_p), ("dist_parts", c_void_p), ("loop_state", c_void_p), ("status", c_void_p),
-        ("edge_j", c_void_p), ("sweep_variants", POINTER(c_int32)),
+        ("edge_j", c_void_p), ("sweep_variants", POINTER(c_int32)), ("blocks_valid", c_int32),
     ]
 
 
@@ -75,6 +75,7 @@ SIGNATURES = {
     "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),
     "bqa_ext_msgs_split": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32,
                                      c_void_p, c_double, c_void_p, c_void_p]),
+    "bqa_ext_combine": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_double, c_void_p, c_void_p]),
     "bqa_env_factor": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
     "bqa_bond_canon": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,

@@ -35,6 +35,8 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes, int32_t n_classes, int32_t 
                            void* stream);
 int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, int32_t dtype, void* dist_parts,
                         int32_t* loop_state, double eps, double damping, int32_t max_iters, void* stream);
+int32_t bqa_ext_combine(const void* pm, int32_t edges, int32_t chi, int32_t dtype, const double* edge_j, double ztime,
+                        void* ext_out, void* stream);
 int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype,
                           const int32_t* variants, void* msgs_a, void* msgs_b, void* pm, int32_t edges,
                           void* dist_parts, const int32_t* loop_state, void* stream);
@@ -55,10 +57,14 @@ static int gate_layer(bqa_job* j, double xtime, double ztime, bqa_layer_info* in
     void* s = reinterpret_cast<void*>(st);
     void* msgs = j->msgs[j->mcur];
     int rc;
-    if (j->split_sweeps)
+    if (j->split_sweeps && j->blocks_valid)
+        // the converged BP run left the open-bond blocks of these messages in lu
+        rc = bqa_ext_combine(j->lu, E, chi, dt, j->edge_j, ztime, j->ext, s);
+    else if (j->split_sweeps)
         rc = bqa_ext_msgs_split(j->classes, j->n_classes, chi, dt, msgs, j->lu, E, j->edge_j, ztime, j->ext, s);
     else
         rc = bqa_ext_msgs(j->classes, j->n_classes, chi, dt, msgs, j->ext, ztime, s);
+    j->blocks_valid = 0;   // lu is overwritten by the environment factors below
     if (rc) return rc;
     if ((rc = bqa_env_factor(j->ext, E, n, dt, j->pinv_eps, j->lu, j->ul, j->status, s))) return rc;
     const size_t bits = dt == BQA_C64 ? 4 : 8;
@@ -104,6 +110,15 @@ static int gate_layer(bqa_job* j, double xtime, double ztime, bqa_layer_info* in
     return bqa_msgs_from_lmbds(j->lmbds, n, E, dims, dt, j->msgs[j->mcur], s);
 }
 
+// Whether the job's BP sweeps run in two stages (open-bond blocks in lu, then messages).
+static bool job_two_stage(const bqa_job* j) {
+    if (j->sweep_variants) {
+        const int32_t form = j->sweep_variants[(size_t)j->chis * (j->n_classes + 1)];
+        return form == 0 ? j->split_sweeps != 0 : form == 1;
+    }
+    return j->split_sweeps != 0;
+}
+
 // One sweep of the job's BP loop: the tuned per-class kernels when the job carries a plan.
 static int job_sweep(bqa_job* j, void* a, void* b, void* s) {
     if (j->sweep_variants) {
@@ -147,6 +162,8 @@ static int run_bp(bqa_job* j, bqa_layer_info* info, cudaStream_t st) {
             return set_error(BQA_ERR_UNSUPPORTED, "BP loop state did not finish after the iteration cap");
     }
     if (ls[2]) j->mcur = 1 - j->mcur;
+    // converged: the kept messages are the last sweep's input, whose blocks that sweep left in lu
+    j->blocks_valid = (!ls[3] && job_two_stage(j)) ? 1 : 0;
     info->sweeps = ls[1];
     info->bp_exhausted = ls[3];
     float best;
@@ -359,6 +376,7 @@ static int run_bp_graph(bqa_job* j, bqa_graph_cache* cache, bqa_layer_info* info
     std::memcpy(ls, cache->host_ls, sizeof(ls));
     if (!ls[0]) return set_error(BQA_ERR_UNSUPPORTED, "BP graph ended without a decision after %d sweeps", ls[1]);
     if (ls[2]) j->mcur = 1 - j->mcur;
+    j->blocks_valid = (!ls[3] && job_two_stage(j)) ? 1 : 0;
     info->sweeps = ls[1];
     info->bp_exhausted = ls[3];
     float best;

@@ -1234,13 +1234,23 @@ int32_t bqa_ext_msgs_split(const bqa_class* classes, int32_t n_classes, int32_t 
         rc = run_classes_dt(dtype, MODE_PSPLIT, &one, 1, chi, msgs, nullptr, pm, nullptr, nullptr, 0.0, st);
         if (rc) return rc;
     }
+    return bqa_ext_combine(pm, edges, chi, dtype, edge_j, ztime, ext_out, stream);
+}
+
+int32_t bqa_ext_combine(const void* pm, int32_t edges, int32_t chi, int32_t dtype, const double* edge_j, double ztime,
+                        void* ext_out, void* stream) {
+    if (!pm || !edge_j || !ext_out || chi < 1 || edges < 2 || edges % 2)
+        return set_error(BQA_ERR_ARG, "bqa_ext_combine: bad argument");
+    cudaStream_t st = as_stream(stream);
     const int blocks = (int)(((int64_t)edges * 32 + 255) / 256);
     if (dtype == BQA_C64)
         ext_combine_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float2*>(pm), edges, chi, edge_j, ztime,
                                                            static_cast<float2*>(ext_out));
-    else
+    else if (dtype == BQA_C128)
         ext_combine_kernel<double><<<blocks, 256, 0, st>>>(static_cast<const double2*>(pm), edges, chi, edge_j, ztime,
                                                             static_cast<double2*>(ext_out));
+    else
+        return set_error(BQA_ERR_ARG, "bqa_ext_combine: unknown dtype %d", dtype);
     return check_launch("ext_combine");
 }
 

@@ -74,7 +74,7 @@ class Annealer:
 
     def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4,
                  pad_bonds: bool | None = None, native: bool = True, graphs: bool | None = None,
-                 autotune: bool | None = None):
+                 autotune: bool | None = None, reuse_blocks: bool | None = None):
         import torch
         self.torch = torch
         if not torch.cuda.is_available():
@@ -104,6 +104,15 @@ class Annealer:
             autotune = os.environ.get("BQA_GB300_AUTOTUNE", "0") == "1"
         self.autotune = bool(autotune)
         self.plans: dict = {}
+        # A BP run that converged with two-stage sweeps leaves in lu the open-bond blocks of the
+        # messages it keeps (its last sweep's input); the next gate layer then forms the extended
+        # messages from them with one combine pass (off with reuse_blocks=False or
+        # BQA_GB300_REUSE_BLOCKS=0).  Anything that changes tensors, messages or lu clears it.
+        if reuse_blocks is None:
+            import os
+            reuse_blocks = os.environ.get("BQA_GB300_REUSE_BLOCKS", "1") != "0"
+        self.reuse_blocks = bool(reuse_blocks)
+        self.blocks_valid = False
         self.device = torch.device(device if device is not None else "cuda")
         self.bp_check_every = max(1, int(bp_check_every))
         E = ctx.edges_number
@@ -266,6 +275,7 @@ class Annealer:
         self.chi = self.chis = 1
         self.tcur = 0
         self.mcur = 0
+        self.blocks_valid = False
         init = self.torch.tensor([complex(INIT_STATE[0]), complex(INIT_STATE[1])], dtype=self.msgs[0].dtype,
                                  device=self.device)
         for c in self.classes:
@@ -284,6 +294,7 @@ class Annealer:
             raise ValueError("state bond dim exceeds max_bond_dim")
         chis = self._store(chi)
         self.chi, self.chis, self.tcur, self.mcur = chi, chis, 0, 0
+        self.blocks_valid = False
         for c in self.classes:
             t = np.asarray(degree_to_tensor[c.degree], dtype=self._np_cplx)
             if chis != chi:
@@ -315,6 +326,7 @@ class Annealer:
     def restore(self, snap: dict) -> None:
         self.chi, self.chis, self.lam_stride = snap["dims"]
         self.tcur, self.mcur = 0, 0
+        self.blocks_valid = False
         for c, t in zip(self.classes, snap["tensors"]):
             c.tensors[0][: t.numel()].copy_(t)
         self.msgs[0][: snap["msgs"].numel()].copy_(snap["msgs"])
@@ -347,7 +359,11 @@ class Annealer:
         eps = float(ctx.pinv_eps)
         cls = self._class_array()
         dt = self.dtype
-        if self.split_sweeps:
+        if self.split_sweeps and self.blocks_valid and self.reuse_blocks:
+            # the converged BP run left the open-bond blocks of these messages in lu
+            self._launch("ext_msgs", 0.0, 0.0, lib.call, "bqa_ext_combine", _ptr(self.lu), self.E, chi, dt,
+                         _ptr(self.edge_j), float(ztime), _ptr(self.ext), st)
+        elif self.split_sweeps:
             # half-node kernels write P_0, P_1 into lu (free until the environment factors)
             self._launch("ext_msgs", 0.0, 0.0, lib.call, "bqa_ext_msgs_split", cls, len(self.classes), chi, dt,
                          _ptr(self._msgs_cur()), _ptr(self.lu), self.E, _ptr(self.edge_j), float(ztime),
@@ -355,6 +371,7 @@ class Annealer:
         else:
             self._launch("ext_msgs", 0.0, 0.0, lib.call, "bqa_ext_msgs", cls, len(self.classes), chi, dt,
                          _ptr(self._msgs_cur()), _ptr(self.ext), float(ztime), st)
+        self.blocks_valid = False
         self._launch("env_factor", 0.0, 0.0, lib.call, "bqa_env_factor", _ptr(self.ext), self.E, n, dt, eps,
                      _ptr(self.lu), _ptr(self.ul), _ptr(self.status), st)
         self.colmax.zero_()
@@ -400,6 +417,7 @@ class Annealer:
         """Time the BP message-kernel candidates at the current bond dim on the live state and
         use the fastest from the next sweep on (autotune.tune); returns the plan."""
         from . import autotune
+        self.blocks_valid = False   # the candidate sweeps write lu
         plan = autotune.tune(self)
         self.plans[self.chis] = plan
         row = self.chis * (len(self.classes) + 1)
@@ -434,6 +452,7 @@ class Annealer:
         j.loop_state, j.status, j.edge_j = _ptr(self.loop_state), _ptr(self.status), _ptr(self.edge_j)
         if self.plans:
             j.sweep_variants = ctypes.cast(self._plan_table, ctypes.POINTER(ctypes.c_int32))
+        j.blocks_valid = int(self.blocks_valid and self.reuse_blocks)
         return j, cls
 
     def _run_layer_native(self, xtime: float, ztime: float) -> dict:
@@ -447,6 +466,7 @@ class Annealer:
         else:
             self.lib.call("bqa_run_layer", ctypes.byref(j), xtime, ztime, ctypes.byref(res), self.stream)
         self.chi, self.chis, self.lam_stride, self.mcur, self.tcur = j.chi, j.chis, j.lam_stride, j.mcur, j.tcur
+        self.blocks_valid = bool(j.blocks_valid)
         if res.svd_not_converged:
             log.warning("a Jacobi SVD of the truncation step hit its sweep cap")
         log.info(f"Truncation performed, per edge error upper bound: {res.trunc_err}")
@@ -507,6 +527,8 @@ class Annealer:
                 e[0] = "bp_sweep_skipped"
         if ls[2]:
             self.mcur = 1 - self.mcur
+        two_stage = plan[0] if plan is not None else self.split_sweeps
+        self.blocks_valid = not ls[3] and bool(two_stage)
         if ls[3]:
             best = np.array([ls[6]], dtype=np.int32).view(np.float32)[0]
             log.warning(f"BP algorithm exceeds iterations limit set to {ctx.max_bp_iters_number}, "
@@ -518,6 +540,7 @@ class Annealer:
         res = _lib.BqaLayerInfo()
         self.lib.call("bqa_run_bp_graph", ctypes.byref(j), self._graphs(), ctypes.byref(res), self.stream)
         self.mcur = j.mcur
+        self.blocks_valid = bool(j.blocks_valid)
         if res.bp_exhausted:
             log.warning(f"BP algorithm exceeds iterations limit set to {self.ctx.max_bp_iters_number}, "
                         f"obtained bp_eps {res.best_dist}")
@@ -540,6 +563,7 @@ class Annealer:
     def edge_zz(self) -> np.ndarray:
         """BP two-site <Z_u Z_v> per undirected edge (oracle ``edge_zz``)."""
         pm = self.lu   # scratch of the simple update, idle between steps
+        self.blocks_valid = False
         self.lib.call("bqa_psplit", self._class_array(), len(self.classes), self.chis, self.dtype,
                       _ptr(self._msgs_cur()), _ptr(pm), self.stream)
         self.lib.call("bqa_edge_zz", _ptr(pm), self.E, self.chis, self.dtype, _ptr(self.zz), self.stream)
@@ -564,6 +588,7 @@ class Annealer:
     def _project(self, nodes, outcomes) -> None:
         """Project nodes onto outcomes (0: |0>, 1: |1>), then renormalise each touched class."""
         ctx = self.ctx
+        self.blocks_valid = False
         nodes = np.asarray(nodes, dtype=np.int64)
         outcomes = np.asarray(outcomes, dtype=np.int64)
         deg = ctx.node_degree[nodes]

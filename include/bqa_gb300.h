@@ -107,6 +107,10 @@ typedef struct bqa_job {
                                       plans the BP sweeps at storage bond dim chis (bqa_bp_sweep_plan): entry 0
                                       the form (0: as split_sweeps, 1: two-stage, 2: one-stage), entry 1 + c
                                       class c's BQA_VARIANT_*.  Extended messages keep split_sweeps. */
+    int32_t blocks_valid;      /* state: lu holds the open-bond blocks of the current messages and tensors
+                                  (set by a BP run that converged with two-stage sweeps; the next gate
+                                  layer then forms its extended messages with bqa_ext_combine alone and
+                                  clears it).  Set it to 0 after changing tensors or messages. */
 } bqa_job;
 
 /* What one step did. */
@@ -249,6 +253,16 @@ int32_t bqa_ext_msgs(const bqa_class* classes, int32_t n_classes, int32_t chi, i
  */
 int32_t bqa_ext_msgs_split(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype, const void* msgs,
                            void* pm, int32_t edges, const double* edge_j, double ztime, void* ext_out, void* stream);
+
+/*
+ * The second stage of bqa_ext_msgs_split alone: extended messages from open-bond blocks
+ * pm[edges][2][chi][chi] that are already in place.  A BP run that stopped on convergence
+ * keeps its last sweep's input messages (src/bqa/state.py:118-120), and a two-stage sweep
+ * leaves in pm the blocks of exactly those messages and the current tensors, so the next
+ * step's extended messages need only this pass (bqa_job.blocks_valid).
+ */
+int32_t bqa_ext_combine(const void* pm, int32_t edges, int32_t chi, int32_t dtype, const double* edge_j, double ztime,
+                        void* ext_out, void* stream);
 
 /*
  * Environment factors of every (extended) message m = U S Vh, singular values <= eps

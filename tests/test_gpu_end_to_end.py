@@ -198,6 +198,33 @@ def test_graph_bp_equals_native_step(name, precision):
     assert np.array_equal(jobs[0].bloch_vectors(), jobs[1].bloch_vectors())
 
 
+@pytest.mark.parametrize("name,graphs", [("rr3_n16_chi4", True), ("grid3x4_chi4_damped", True),
+                                         ("rr3_n24_chi8", False), ("mixed_n18_chi3", True)])
+def test_reused_blocks_equal_recomputed(name, graphs):
+    """Extended messages formed from the open-bond blocks a converged BP run left in lu (one
+    combine pass) equal those recomputed by the half-node kernels: identical state every step,
+    including damped runs whose BP exhausts (those recompute)."""
+    from bqa_gb300.engine import Annealer
+    from bqa_gb300.layout import build_context
+    ctx = build_context(gc.config(name))
+    steps = [i for i in ctx.instructions if isinstance(i, dict)][:10]
+    jobs = [Annealer(ctx, graphs=graphs, reuse_blocks=r) for r in (True, False)]
+    reused = 0
+    for ins in steps:
+        reused += int(jobs[0].blocks_valid)
+        for job in jobs:
+            job.run_layer(ins["xtime"], ins["ztime"])
+        (t1, m1, l1), (t2, m2, l2) = (j.get_state() for j in jobs)
+        assert np.array_equal(m1, m2) and np.array_equal(l1, l2)
+        for d in t1:
+            assert np.array_equal(t1[d], t2[d])
+    assert jobs[0].stats == jobs[1].stats
+    assert reused > 0
+    # a read-out that writes lu in between clears the flag
+    jobs[0].edge_zz()
+    assert not jobs[0].blocks_valid
+
+
 def test_graph_measurement_matches_oracle():
     """The measurement loop (two BP runs per draw) on graph-replayed BP: outcomes equal the
     reference's recorded ones."""
