@@ -296,8 +296,7 @@ __device__ __forceinline__ void qr_precondition(typename Cx<R>::T (&a)[W], typen
     __syncwarp();
 }
 
-// Column `lane` of sV (V_r after the Jacobi) <- Q V_r = H_0 H_1 ... H_{W-1} V_r, Q from the last
-// qr_precondition.
+// Column `lane` of sV (V_r after the Jacobi) <- Q V_r = H_0 H_1 ... H_{W-1} V_r.
 template <int W, typename R>
 __device__ __forceinline__ void qr_apply_q(typename Cx<R>::T* sV, const typename Cx<R>::T* sH, const R* sTau,
                                            int lane) {
@@ -350,12 +349,9 @@ __global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>
     C a[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) a[i] = (live && i < n && lane < n) ? mats[base + (size_t)i * n + lane] : c_zero<C>();
-    if constexpr (QR) {
-        // two passes: m = Q1 R1, then R1^H = Q2 R2 (lanes hold R2^H); the Jacobi on R2^H = Q1^H m Q2
-        // gives m (Q2 V) = Q1 A, so only the second pass's reflectors are kept for the eigenvectors
-#pragma unroll 1
-        for (int pass = 0; pass < 2; ++pass) qr_precondition<W, R>(a, sV, sH, sTau, lane);
-    }
+    // (a second pass, R1^H = Q2 R2 with the Jacobi on R2^H, saves about one more sweep in the
+    // float32 model but measured slower on GB300: 61.4 -> 72.4 ms per 100k-node step)
+    if constexpr (QR) qr_precondition<W, R>(a, sV, sH, sTau, lane);
     const bool ok = jacobi_columns<W, R>(a, sV, lane);
     const C* v = sV + lane * VS;
     if (!ok && live && lane == 0) atomicOr(status, BQA_STATUS_SVD_NOT_CONVERGED);
