@@ -34,7 +34,9 @@ def test_complex128_matches_reference(case, monkeypatch):
     conf, want = case
     got = _bloch(conf, "double", monkeypatch)
     assert got.shape == want.shape
-    assert np.abs(got - want).max() < 1e-8
+    err = np.abs(got - want).max()
+    print(f"complex128 vs reference: max Bloch error {err:.3e}")
+    assert err < 1e-8
 
 
 def test_complex64_within_bar(case, monkeypatch):
@@ -42,4 +44,6 @@ def test_complex64_within_bar(case, monkeypatch):
     conf, want = case
     got = _bloch(conf, "single", monkeypatch)
     err = np.abs(got - want).max()
+    print(f"complex64 vs reference: max Bloch error {err:.3e}, mean |<Z> error| "
+          f"{np.abs(got[:, 2] - want[:, 2]).mean():.3e}")
     assert err < 5e-4, err

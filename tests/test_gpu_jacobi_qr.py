@@ -86,3 +86,38 @@ def test_qr_preconditioned_env_factors_match_fp64(tmp_path):
         assert r["same"] >= 0.99
         assert r["pmax"] < 5e-3
     assert q["pmed"] <= 1.5 * d["pmed"] + 1e-7
+
+
+def test_qr_env_factors_with_negligible_columns_stay_finite():
+    """Hermitian PSD matrices whose spectra include directions of size ~1e-20 next to O(1)
+    ones (column remainders far below float32 resolution, the case whose Householder scale
+    once overflowed): the factors stay finite and rebuild the masked matrix."""
+    import torch
+    from bqa_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(3)
+    count, n = 256, 32
+    q, _ = np.linalg.qr(rng.normal(size=(count, n, n)) + 1j * rng.normal(size=(count, n, n)))
+    lam = np.concatenate([np.sort(rng.uniform(1e-3, 1.0, size=(count, 12)))[:, ::-1],
+                          np.full((count, 8), 1e-8), np.full((count, 12), 1e-20)], axis=1)
+    m = np.einsum("eik,ek,ejk->eij", q, lam, np.conj(q))
+    m /= np.trace(m, axis1=1, axis2=2).real[:, None, None]
+    m = m.astype(np.complex64)
+    dev = torch.device("cuda")
+    mt = torch.from_numpy(m.reshape(-1)).to(dev)
+    lu = torch.empty_like(mt)
+    ul = torch.empty_like(mt)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    lib.call("bqa_env_factor", mt.data_ptr(), count, n, _lib.BQA_C64, 1e-6, lu.data_ptr(), ul.data_ptr(),
+             status.data_ptr(), st)
+    torch.cuda.synchronize()
+    lu_h = lu.cpu().numpy().reshape(count, n, n).astype(np.complex128)
+    ul_h = ul.cpu().numpy().reshape(count, n, n).astype(np.complex128)
+    assert np.isfinite(lu_h).all() and np.isfinite(ul_h).all()
+    assert int(status.item()) == 0
+    w, u = np.linalg.eigh(m.astype(np.complex128))
+    kept = np.einsum("eik,ek,ejk->eij", u, np.where(w > 1e-6, w, 0.0), np.conj(u))
+    recon = np.conj(np.swapaxes(lu_h, 1, 2)) @ lu_h
+    assert np.abs(recon - kept).max() < 2e-5 * np.abs(m).max()
+    assert (np.sum(np.linalg.norm(lu_h, axis=2) > 0, axis=1) == 12).all()
