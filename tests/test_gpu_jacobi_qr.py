@@ -96,12 +96,19 @@ def test_qr_env_factors_with_negligible_columns_stay_finite():
     from bqa_gb300 import _lib
     lib = _lib.load()
     rng = np.random.default_rng(3)
-    count, n = 256, 32
-    q, _ = np.linalg.qr(rng.normal(size=(count, n, n)) + 1j * rng.normal(size=(count, n, n)))
-    lam = np.concatenate([np.sort(rng.uniform(1e-3, 1.0, size=(count, 12)))[:, ::-1],
-                          np.full((count, 8), 1e-8), np.full((count, 12), 1e-20)], axis=1)
-    m = np.einsum("eik,ek,ejk->eij", q, lam, np.conj(q))
-    m /= np.trace(m, axis1=1, axis2=2).real[:, None, None]
+    count, n, big = 256, 32, 12
+    # block-diagonal: a 12x12 PSD block of O(1) eigenvalues and a 20x20 PSD block of size
+    # ~1e-22, rows and columns interleaved by a random permutation: after 12 Householder steps
+    # the trailing column norms are ~1e-21, representable but far below float32 resolution
+    m = np.zeros((count, n, n), dtype=np.complex128)
+    for e in range(count):
+        x = rng.normal(size=(big, big)) + 1j * rng.normal(size=(big, big))
+        y = rng.normal(size=(n - big, n - big)) + 1j * rng.normal(size=(n - big, n - big))
+        blk = np.zeros((n, n), dtype=np.complex128)
+        blk[:big, :big] = x @ np.conj(x.T) / np.trace(x @ np.conj(x.T)).real
+        blk[big:, big:] = 1e-22 * (y @ np.conj(y.T)) / (n - big)
+        p_ = rng.permutation(n)
+        m[e] = blk[np.ix_(p_, p_)]
     m = m.astype(np.complex64)
     dev = torch.device("cuda")
     mt = torch.from_numpy(m.reshape(-1)).to(dev)
@@ -120,4 +127,4 @@ def test_qr_env_factors_with_negligible_columns_stay_finite():
     kept = np.einsum("eik,ek,ejk->eij", u, np.where(w > 1e-6, w, 0.0), np.conj(u))
     recon = np.conj(np.swapaxes(lu_h, 1, 2)) @ lu_h
     assert np.abs(recon - kept).max() < 2e-5 * np.abs(m).max()
-    assert (np.sum(np.linalg.norm(lu_h, axis=2) > 0, axis=1) == 12).all()
+    assert (np.sum(np.linalg.norm(lu_h, axis=2) > 0, axis=1) == (w > 1e-6).sum(axis=1)).all()
