@@ -105,7 +105,8 @@ def test_qr_env_factors_with_negligible_columns_stay_finite():
         x = rng.normal(size=(big, big)) + 1j * rng.normal(size=(big, big))
         y = rng.normal(size=(n - big, n - big)) + 1j * rng.normal(size=(n - big, n - big))
         blk = np.zeros((n, n), dtype=np.complex128)
-        blk[:big, :big] = x @ np.conj(x.T) / np.trace(x @ np.conj(x.T)).real
+        xx = x @ np.conj(x.T) + big * np.eye(big)      # kept eigenvalues well above the 1e-6 mask
+        blk[:big, :big] = xx / np.trace(xx).real
         blk[big:, big:] = 1e-22 * (y @ np.conj(y.T)) / (n - big)
         p_ = rng.permutation(n)
         m[e] = blk[np.ix_(p_, p_)]
