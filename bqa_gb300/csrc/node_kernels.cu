@@ -654,16 +654,22 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
                 *reinterpret_cast<float4*>(sT + tiled::swz<SW>(2 * i)) = tg[i];
         }
     }
+    int offdiag = 0;   // this thread loaded a nonzero off-diagonal message entry
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
         // transpose on the way in; consecutive threads write consecutive shared addresses
         for (int o = threadIdx.x; o < N2; o += TH) {
             const int j = o / CHI, i = o - j * CHI;
-            sMt[k * N2 + o] = mg[i * CHI + j];
+            const float2 v = mg[i * CHI + j];
+            sMt[k * N2 + o] = v;
+            offdiag |= (i != j) && (v.x != 0.f || v.y != 0.f);
         }
     }
-    __syncthreads();
+    // Every incoming message diagonal (the first sweep after a truncation starts from
+    // diag(lambda)/tr): the degree-3 bond products are bond scalings (diag_scale3), the same
+    // values without the dense products.  NaN counts as nonzero.
+    const bool diag = !__syncthreads_or(offdiag);
     auto prod = [&](const float2* X, float2* Y, int k) {
         tiled::product<D, CHI, TH, SW, 1>(X, Y, sMt + k * N2, k);
         __syncthreads();
@@ -685,12 +691,18 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
             tiled::write_half_block<CHI, TH>(sP, og);
             __syncthreads();
         };
-        q::prod1(sT, sA, sMt + N2);
-        __syncthreads();
-        q::prod2(sT, sB, sMt + 2 * N2);
+        if (diag) {
+            tiled::diag_scale3<CHI, TH, SW>(sT, sA, sMt + N2, 1);
+            tiled::diag_scale3<CHI, TH, SW>(sT, sB, sMt + 2 * N2, 2);
+        } else {
+            q::prod1(sT, sA, sMt + N2);
+            __syncthreads();
+            q::prod2(sT, sB, sMt + 2 * N2);
+        }
         __syncthreads();
         emit_s(std::integral_constant<int, 0>{}, sA, sB);
-        q::prod0_inplace(sT, sMt);
+        if (diag) tiled::diag_scale3<CHI, TH, SW>(sT, sT, sMt, 0);
+        else q::prod0_inplace(sT, sMt);
         __syncthreads();
         emit_s(std::integral_constant<int, 2>{}, sT, sA);
         emit_s(std::integral_constant<int, 1>{}, sT, sB);
@@ -698,10 +710,17 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         prod(sT, sA, 1); emit(0, sT, sA);
         prod(sT, sA, 0); emit(1, sT, sA);
     } else if (D == 3) {
-        prod(sT, sA, 1);
-        prod(sT, sB, 2);
+        if (diag) {
+            tiled::diag_scale3<CHI, TH, SW>(sT, sA, sMt + N2, 1);
+            tiled::diag_scale3<CHI, TH, SW>(sT, sB, sMt + 2 * N2, 2);
+            __syncthreads();
+        } else {
+            prod(sT, sA, 1);
+            prod(sT, sB, 2);
+        }
         emit(0, sA, sB);
-        tiled::product_first_inplace<D, CHI, TH, SW, 1>(sT, sMt);
+        if (diag) tiled::diag_scale3<CHI, TH, SW>(sT, sT, sMt, 0);
+        else tiled::product_first_inplace<D, CHI, TH, SW, 1>(sT, sMt);
         __syncthreads();
         emit(2, sT, sA);
         emit(1, sT, sB);

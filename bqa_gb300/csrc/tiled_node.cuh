@@ -333,6 +333,21 @@ __device__ __forceinline__ void close_tiled(const float2* __restrict__ T, const 
     reduce_tile<KS, CHI>(acc, ks, active, P + (size_t)s * CHI * CHI, ag, bg);
 }
 
+// Y = X x_k diag(M) for degree 3: Y[e] = M[i][i] X[e], i the bond-k index of element e =
+// x0 CHI^2 + x1 CHI + x2 (Mt is the transposed message, its diagonal at i CHI + i).  The dense
+// product with a diagonal M adds exact zeros to this one term, so the values are the same.
+// Elementwise: X == Y (in place) is allowed.
+template <int CHI, int TH, int SW>
+__device__ __forceinline__ void diag_scale3(const float2* X, float2* Y, const float2* __restrict__ Mt, int k) {
+    constexpr int PS = CHI * CHI * CHI;
+    const int div = k == 0 ? CHI * CHI : (k == 1 ? CHI : 1);
+    for (int e = threadIdx.x; e < PS; e += TH) {
+        const int i = (e / div) % CHI;
+        const int p = swz<SW>(e);
+        Y[p] = c_fma(Mt[i * CHI + i], X[p], make_float2(0.f, 0.f));
+    }
+}
+
 // Copy a half-node block P (CHI x CHI, row-major, upper tiles valid) to global memory, the
 // tiles below the diagonal as conjugate transposes of those above.
 template <int CHI, int TH>

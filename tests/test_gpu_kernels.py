@@ -106,6 +106,40 @@ def test_split_bp_sweep_matches_oracle(name, chi, precision):
     assert abs(np.sqrt(num) / np.sqrt(den) - d_want) < 1e-5 * max(1.0, d_want)
 
 
+@pytest.mark.parametrize("name,chi", [("rr3_n16_chi4", 16), ("rr3_n24_chi8", 8), ("rr3_n24_chi8", 12),
+                                      ("rr3_n16_chi4", 4)])
+def test_split_sweep_with_diagonal_messages_matches_oracle(name, chi):
+    """Diagonal incoming messages (the first sweep after a truncation, diag(lambda)/tr): the
+    degree-3 half-node kernels detect them and apply them as bond scalings; one oracle sweep
+    to the complex64 tolerance, and the dense products' values (to 1e-6) when one off-diagonal
+    entry of 1e-30 per message makes the kernels take the dense path."""
+    octx, st, job = random_state(name, chi, seed=11)
+    rng = np.random.default_rng(5)
+    lam = rng.uniform(0.1, 1.0, size=(octx.edges_number, chi))
+    m = np.zeros((octx.edges_number, chi, chi), dtype=np.complex128)
+    m[:, np.arange(chi), np.arange(chi)] = lam / lam.sum(axis=1, keepdims=True)
+    m = m.astype(np.complex64).astype(np.complex128)
+    st.msgs = m
+    job.set_state(st.degree_to_tensor, m)
+    want = np.empty_like(m)
+    for d, t in st.degree_to_tensor.items():
+        L = octx.degree_to_layout[d]
+        for mm, p in zip(orc.pass_msgs(t, [m[p] for p in L.input_msgs_position]), L.output_msgs_position):
+            want[p] = mm
+    job.dist_parts.zero_()
+    job.lib.call("bqa_bp_sweep_split", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.msgs[1]), _ptr(job.lu), octx.edges_number, _ptr(job.dist_parts), None, job.stream)
+    got = job.msgs[1][: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, want) < RTOL
+    # one off-diagonal entry of 1e-30 per message sends the kernels down the dense products
+    m2 = m.copy()
+    m2[:, 0, chi - 1] = 1e-30
+    job.set_state(st.degree_to_tensor, m2)
+    job.dist_parts.zero_()
+    job.lib.call("bqa_bp_sweep_split", job._class_array(), len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.msgs[1]), _ptr(job.lu), octx.edges_number, _ptr(job.dist_parts), None, job.stream)
+    dense = job.msgs[1][: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, dense) < 1e-6
 @pytest.mark.parametrize("name,chi", CASES)
 def test_ext_msgs_match_oracle(name, chi):
     octx, st, job = random_state(name, chi, seed=1)
