@@ -200,7 +200,9 @@ int32_t bqa_bp_sweep(const bqa_class* classes /* host array */, int32_t n_classe
  * every node writes its phys-resolved open-bond blocks P_0, P_1 of every bond (complex64
  * nodes of degree 2-4 at chi % 4 == 0 run one CTA per (node, physical index), in half the
  * shared memory), then one kernel forms msg = (P_0 + P_1)/tr per slot and the convergence
- * maxima.  Same inputs, outputs and loop_state behaviour as bqa_bp_sweep.
+ * maxima.  Same inputs, outputs and loop_state behaviour as bqa_bp_sweep.  A degree-3
+ * half-node CTA whose incoming messages are all exactly diagonal (the first sweep after
+ * bqa_msgs_from_lmbds) applies them as bond scalings: the values the dense products give.
  */
 int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi, int32_t dtype,
                            void* msgs_a, void* msgs_b, void* pm, int32_t edges, void* dist_parts,
