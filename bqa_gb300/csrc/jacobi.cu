@@ -401,13 +401,33 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
     const bool live = p < half;
     const int pf = live ? p : 0, pb = pf + half;
     const size_t nn = (size_t)n * n;
-    // direct: stage lu_f, then ker[:, lane] = lu_f . lu_b[lane, :]^T
-    // QR: stage lu_b, then ker^H[:, lane] = conj(lu_b . lu_f[lane, :]^T)
+    // direct: stage lu_f, then ker[:, lane] = lu_f . lu_b[lane, :]^T (row lane of lu_b in registers)
+    // QR: stage lu_b, and lu_f in the (still idle) V block at an odd row stride (conflict-free row
+    // reads), then ker^H[:, lane] = conj(lu_b . lu_f[lane, :]^T); no row registers (they spilled)
     const size_t staged = QR ? (size_t)pb : (size_t)pf, other = QR ? (size_t)pf : (size_t)pb;
     for (int i = lane; i < n * n; i += W) sm[i] = live ? lu[staged * nn + i] : c_zero<C>();
+    constexpr int RS = W + 1;   // row stride of lu_f in the V block (W * RS <= W * VS)
+    if constexpr (QR) {
+        for (int i = lane; i < n * n; i += W) {
+            const int r = i / n, c = i - r * n;
+            sV[r * RS + c] = live ? lu[other * nn + i] : c_zero<C>();
+        }
+    }
     __syncwarp();
     C a[W];
-    {
+    if constexpr (QR) {
+        const C* frow = sV + lane * RS;
+#pragma unroll
+        for (int i = 0; i < W; ++i) {
+            C acc = c_zero<C>();
+            if (i < n && lane < n) {
+#pragma unroll
+                for (int k = 0; k < W; ++k)
+                    if (k < n) acc = c_fma(sm[i * n + k], frow[k], acc);
+            }
+            a[i] = c_conj(acc);
+        }
+    } else {
         C brow[W];
 #pragma unroll
         for (int k = 0; k < W; ++k)
@@ -420,7 +440,7 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
                 for (int k = 0; k < W; ++k)
                     if (k < n) acc = c_fma(sm[i * n + k], brow[k], acc);
             }
-            a[i] = QR ? c_conj(acc) : acc;
+            a[i] = acc;
         }
     }
     C* sH = sm;
