@@ -107,8 +107,15 @@ SIGNATURES = {
 }
 
 
+BQA_ERR_UNSUPPORTED = 2
+
+
 class BqaError(RuntimeError):
-    pass
+    """A library call returned a non-zero status (``status``: BQA_ERR_*)."""
+
+    def __init__(self, message: str, status: int | None = None):
+        super().__init__(message)
+        self.status = status
 
 
 class Library:
@@ -132,7 +139,7 @@ class Library:
         rc = getattr(self.dll, name)(*args)
         if rc != BQA_OK:
             msg = self.dll.bqa_last_error().decode(errors="replace")
-            raise BqaError(f"{name} failed with status {rc}: {msg}")
+            raise BqaError(f"{name} failed with status {rc}: {msg}", status=int(rc))
 
     def max_bond_dim(self, degree: int, dtype: int = BQA_C64) -> int:
         return int(self.dll.bqa_max_bond_dim(degree, dtype))

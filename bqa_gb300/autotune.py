@@ -108,6 +108,12 @@ def clear_cache() -> None:
         _PLAN_CACHE.clear()
 
 
+def _missing_variant(e: "_lib.BqaError") -> bool:
+    """The library has no kernel of this variant for the class (not a candidate); any other
+    failure is an error."""
+    return e.status == _lib.BQA_ERR_UNSUPPORTED
+
+
 class _Timer:
     """Times launches of one job's sweeps with CUDA events on the job's stream."""
 
@@ -134,8 +140,10 @@ class _Timer:
         ev0.record()
         try:
             self.sweep(classes, variants, split)       # warm-up (also opts kernels into shared memory)
-        except _lib.BqaError:
-            return None
+        except _lib.BqaError as e:
+            if _missing_variant(e):
+                return None
+            raise
         ev1.record()
         ev1.synchronize()
         warm = ev0.elapsed_time(ev1)

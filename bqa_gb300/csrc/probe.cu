@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(float* __restrict__ out,
 // mma.sync on register operands (kind 0: m16n8k16 bf16 -> f32, 4096 FLOP each; kind 1:
 // m16n8k8 tf32 -> f32, 2048 FLOP each) and each thread writes one sum.  FLOPs =
 // flop_per_mma * 8 * iters * blocks * 8 warps.  It gives the legacy tensor path's ceiling next
-// to the FP32 one, the numbers a tensor-core message contraction would be judged against.
+// to the FP32 one: the ceilings a tensor-core message contraction would run against.
 template <int KIND>
 __global__ void __launch_bounds__(256) mma_probe_kernel(float* __restrict__ out, int iters) {
     const unsigned a0 = 0x3f803f80u ^ threadIdx.x, a1 = 0x3f803f80u, a2 = 0x3f803f80u, a3 = 0x3f803f80u;

@@ -43,3 +43,11 @@ def test_plan_description_and_buckets():
     assert d["form"] == "one-stage" and d["variants"] == ["default", "tiled", "generic"]
     assert d["class_ms"][1] == {"tiled": 0.5}
     assert [autotune._bucket(n) for n in (1, 2, 3, 1000, 1024, 1025)] == [1, 2, 4, 1024, 1024, 2048]
+
+
+
+def test_only_missing_variants_are_skipped():
+    """A candidate the library reports as unsupported is skipped; any other failure propagates."""
+    assert autotune._missing_variant(_lib.BqaError("no tiled kernel", status=_lib.BQA_ERR_UNSUPPORTED))
+    assert not autotune._missing_variant(_lib.BqaError("launch failed", status=3))
+    assert not autotune._missing_variant(_lib.BqaError("bad argument", status=1))
