@@ -48,3 +48,34 @@ def test_bad_arguments_are_reported_not_crashing(lib):
     assert b"bqa_env_factor" in lib.dll.bqa_last_error()
     with pytest.raises(_lib.BqaError):
         lib.call("bqa_edge_zz", None, 4, 2, 0, None, None)
+
+
+def _c_offsets(tmp_path, struct: str, fields: list) -> dict:
+    """offsetof each field and sizeof the struct, from the header, by a C compiler."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / f"{struct}.c"
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void) {",
+             f'  printf("sizeof %zu\\n", sizeof({struct}));']
+    lines += [f'  printf("{f} %zu\\n", offsetof({struct}, {f}));' for f in fields]
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / struct
+    subprocess.run([cc, "-o", str(exe), str(src)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {k: int(v) for k, v in (line.split() for line in out.strip().splitlines())}
+
+
+@pytest.mark.parametrize("cls,struct", [(_lib.BqaClass, "bqa_class"), (_lib.BqaJob, "bqa_job"),
+                                        (_lib.BqaLayerInfo, "bqa_layer_info")])
+def test_struct_layout_matches_header(tmp_path, cls, struct):
+    """The ctypes mirrors have the C structs' field offsets and sizes (a mismatch would pass
+    garbage pointers to the library silently)."""
+    names = [f[0] for f in cls._fields_]
+    c = _c_offsets(tmp_path, struct, names)
+    assert c["sizeof"] == ctypes.sizeof(cls)
+    for n in names:
+        assert c[n] == getattr(cls, n).offset, n
