@@ -16,7 +16,7 @@ same generator in the same saturated regime (random bond-dim-16 state in the sym
 gauge), one annealing step per timed step, scaled to 100k nodes by the node count (all
 per-step work is per node).
 Under torchrun (N > 1) every rank runs an independent replica job on its own GPU
-(the path does not shard across GPUs in this build); rank 0 prints one JSON line.
+(the step is not sharded across GPUs here: replicas only); rank 0 prints one JSON line.
 """
 from __future__ import annotations
 
