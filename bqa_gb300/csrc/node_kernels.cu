@@ -678,18 +678,27 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         tiled::close_tiled<CHI, TH, S::KS, PS, SW, 1, true>(X, R, sP, ipow(CHI, idx), ipow(CHI, D - 1 - idx));
         __syncthreads();
         float4* og = reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2);
-        tiled::write_half_block<CHI, TH>(sP, og);
+        tiled::write_half_block<CHI>(sP, og, threadIdx.x, TH);
         __syncthreads();
     };
     if constexpr (SPEC) {
         namespace q = tiled::d3c16;
+        // The closing contractions run on warps 0-4 (the 10 upper tiles); warps 5-7 meanwhile copy
+        // the previous block to global memory, so each closing phase ends with one barrier and the
+        // blocks alternate between two shared buffers.  The last block is copied at the end.
+        constexpr int CT = 160;
+        float2* const sPb[2] = {sP, sP + N2};
+        int pend = -1, cur = 0;   // bond whose block waits in sPb[cur ^ 1] (-1: none)
+        auto out_block = [&](int idx) {
+            return reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2);
+        };
         auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
             constexpr int IDX = decltype(idx_tag)::value;
-            q::close<IDX>(X, R, sP);
+            if (threadIdx.x < CT) q::close<IDX>(X, R, sPb[cur]);
+            else if (pend >= 0) tiled::write_half_block<CHI>(sPb[cur ^ 1], out_block(pend), threadIdx.x - CT, TH - CT);
             __syncthreads();
-            float4* og = reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + IDX] * 2 + s) * N2);
-            tiled::write_half_block<CHI, TH>(sP, og);
-            __syncthreads();
+            pend = IDX;
+            cur ^= 1;
         };
         if (diag) {
             tiled::diag_scale3<CHI, TH, SW>(sT, sA, sMt + N2, 1);
@@ -706,6 +715,7 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         __syncthreads();
         emit_s(std::integral_constant<int, 2>{}, sT, sA);
         emit_s(std::integral_constant<int, 1>{}, sT, sB);
+        tiled::write_half_block<CHI>(sPb[cur ^ 1], out_block(pend), threadIdx.x, TH);
     } else if (D == 2) {
         prod(sT, sA, 1); emit(0, sT, sA);
         prod(sT, sA, 0); emit(1, sT, sA);

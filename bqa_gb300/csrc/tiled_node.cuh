@@ -69,8 +69,8 @@ struct HalfShape {
     static constexpr int KS_RAW = THREADS / CLOSE_TILES;
     static constexpr int KS = KS_RAW >= 32 ? 32 : (KS_RAW >= 16 ? 16 : (KS_RAW >= 8 ? 8 : (KS_RAW >= 4 ? 4 : (KS_RAW >= 2 ? 2 : 1))));
     static constexpr int SW = CHI == 16 ? 7 : (CHI == 8 ? 3 : 0);
-    // T_s, two buffers, D transposed messages, P_s
-    static constexpr int SMEM_ELEMS = 3 * PER_S + D * N2 + N2;
+    // T_s, two buffers, D transposed messages, P_s (two buffers: the (3, 16) kernel alternates)
+    static constexpr int SMEM_ELEMS = 3 * PER_S + D * N2 + 2 * N2;
 };
 
 template <int SW>
@@ -350,10 +350,12 @@ __device__ __forceinline__ void diag_scale3(const float2* X, float2* Y, const fl
 
 // Copy a half-node block P (CHI x CHI, row-major, upper tiles valid) to global memory, the
 // tiles below the diagonal as conjugate transposes of those above.
-template <int CHI, int TH>
-__device__ __forceinline__ void write_half_block(const float2* __restrict__ P, float4* __restrict__ og) {
+// Threads t0 .. t0 + nt - 1 of the block take part (t = this thread's index among them).
+template <int CHI>
+__device__ __forceinline__ void write_half_block(const float2* __restrict__ P, float4* __restrict__ og, int t,
+                                                 int nt) {
     const float4* sp = reinterpret_cast<const float4*>(P);
-    for (int i = threadIdx.x; i < CHI * CHI / 2; i += TH) {
+    for (int i = t; i < CHI * CHI / 2; i += nt) {
         const int r = (2 * i) / CHI, c = (2 * i) % CHI;
         if ((r >> 2) > (c >> 2)) {
             const float2 x = P[c * CHI + r], y = P[(c + 1) * CHI + r];
