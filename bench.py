@@ -384,8 +384,9 @@ def run_gpu_arm(args) -> None:
 
 def run_sweep_mode(args) -> None:
     """Time the dominant kernel alone: one BP sweep over all nodes at a fixed bond dim, on
-    random normalised node tensors with maximally mixed messages (a launch of the
-    message kernel does the same work whatever the values).  Prints one JSON line."""
+    random normalised node tensors with random Hermitian positive-definite trace-normalised
+    messages (not diagonal: diagonal incoming messages take the kernels' bond-scaling path,
+    which only the first sweep after a truncation sees).  Prints one JSON line."""
     import torch
     from bqa_gb300 import instances
     from bqa_gb300.engine import Annealer, _ptr
@@ -399,8 +400,14 @@ def run_sweep_mode(args) -> None:
         size = c.count * 2 * chi ** c.degree
         t = torch.randn(size, dtype=job.msgs[0].dtype, device="cuda", generator=gen).view(c.count, -1)
         c.tensors[0][:size].copy_((t / t.norm(dim=1, keepdim=True)).view(-1))
-    eye = torch.eye(chi, dtype=job.msgs[0].dtype, device="cuda") / chi
-    job.msgs[0][: ctx.edges_number * chi * chi].copy_(eye.expand(ctx.edges_number, chi, chi).reshape(-1))
+    E = ctx.edges_number
+    eye = torch.eye(chi, dtype=job.msgs[0].dtype, device="cuda")
+    for e0 in range(0, E, 65536):
+        e1 = min(E, e0 + 65536)
+        x = torch.randn(e1 - e0, chi, chi, dtype=job.msgs[0].dtype, device="cuda", generator=gen)
+        m = x @ x.conj().transpose(1, 2) + 0.1 * eye
+        m = m / torch.diagonal(m, dim1=1, dim2=2).sum(-1).view(-1, 1, 1)
+        job.msgs[0][e0 * chi * chi: e1 * chi * chi].copy_(m.reshape(-1))
     job.chi = job.chis = chi
     job.tcur = job.mcur = 0
     cls = job._class_array()
