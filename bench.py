@@ -219,6 +219,24 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line))
 
 
+def max_over_ranks(values: list, device=None) -> list:
+    """Element-wise maximum of ``values`` over the ranks of the default process group (the
+    slowest replica's times define the job's time); the values themselves without one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def replica_value(world: int, steps: int, t_max_ms: float) -> float:
+    """Whole-job steps/s of ``world`` independent replicas that each ran ``steps`` steps, the
+    slowest in ``t_max_ms``."""
+    return world * steps / (t_max_ms / 1000.0)
+
+
 def gpu_launches(job, kt, steps: int) -> int:
     """Kernels of this library launched in the timed region: node kernels launch once per
     degree class, the SVD kernels once per call; every sweep adds its finalize kernel and
@@ -309,17 +327,13 @@ def run_gpu_arm(args) -> None:
         bloch = job.bloch_vectors()
     e2e_s = time.perf_counter() - t0
 
-    t_max = ms
-    if world > 1:
-        tt = torch.tensor([ms, e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max, e2e_s = float(tt[0]), float(tt[1])
+    t_max, e2e_s = max_over_ranks([ms, e2e_s], device=dev)
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
-    value = world * args.steps / (t_max / 1000.0)
+    value = replica_value(world, args.steps, t_max)
     sweep_ev = [k for k in kt if k[0] == "bp_sweep"]
     bp_ms = sum(k[1] for k in sweep_ev)
     bp_flops = sum(k[2] for k in sweep_ev)
@@ -363,7 +377,7 @@ def run_gpu_arm(args) -> None:
                      "legacy_mma_peaks_measured": {"bf16_m16n8k16": mma_peak_tflops(job.lib, dev, 0),
                                                    "tf32_m16n8k8": mma_peak_tflops(job.lib, dev, 1),
                                                    "unit": "TFLOP/s", "probe": "bqa_mma_probe"}},
-        "e2e": {"value": world * args.steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 16,
+        "e2e": {"value": replica_value(world, args.steps, 1000.0 * e2e_s), "unit": "steps/s", "h2d_bytes_per_step": 16,
                 "d2h_bytes_per_step": int(n_el * 4 * 8 + 2 * args.chi * 4 + 64),
                 "what": "Annealer.run_layer + bloch_vectors per step (host scalars in, all marginals out), "
                         "the timed window's steps replayed from a snapshot of its starting state"},
