@@ -9,10 +9,10 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 9
+ABI_VERSION = 10
 BQA_C64 = 0
 BQA_C128 = 1
-BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC = 0, 1, 2
+BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC, BQA_VARIANT_TENSOR = 0, 1, 2, 3
 
 BQA_OK = 0
 BQA_STATUS_SVD_NOT_CONVERGED = 1
@@ -70,6 +70,7 @@ SIGNATURES = {
                                      c_int32, c_void_p, c_void_p, c_void_p]),
     "bqa_bp_sweep_plan": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, POINTER(c_int32), c_void_p,
                                     c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p]),
+    "bqa_tc_faults": (c_int32, [POINTER(c_int32), c_int32, c_void_p]),
     "bqa_bp_finalize": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_double, c_double,
                                   c_int32, c_void_p]),
     "bqa_ext_msgs": (c_int32, [POINTER(BqaClass), c_int32, c_int32, c_int32, c_void_p, c_void_p, c_double, c_void_p]),
@@ -143,6 +144,12 @@ class Library:
 
     def max_bond_dim(self, degree: int, dtype: int = BQA_C64) -> int:
         return int(self.dll.bqa_max_bond_dim(degree, dtype))
+
+    def tc_faults(self, stream=None, reset: bool = True) -> int:
+        """CTAs of the tensor-core kernels whose wait for their MMAs ran out (0 when healthy)."""
+        out = c_int32(0)
+        self.call("bqa_tc_faults", ctypes.byref(out), 1 if reset else 0, stream)
+        return int(out.value)
 
 
 _LIB: Library | None = None

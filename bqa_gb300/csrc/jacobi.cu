@@ -838,6 +838,7 @@ int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n,
                        void* lmbds, void* colmax, int32_t* status, void* stream) {
     if (!lu || !ul || !canon || !lmbds || !colmax || !status || edges < 2 || n < 1)
         return set_error(BQA_ERR_ARG, "bqa_bond_canon: bad argument");
+    if (edges & 1) return set_error(BQA_ERR_ARG, "bqa_bond_canon: odd number of directed edges %d", edges);
     cudaStream_t st = as_stream(stream);
     if (dtype == BQA_C64) return canon_dispatch<float>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
     if (dtype == BQA_C128) return canon_dispatch<double>(lu, ul, edges, n, eps, canon, lmbds, colmax, status, st);
@@ -863,6 +864,9 @@ int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n,
 // calls share the array and it keeps the previous call's contents; every element the kernels
 // read is written earlier in the same call, and nothing in it must start at zero.  Calls that
 // overlap on the GPU (different streams, or different host threads) race on the array.
+// The looked-up address is cached per device ordinal for the life of the process: it does not
+// survive cudaDeviceReset (or any other teardown of the device's primary context), after which
+// the library's module is loaded again at a new address.
 
 namespace bqa {
 
@@ -898,6 +902,8 @@ int32_t bqa_canonicalize_noalloc(const void* ext_msgs, int32_t edges, int32_t n,
                                  void* canon, void* lmbds, void* colmax, int32_t* status, void* stream) {
     if (!ext_msgs || !canon || !lmbds || !colmax || !status || edges < 2 || n < 1)
         return set_error(BQA_ERR_ARG, "bqa_canonicalize_noalloc: bad argument");
+    if (edges & 1)
+        return set_error(BQA_ERR_ARG, "bqa_canonicalize_noalloc: odd number of directed edges %d", edges);
     if (dtype != BQA_C64 && dtype != BQA_C128)
         return set_error(BQA_ERR_ARG, "bqa_canonicalize_noalloc: unknown dtype %d", dtype);
     if (n > 32) return set_error(BQA_ERR_UNSUPPORTED, "bqa_canonicalize_noalloc: matrix size %d > 32", n);

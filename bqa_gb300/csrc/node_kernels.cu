@@ -17,6 +17,7 @@
 #include "internal.h"
 #include "tiled_node.cuh"
 #include "tiled_d3c16.cuh"
+#include "tc_d3c16.cuh"
 
 #include <algorithm>
 #include <type_traits>
@@ -38,6 +39,15 @@ static const bool g_use_specialized = [] {
     const char* v = getenv("BQA_GB300_SPECIALIZED");
     return !(v && v[0] == '0');
 }();
+// The (3, 16) half-node kernel runs its bond products on the tensor cores (tc_d3c16.cuh)
+// when BQA_GB300_TC=1 is set when the library loads (the CUDA-core kernel otherwise).
+static const bool g_use_tc = [] {
+    const char* v = getenv("BQA_GB300_TC");
+    return v && v[0] == '1';
+}();
+
+// CTAs of the tensor-core kernels whose wait for their MMAs timed out (bqa_tc_faults).
+__device__ int32_t g_tc_faults;
 
 template <typename R>
 struct NodeArgs {
@@ -754,9 +764,142 @@ static int launch_half_k(const NodeArgs<float>& args, int count, cudaStream_t st
     return check_launch("tiled half kernel");
 }
 
+// Half-node kernel of degree 3, bond dim 16 with the bond products on the tensor cores
+// (tc_d3c16.cuh) and the closing contractions of the specialised CUDA-core kernel; same inputs,
+// outputs and schedule of closes as tiled_half_kernel<3, 16, true>.  Two CTAs of 256 threads and
+// 106 KB share an SM (256 tensor-memory columns each).  A CTA whose incoming messages are all
+// diagonal applies them as bond scalings on the CUDA cores, as the other half-node kernels do.
+__global__ void __launch_bounds__(tcd3::TH, 2) tc_half_kernel_d3c16(NodeArgs<float> a) {
+    constexpr int CHI = 16, D = 3, N2 = CHI * CHI, PS = CHI * CHI * CHI, TH = tcd3::TH;
+    extern __shared__ double4 smem_raw[];
+    float2* region = reinterpret_cast<float2*>(smem_raw);
+    float2* sMt = region + tcd3::REGION / 8;
+    float2* sP = sMt + D * N2;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sP + 2 * N2);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+    float2* const V1 = region + tcd3::X_V1;
+    float2* const V2 = region + tcd3::X_V2;
+    float2* const V0 = region + tcd3::X_V0;
+    const float2* msgs_in = a.msgs_a;
+    if (a.loop_state != nullptr) {
+        if (a.loop_state[0]) return;
+        if (a.loop_state[2]) msgs_in = a.msgs_b;
+    }
+    const int t = threadIdx.x, warp = t >> 5;
+    const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
+    float4 tv[8];
+    tcd3::load_share(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS, tv);
+    int offdiag = 0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
+        const int j = t / CHI, i = t - j * CHI;
+        const float2 v = mg[i * CHI + j];
+        sMt[k * N2 + t] = v;
+        offdiag |= (i != j) && (v.x != 0.f || v.y != 0.f);
+    }
+    const bool diag = !__syncthreads_or(offdiag);
+    if (diag) {
+        tcd3::store_share_swizzled(tv, V0);
+        __syncthreads();
+        tiled::diag_scale3<CHI, TH, 7>(V0, V1, sMt + N2, 1);
+        tiled::diag_scale3<CHI, TH, 7>(V0, V2, sMt + 2 * N2, 2);
+        __syncthreads();
+        tiled::diag_scale3<CHI, TH, 7>(V0, V0, sMt, 0);
+    } else {
+        if (warp == 0) {
+            tc::alloc(slot, tcd3::TMEM_COLS);
+            tc::relinquish();
+        }
+        if (t == 0) {
+            tc::mbar_init(bar, 1);
+            tc::fence_mbar_init();
+        }
+        float* rf = reinterpret_cast<float*>(region);
+        tcd3::store_b(sMt, rf + tcd3::B_OPS / 4);
+        tcd3::store_a<2>(tv, rf + tcd3::A_HI / 4, rf + tcd3::A_LO / 4);
+        tc::fence_proxy_async();
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+        const uint32_t tmem = *slot;
+        const uint32_t rb = tc::smem_u32(region);
+        // V_2 = T x_2 M_2, then V_1, then V_0 through the same A space
+        uint32_t parity = 0;
+        bool late = false;
+#pragma unroll 1
+        for (int p = 0; p < 3; ++p) {
+            const int bond = 2 - p;
+            if (p > 0) {
+                if (bond == 1) tcd3::store_a<1>(tv, rf + tcd3::A_HI / 4, rf + tcd3::A_LO / 4);
+                else tcd3::store_a<0>(tv, rf + tcd3::A_HI / 4, rf + tcd3::A_LO / 4);
+                tc::fence_proxy_async();
+                __syncthreads();
+            }
+            if (t == 0) {
+                tc::fence_after();
+                const uint32_t col = bond == 2 ? tcd3::COL_V2 : (bond == 1 ? tcd3::COL_V1 : tcd3::COL_V0);
+                tcd3::issue_product(tmem, col, rb, rb + tcd3::B_OPS + 8192 * bond);
+                tc::commit(bar);
+            }
+            const bool ok = tc::mbar_wait(bar, parity, tcd3::WAIT_CYCLES);
+            parity ^= 1;
+            if (__syncthreads_or(!ok)) {
+                late = true;
+                break;
+            }
+        }
+        if (late) {
+            // the MMAs did not complete in time: count the fault, give them one more bounded
+            // wait, release the tensor memory and leave this CTA's blocks unwritten
+            if (t == 0) atomicAdd(&g_tc_faults, 1);
+            tc::mbar_wait(bar, parity ^ 1, tcd3::WAIT_CYCLES);
+            tc::fence_before();
+            __syncthreads();
+            if (warp == 0) tc::dealloc(tmem, tcd3::TMEM_COLS);
+            return;
+        }
+        tc::fence_after();
+        tcd3::epilogue(tmem, region);
+        tc::fence_before();
+        __syncthreads();
+        if (warp == 0) tc::dealloc(tmem, tcd3::TMEM_COLS);
+    }
+    __syncthreads();
+    // closing contractions on warps 0-4, the previous block copied out by warps 5-7 meanwhile
+    namespace q = tiled::d3c16;
+    constexpr int CT = 160;
+    float2* const sPb[2] = {sP, sP + N2};
+    int pend = -1, cur = 0;
+    auto out_block = [&](int idx) {
+        return reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2);
+    };
+    auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
+        constexpr int IDX = decltype(idx_tag)::value;
+        if (t < CT) q::close<IDX>(X, R, sPb[cur]);
+        else if (pend >= 0) tiled::write_half_block<CHI>(sPb[cur ^ 1], out_block(pend), t - CT, TH - CT);
+        __syncthreads();
+        pend = IDX;
+        cur ^= 1;
+    };
+    emit_s(std::integral_constant<int, 0>{}, V1, V2);
+    emit_s(std::integral_constant<int, 2>{}, V0, V1);
+    emit_s(std::integral_constant<int, 1>{}, V0, V2);
+    tiled::write_half_block<CHI>(sPb[cur ^ 1], out_block(pend), t, TH);
+}
+
+static int launch_tc_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    const size_t smem = (size_t)tcd3::REGION + (3 + 2) * 256 * sizeof(float2) + 16;
+    int rc = ensure_smem((const void*)tc_half_kernel_d3c16, smem, "tensor-core half kernel");
+    if (rc) return rc;
+    tc_half_kernel_d3c16<<<2 * count, tcd3::TH, smem, st>>>(args);
+    return check_launch("tensor-core half kernel");
+}
+
 template <int D, int CHI>
 static int launch_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
     if constexpr (D == 3 && CHI == 16) {
+        if (g_use_tc) return launch_tc_half(args, count, st);
         if (g_use_specialized) return launch_half_k<D, CHI, true>(args, count, st);
     }
     return launch_half_k<D, CHI, false>(args, count, st);
@@ -1181,10 +1324,22 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t c
         const bqa_class& k = classes[c];
         if (k.count <= 0 || k.degree == 0) continue;
         const int v = variants[c];
-        if (v < BQA_VARIANT_DEFAULT || v > BQA_VARIANT_GENERIC)
+        if (v < BQA_VARIANT_DEFAULT || v > BQA_VARIANT_TENSOR)
             return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: unknown variant %d", v);
         int rc = BQA_OK;
-        if (v == BQA_VARIANT_DEFAULT) {
+        if (v == BQA_VARIANT_TENSOR) {
+            if (dtype != BQA_C64 || !pm || k.degree != 3 || chi != 16)
+                return set_error(BQA_ERR_UNSUPPORTED, "bqa_bp_sweep_plan: the tensor-core kernel serves the two-stage "
+                                 "complex64 sweep of degree 3 at bond dim 16 (got degree %d, bond dim %d)", k.degree, chi);
+            rc = launch_tc_half(class_args<float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state), k.count, st);
+        } else if (v == BQA_VARIANT_TILED && pm && dtype == BQA_C64 && k.degree == 3 && chi == 16) {
+            // the CUDA-core half-node kernel, whatever the default (3, 16) kernel is
+            rc = g_use_specialized
+                     ? launch_half_k<3, 16, true>(class_args<float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state),
+                                                  k.count, st)
+                     : launch_half_k<3, 16, false>(class_args<float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state),
+                                                   k.count, st);
+        } else if (v == BQA_VARIANT_DEFAULT) {
             // the kernel bqa_bp_sweep_split / bqa_bp_sweep would launch for this class
             bqa_class one = k;
             if (pm) {
@@ -1218,6 +1373,20 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t c
         if (rc) return rc;
     }
     return pm ? launch_bp_combine(dtype, pm, edges, chi, msgs_a, msgs_b, loop_state, dist_parts, st) : BQA_OK;
+}
+
+int32_t bqa_tc_faults(int32_t* out, int32_t reset, void* stream) {
+    if (!out) return set_error(BQA_ERR_ARG, "bqa_tc_faults: null output");
+    cudaStream_t st = as_stream(stream);
+    cudaError_t e = cudaMemcpyFromSymbolAsync(out, g_tc_faults, sizeof(int32_t), 0, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && reset) {
+        static const int32_t zero = 0;
+        e = cudaMemcpyToSymbolAsync(g_tc_faults, &zero, sizeof(int32_t), 0, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "bqa_tc_faults: %s", cudaGetErrorString(e));
+    return BQA_OK;
 }
 
 int32_t bqa_bp_finalize(void* msgs_a, void* msgs_b, int64_t msg_elems, int32_t dtype, void* dist_parts,

@@ -1,0 +1,186 @@
+// Tensor-core (tcgen05) bond products of the degree-3, bond-dim-16 half-node message kernel.
+//
+// A half-node CTA holds T_s[a][b][c] (16^3 complex64, s fixed).  With V_k = T x_k M_k the BP
+// messages close <V_1|V_2> (bond 0), <V_0|V_1> (bond 2) and <V_0|V_2> (bond 1) (the Hermitian
+// split of tiled_node.cuh).  Here the three products run on the tensor cores and the closing
+// contractions stay on the CUDA cores (d3c16::close).
+//
+// Product on bond x as a real GEMM.  Rows r = the two other bond indices (256), contraction
+// index kk = 2 x + p over the interleaved (re, im) parts of T (32), columns n = 2 y + q over the
+// interleaved parts of the output (32):
+//     D[r][n] = sum_kk A[r][kk] B[n][kk],  A[r][2x + p] = part p of T at (r, x),
+//     B[2y][2x] = Re M[y][x], B[2y][2x+1] = -Im M[y][x], B[2y+1][2x] = Im M[y][x],
+//     B[2y+1][2x+1] = Re M[y][x],
+// so row r of D is V_x at (r, y = 0..15), already interleaved.  Per product: two M = 128 tiles,
+// N = 32, K = 32 as four K = 8 steps.
+//
+// FP32 accuracy from TF32 operands (3xTF32): every operand is split as v = hi + lo, hi and lo
+// both TF32 (cvt.rna), and each K step accumulates A_lo B_hi + A_hi B_lo + A_hi B_hi in FP32
+// tensor memory; the dropped A_lo B_lo and the residual of the split are below 2^-21 |v|.
+//
+// Operands in shared memory are K-major without swizzle, [r/8][kk/4][r%8][kk%4] floats
+// (core matrices of 8 rows x 16 bytes; LBO = 128 bytes along K, SBO = 1024 bytes along M or N).
+// One 96 KB region holds, during the products, A hi/lo (2 x 32 KB) and the three messages'
+// B hi/lo (6 x 4 KB); the products run one after another through the same A space (the next
+// layout of T is written once the previous product's MMAs have completed); after the last one
+// the region becomes the three 32 KB close buffers.  The accumulators use 192 of the CTA's 256
+// tensor-memory columns: V_2 at [0, 64), V_1 at [64, 128), V_0 at [128, 192), column 32 j for
+// rows [128 j, 128 j + 128).
+#pragma once
+
+#include "tcgen05.cuh"
+#include "tiled_d3c16.cuh"
+
+namespace bqa {
+namespace tcd3 {
+
+constexpr int TH = 256;
+constexpr int REGION = 98304;                 // bytes
+constexpr int A_HI = 0, A_LO = 32768;         // byte offsets of the A operand (product phase)
+constexpr int B_OPS = 65536;                  // three messages x (hi, lo) x 4 KB
+constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t IDESC = tc::idesc(tc::FMT_TF32, 128, 32);
+constexpr uint32_t LBO = 128, SBO = 1024;
+// close buffers (float2 offsets inside the region): V_1, V_2, V_0
+constexpr int X_V1 = 0, X_V2 = 4096, X_V0 = 8192;
+constexpr uint32_t COL_V2 = 0, COL_V1 = 64, COL_V0 = 128;
+// cycles a wait on the MMA barrier may take before the CTA gives up (~1 s)
+constexpr long long WAIT_CYCLES = 2000000000LL;
+
+// float offset of element (r, kk) of a K-major operand with 32 columns
+__device__ __forceinline__ int aoff(int r, int kk) { return (r >> 3) * 256 + (kk >> 2) * 32 + (r & 7) * 4 + (kk & 3); }
+
+// Thread t's share of T_s: element pairs (a, b, c0), (a, b, c0 + 1) for a = ap + 2 m, m < 8, with
+//   b = (t & 7) + 8 ((t >> 5) & 1),  c0 = 2 (((t >> 3) & 3) + 4 ((t >> 6) & 1)),  ap = t >> 7.
+// A warp reads one a, eight b and four pairs of c: 64 contiguous bytes of eight rows.
+struct ShareCoord {
+    int b, c0, ap;
+    __device__ __forceinline__ ShareCoord(int t)
+        : b((t & 7) + 8 * ((t >> 5) & 1)), c0(2 * (((t >> 3) & 3) + 4 * ((t >> 6) & 1))), ap(t >> 7) {}
+};
+
+__device__ __forceinline__ void load_share(const float2* __restrict__ ts, float4 (&v)[8]) {
+    const ShareCoord q(threadIdx.x);
+    const float4* p = reinterpret_cast<const float4*>(ts);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = p[((q.ap + 2 * m) * 256 + q.b * 16 + q.c0) >> 1];
+}
+
+// the share into a swizzled close buffer (layout of tiled_d3c16.cuh)
+__device__ __forceinline__ void store_share_swizzled(const float4 (&v)[8], float2* __restrict__ X) {
+    const ShareCoord q(threadIdx.x);
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+        *reinterpret_cast<float4*>(X + (q.ap + 2 * m) * 256 + q.b * 16 + (q.c0 ^ ((q.b & 7) << 1))) = v[m];
+}
+
+struct Split {
+    float hi, lo;
+};
+__device__ __forceinline__ Split split(float v) {
+    const float h = tc::to_tf32(v);
+    return {h, tc::to_tf32(v - h)};
+}
+
+// A operand of the product on bond X (2: c, 1: b, 0: a) from the share, hi and lo
+template <int X>
+__device__ __forceinline__ void store_a(const float4 (&v)[8], float* __restrict__ ahi, float* __restrict__ alo) {
+    const ShareCoord q(threadIdx.x);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int a = q.ap + 2 * m;
+        const Split e0 = split(v[m].x), e1 = split(v[m].y), e2 = split(v[m].z), e3 = split(v[m].w);
+        if (X == 2) {   // r = 16 a + b, kk = 2 c + p: the pair is one 16-byte chunk
+            const int o = aoff(16 * a + q.b, 2 * q.c0);
+            *reinterpret_cast<float4*>(ahi + o) = make_float4(e0.hi, e1.hi, e2.hi, e3.hi);
+            *reinterpret_cast<float4*>(alo + o) = make_float4(e0.lo, e1.lo, e2.lo, e3.lo);
+        } else {
+            // X == 1: r = 16 a + c, kk = 2 b + p;  X == 0: r = 16 b + c, kk = 2 a + p
+            const int r0 = X == 1 ? 16 * a + q.c0 : 16 * q.b + q.c0;
+            const int kk = X == 1 ? 2 * q.b : 2 * a;
+            const int o0 = aoff(r0, kk), o1 = aoff(r0 + 1, kk);
+            *reinterpret_cast<float2*>(ahi + o0) = make_float2(e0.hi, e1.hi);
+            *reinterpret_cast<float2*>(alo + o0) = make_float2(e0.lo, e1.lo);
+            *reinterpret_cast<float2*>(ahi + o1) = make_float2(e2.hi, e3.hi);
+            *reinterpret_cast<float2*>(alo + o1) = make_float2(e2.lo, e3.lo);
+        }
+    }
+}
+
+// B operands (hi at bops + 2048 k, lo at + 1024; float offsets) of the three messages from the
+// transposed messages Mt (Mt[k][x][y] = M_k[y][x]); thread t forms entry (y, x) = (t >> 4, t & 15).
+__device__ __forceinline__ void store_b(const float2* __restrict__ Mt, float* __restrict__ bops) {
+    const int t = threadIdx.x;
+    const int y = t >> 4, x = t & 15;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float2 m = Mt[k * 256 + x * 16 + y];
+        const Split re = split(m.x), im = split(m.y), nim = split(-m.y);
+        float* hi = bops + 2048 * k;
+        float* lo = hi + 1024;
+        const int o0 = aoff(2 * y, 2 * x), o1 = aoff(2 * y + 1, 2 * x);
+        *reinterpret_cast<float2*>(hi + o0) = make_float2(re.hi, nim.hi);
+        *reinterpret_cast<float2*>(lo + o0) = make_float2(re.lo, nim.lo);
+        *reinterpret_cast<float2*>(hi + o1) = make_float2(im.hi, re.hi);
+        *reinterpret_cast<float2*>(lo + o1) = make_float2(im.lo, re.lo);
+    }
+}
+
+// One thread: the 24 MMAs of a product (2 row tiles x 4 K steps x 3 terms) into columns col.
+__device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint32_t a_base, uint32_t b_base) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const uint32_t d = tmem + col + 32 * j;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const uint32_t ao = a_base + j * 16384 + s * 256, bo = b_base + s * 256;
+            const uint64_t ahi = tc::desc_noswz(ao + A_HI, LBO, SBO), alo = tc::desc_noswz(ao + A_LO, LBO, SBO);
+            const uint64_t bhi = tc::desc_noswz(bo, LBO, SBO), blo = tc::desc_noswz(bo + 4096, LBO, SBO);
+            tc::mma_tf32(d, alo, bhi, IDESC, s > 0 ? 1u : 0u);
+            tc::mma_tf32(d, ahi, blo, IDESC, 1u);
+            tc::mma_tf32(d, ahi, bhi, IDESC, 1u);
+        }
+    }
+}
+
+// Epilogue of one warp: its 32 rows (quarter w % 4 of row tile w / 4) of the three products,
+// from tensor memory into the swizzled close buffers of the region.
+__device__ __forceinline__ void epilogue(uint32_t tmem, float2* __restrict__ region) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = w >> 2, qd = w & 3;
+    const int r = 128 * j + 32 * qd + lane;
+    const uint32_t tl = tmem + ((uint32_t)(32 * qd) << 16) + 32 * j;
+    uint32_t f[32];
+    {   // V_2: r = 16 a + b, columns y -> V_2[a][b][y]
+        tc::ld_32x32b_x32(tl + COL_V2, f);
+        tc::wait_ld();
+        const int a = r >> 4, b = r & 15;
+        float2* row = region + X_V2 + a * 256 + b * 16;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            *reinterpret_cast<float4*>(row + ((2 * u) ^ ((b & 7) << 1))) =
+                make_float4(__uint_as_float(f[4 * u]), __uint_as_float(f[4 * u + 1]), __uint_as_float(f[4 * u + 2]),
+                            __uint_as_float(f[4 * u + 3]));
+    }
+    {   // V_1: r = 16 a + c, columns y (new b) -> V_1[a][y][c]
+        tc::ld_32x32b_x32(tl + COL_V1, f);
+        tc::wait_ld();
+        const int a = r >> 4, c = r & 15;
+        float2* base = region + X_V1 + a * 256;
+#pragma unroll
+        for (int y = 0; y < 16; ++y)
+            base[y * 16 + (c ^ ((y & 7) << 1))] = make_float2(__uint_as_float(f[2 * y]), __uint_as_float(f[2 * y + 1]));
+    }
+    {   // V_0: r = 16 b + c, columns y (new a) -> V_0[y][b][c]
+        tc::ld_32x32b_x32(tl + COL_V0, f);
+        tc::wait_ld();
+        const int b = r >> 4, c = r & 15;
+        float2* base = region + X_V0 + b * 16 + (c ^ ((b & 7) << 1));
+#pragma unroll
+        for (int y = 0; y < 16; ++y)
+            base[y * 256] = make_float2(__uint_as_float(f[2 * y]), __uint_as_float(f[2 * y + 1]));
+    }
+}
+
+}  // namespace tcd3
+}  // namespace bqa

@@ -29,8 +29,12 @@ from .engine import Annealer, resolve_precision
 from .layout import Context, build_context
 
 
-def job_footprint(ctx: Context, precision: str | None = None) -> int:
-    """Device bytes an ``Annealer`` for ``ctx`` allocates (the buffers of its constructor)."""
+def job_footprint(ctx: Context, precision: str | None = None, sm_count: int | None = None) -> int:
+    """Device bytes an ``Annealer`` for ``ctx`` allocates (the buffers of its constructor).
+
+    ``sm_count``: multiprocessors of the device the job runs on (the engine sizes the work
+    tensors of classes beyond shared memory as 8 CTAs per SM); None asks the current CUDA
+    device, or takes GB300's 152 where no GPU is visible (footprint planning on a host)."""
     p = resolve_precision(precision)
     es = 8 if p == "single" else 16
     rs = es // 2
@@ -49,9 +53,13 @@ def job_footprint(ctx: Context, precision: str | None = None) -> int:
     total += 3 * E * nmax * nmax * es                      # ext / lu / ul
     total += half * nmax * rs + n * 4 * es + half * 8      # lambdas, densities, <ZZ>
     # work tensors for classes beyond shared memory (engine: min(count, 8 x SMs) CTAs)
+    if sm_count is None:
+        import torch
+        sm_count = (torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+                    if torch.cuda.is_available() else 152)
     lib = _lib.load()
     dt = _lib.BQA_C64 if p == "single" else _lib.BQA_C128
-    total += max((min(L.batch_size, 8 * 152) * int(lib.dll.bqa_node_scratch_elems(d, chi, dt)) * es
+    total += max((min(L.batch_size, 8 * sm_count) * int(lib.dll.bqa_node_scratch_elems(d, chi, dt)) * es
                   for d, L in ctx.degree_to_layout.items()), default=0)
     return int(total) + (1 << 20)
 
@@ -81,6 +89,8 @@ class JobServer:
             free, _ = torch.cuda.mem_get_info(self.device)
             hbm_budget = int(free * 0.85)
         self.budget = int(hbm_budget)
+        self.sm_count = (torch.cuda.get_device_properties(self.device).multi_processor_count
+                         if self.device.type == "cuda" else None)
         self.precision = precision
         self.max_active = max_active
         self._queue: list[_Job] = []
@@ -102,7 +112,7 @@ class JobServer:
         """Queue a job (arrival = now by default); returns its id.  Configs that cannot fit the
         budget even alone are rejected with ValueError."""
         ctx = build_context(config, layout_device=self.device)
-        fp = job_footprint(ctx, self.precision)
+        fp = job_footprint(ctx, self.precision, self.sm_count)
         if fp > self.budget:
             raise ValueError(f"job needs {fp} device bytes, above the server budget {self.budget}")
         job = _Job(self.now() if arrival is None else arrival, next(self._seq), config, ctx, fp)

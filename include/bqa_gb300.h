@@ -48,7 +48,9 @@ enum { BQA_C64 = 0, BQA_C128 = 1 };
 enum {
     BQA_VARIANT_DEFAULT = 0,  /* the kernel bqa_bp_sweep / bqa_bp_sweep_split launch */
     BQA_VARIANT_TILED = 1,    /* register-tiled: half-node (two-stage sweep) or whole-node (one stage) */
-    BQA_VARIANT_GENERIC = 2   /* generic shared-memory kernel (global-memory form beyond shared memory) */
+    BQA_VARIANT_GENERIC = 2,  /* generic shared-memory kernel (global-memory form beyond shared memory) */
+    BQA_VARIANT_TENSOR = 3    /* half-node kernel with tensor-core (tcgen05, 3xTF32) bond products:
+                                 two-stage complex64 sweeps of degree 3 at bond dim 16 */
 };
 
 /* device status word bits (written by kernels into a caller int32) */
@@ -214,7 +216,10 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_
  * of bqa_bp_sweep_split (TILED = half-node kernels, GENERIC = generic open-bond blocks, then one
  * combine pass over all `edges` slots), pm == NULL the one-stage form of bqa_bp_sweep (TILED =
  * whole-node kernels).  TILED is BQA_ERR_UNSUPPORTED where no register-tiled kernel exists
- * (complex64, degree 2-4, chi in {4, 8, 12, 16} minus (2, 4) and (4, 12+)).  variants == NULL is
+ * (complex64, degree 2-4, chi in {4, 8, 12, 16} minus (2, 4) and (4, 12+)); at degree 3, bond dim
+ * 16 it is the CUDA-core half-node kernel.  TENSOR is the tensor-core half-node kernel (two-stage,
+ * complex64, degree 3, bond dim 16 only; BQA_ERR_UNSUPPORTED elsewhere), which is also what
+ * DEFAULT launches there when BQA_GB300_TC=1 was set when the library loaded.  variants == NULL is
  * bqa_bp_sweep_split (pm != NULL) or bqa_bp_sweep.  The choices are the search space of the
  * host-side autotuner (bqa_gb300/autotune.py); every variant computes the same messages up to
  * rounding.  Same loop_state and dist_parts behaviour as bqa_bp_sweep.
@@ -222,6 +227,15 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_
 int32_t bqa_bp_sweep_plan(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi, int32_t dtype,
                           const int32_t* variants /* host */, void* msgs_a, void* msgs_b, void* pm, int32_t edges,
                           void* dist_parts, const int32_t* loop_state, void* stream);
+
+/*
+ * Tensor-core kernel health (no reference counterpart): *out (host) = the number of CTAs of the
+ * tensor-core kernels whose bounded wait for their MMAs ran out since the library loaded (or
+ * since the last reset), 0 in correct operation; such a CTA leaves its output blocks unwritten.
+ * reset != 0 zeroes the counter after reading it.  Blocks the calling thread until `stream`
+ * has drained.
+ */
+int32_t bqa_tc_faults(int32_t* out /* host */, int32_t reset, void* stream);
 
 /*
  * BP convergence decision and damping after one sweep (src/bqa/state.py:113-124,
@@ -281,7 +295,8 @@ int32_t bqa_env_factor(const void* mats, int32_t count, int32_t n, int32_t dtype
  * lmbds[p][0..n-1] (real), canonicalisers ul[p] us -> canon[p+E/2] and ul[p+E/2] vhs^T ->
  * canon[p], and the max over edges of each lambda column folded into colmax[0..n-1]
  * (real bits, uint32 for BQA_C64, uint64 for BQA_C128; caller zeroes;
- * src/bqa/backends.py:297-303).
+ * src/bqa/backends.py:297-303).  edges must be even (BQA_ERR_ARG otherwise): slot p + E/2 is the
+ * reversal of slot p.
  */
 int32_t bqa_bond_canon(const void* lu, const void* ul, int32_t edges, int32_t n, int32_t dtype, double eps, void* canon,
                        void* lmbds, void* colmax, int32_t* status, void* stream);
@@ -346,8 +361,10 @@ int32_t bqa_project_nodes(void* tensors, int32_t count, int32_t node_elems, int3
  * e.g. 65,536 edges at n = 8 or 4,096 at n = 32 in complex64).  Inputs: ext_msgs[edges][n][n].
  * Outputs as bqa_bond_canon (canon, lmbds, status bits OR-ed in); colmax is zeroed here
  * before it is filled.  The first call on a device looks up the array's device address, so
- * make it before any stream capture.  Calls share the array: calls that overlap on the GPU
- * race.
+ * make it before any stream capture; that address is cached per device ordinal and does not
+ * survive cudaDeviceReset.  Calls share the array: calls that overlap on the GPU race.  edges
+ * must be even (BQA_ERR_ARG otherwise).  When the return code is not BQA_OK, every output
+ * (canon, lmbds, colmax, status) is undefined: the call may have cleared or partly written them.
  */
 int32_t bqa_canonicalize_noalloc(const void* ext_msgs, int32_t edges, int32_t n, int32_t dtype, double eps,
                                  void* canon, void* lmbds, void* colmax, int32_t* status, void* stream);

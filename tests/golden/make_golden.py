@@ -1,8 +1,9 @@
 """Generate golden fixtures by running the REFERENCE bqa (v0.1.6) numpy backend at FP64.
 
-Run in a container that holds the reference sources (read-only) at /root/reference:
+Run where the reference sources are available, with BQA_REFERENCE_SRC naming the
+reference's ``src`` directory:
 
-    python tests/golden/make_golden.py [--big]
+    BQA_REFERENCE_SRC=<reference checkout>/src python tests/golden/make_golden.py [--big]
 
 It imports the reference through a stub dist-info (its ``__init__`` asks importlib.metadata
 for its version), runs ``bqa.run_qa`` / the state-VM phase functions on seeded small
@@ -25,16 +26,23 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF_SRC = Path("/root/reference/src")
+
+
+def _reference_src() -> Path:
+    src = os.environ.get("BQA_REFERENCE_SRC")
+    if not src or not (Path(src) / "bqa").is_dir():
+        raise SystemExit("set BQA_REFERENCE_SRC to the reference bqa checkout's src directory")
+    return Path(src)
 
 
 def _import_reference():
+    ref_src = _reference_src()
     shim = Path(tempfile.mkdtemp(prefix="bqa_shim_"))
     info = shim / "bqa-0.1.6.dist-info"
     info.mkdir()
     (info / "METADATA").write_text("Metadata-Version: 2.1\nName: bqa\nVersion: 0.1.6\n")
     os.environ["BQA_PRECISION"] = "double"
-    sys.path[:0] = [str(shim), str(REF_SRC)]
+    sys.path[:0] = [str(shim), str(ref_src)]
     import bqa  # noqa: F401
     import bqa.state as st
     from bqa.config.core import config_to_context

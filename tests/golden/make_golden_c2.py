@@ -3,9 +3,10 @@
 h ~ U(-0.5, 0.5), chi 16, bp_eps 1e-5, <= 50 sweeps), over the first 66 steps of its
 200-step, T = 20 schedule -- past the step at which the bond dimension saturates at 16.
 
-Run in a container that holds the reference sources (read-only) at /root/reference:
+Run where the reference sources are available, with BQA_REFERENCE_SRC naming the
+reference's ``src`` directory:
 
-    python tests/golden/make_golden_c2.py
+    BQA_REFERENCE_SRC=<reference checkout>/src python tests/golden/make_golden_c2.py
 
 (about an hour of one CPU core).  It writes tests/golden/c2_rr3_n10k_chi16.npz with the
 instance (edges, couplings, fields), the schedule parameters and the reference's Bloch

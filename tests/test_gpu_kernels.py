@@ -321,7 +321,8 @@ np.savez(sys.argv[1], msgs=msgs, ext=ext)
 
 
 def test_specialised_half_kernel_bit_identical_to_generic(tmp_path):
-    """The (3, 16) half-node kernel with closed-form addresses gives the generic kernel's bits."""
+    """The (3, 16) CUDA-core half-node kernel with closed-form addresses gives the generic
+    kernel's bits (both with the tensor-core kernel switched off)."""
     import os
     import subprocess
     import sys
@@ -329,7 +330,7 @@ def test_specialised_half_kernel_bit_identical_to_generic(tmp_path):
     root = Path(__file__).resolve().parents[1]
     out = {}
     for flag in ("1", "0"):
-        env = dict(os.environ, BQA_GB300_SPECIALIZED=flag, PYTHONPATH=str(root))
+        env = dict(os.environ, BQA_GB300_SPECIALIZED=flag, BQA_GB300_TC="0", PYTHONPATH=str(root))
         f = tmp_path / f"spec{flag}.npz"
         subprocess.run([sys.executable, "-c", _SWEEP_SCRIPT, str(f)], cwd=root, env=env, check=True, timeout=600)
         out[flag] = np.load(f)

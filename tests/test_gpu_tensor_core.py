@@ -1,0 +1,154 @@
+"""The tensor-core (tcgen05, 3xTF32) half-node message kernel of degree 3 at bond dim 16.
+
+It computes the bond products T x_k M_k on the tensor cores and keeps the closing
+contractions on the CUDA cores.  Checked through the C ABI (bqa_bp_sweep_plan with
+BQA_VARIANT_TENSOR, and the default two-stage entry points that launch it):
+  * one BP sweep equals one oracle sweep to the complex64 kernel tolerance (2e-5 relative);
+  * it agrees with the CUDA-core half-node kernel (BQA_VARIANT_TILED) to 2e-6 relative on a
+    few hundred nodes with dense random Hermitian messages;
+  * diagonal incoming messages take the bond-scaling path and match the oracle;
+  * the extended messages of the two-stage pass match the oracle;
+  * no CTA ever hits the bounded wait for its MMAs (bqa_tc_faults stays 0);
+  * other shapes are refused with BQA_ERR_UNSUPPORTED.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from bqa_gb300 import _lib, instances  # noqa: E402
+from bqa_gb300.engine import Annealer, _ptr  # noqa: E402
+from bqa_gb300.layout import build_context  # noqa: E402
+from oracle import bqa_oracle as orc  # noqa: E402
+from tests.test_gpu_kernels import RTOL, random_state, rel_err  # noqa: E402
+
+
+def oracle_sweep(octx, msgs, tens):
+    want = np.empty_like(msgs)
+    for d, t in tens.items():
+        L = octx.degree_to_layout[d]
+        for mm, p in zip(orc.pass_msgs(t, [msgs[p] for p in L.input_msgs_position]), L.output_msgs_position):
+            want[p] = mm
+    return want
+
+
+def plan_sweep(job, variant):
+    arr = (ctypes.c_int32 * len(job.classes))(*([variant] * len(job.classes)))
+    job.dist_parts.zero_()
+    job.lib.call("bqa_bp_sweep_plan", job._class_array(), len(job.classes), job.chis, job.dtype, arr,
+                 _ptr(job.msgs[0]), _ptr(job.msgs[1]), _ptr(job.lu), job.E, _ptr(job.dist_parts), None, job.stream)
+    return job.msgs[1][: job.E * job.chis * job.chis].cpu().numpy().reshape(job.E, job.chis, job.chis)
+
+
+def dense_state(n, seed, chi=16):
+    """A random 3-regular instance with random normalised tensors and random PSD messages."""
+    edges = instances.random_regular_edges(n, 3, seed)
+    rng = np.random.default_rng(seed)
+    conf = instances.qubo_config(edges, rng.normal(size=len(edges)), rng.normal(size=n), max_bond_dim=chi,
+                                 schedule=instances.anneal_schedule(1.0, 1))
+    ctx = build_context(conf)
+    tens = {}
+    for d, L in ctx.degree_to_layout.items():
+        shape = (L.batch_size, 2) + (chi,) * d
+        t = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        t /= np.linalg.norm(t.reshape(shape[0], -1), axis=1).reshape((-1,) + (1,) * (t.ndim - 1))
+        tens[d] = t.astype(np.complex64).astype(np.complex128)
+    E = ctx.edges_number
+    a = rng.normal(size=(E, chi, chi)) + 1j * rng.normal(size=(E, chi, chi))
+    m = a @ np.conj(np.swapaxes(a, 1, 2)) + 0.1 * np.eye(chi)
+    m /= np.trace(m, axis1=1, axis2=2)[:, None, None]
+    m = m.astype(np.complex64).astype(np.complex128)
+    job = Annealer(ctx, precision="single", pad_bonds=False)
+    job.set_state(tens, m)
+    return ctx, tens, m, job
+
+
+def test_tensor_core_sweep_matches_oracle():
+    octx, st, job = random_state("rr3_n16_chi4", 16, seed=4)
+    want = oracle_sweep(octx, st.msgs, st.degree_to_tensor)
+    got = plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
+    err = rel_err(got, want)
+    print(f"tensor-core sweep vs oracle: {err:.2e}")
+    assert err < RTOL
+    assert job.lib.tc_faults(job.stream) == 0
+
+
+@pytest.mark.parametrize("n,seed", [(64, 1), (512, 2)])
+def test_tensor_core_sweep_matches_cuda_core_kernel(n, seed):
+    ctx, tens, m, job = dense_state(n, seed)
+    tc = plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
+    cc = plan_sweep(job, _lib.BQA_VARIANT_TILED)
+    err = rel_err(tc, cc)
+    print(f"n={n}: tensor-core vs CUDA-core sweep {err:.2e}")
+    assert err < 2e-6
+    if n <= 64:
+        want = oracle_sweep(ctx, m, tens)
+        assert rel_err(tc, want) < RTOL
+    assert job.lib.tc_faults(job.stream) == 0
+
+
+_DEFAULT_SCRIPT = """
+import sys, ctypes, numpy as np
+from tests.test_gpu_tensor_core import dense_state, plan_sweep
+from bqa_gb300 import _lib
+from bqa_gb300.engine import _ptr
+ctx, tens, m, job = dense_state(128, 3)
+tc = plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
+job.dist_parts.zero_()
+job.lib.call("bqa_bp_sweep_split", job._class_array(), len(job.classes), 16, job.dtype, _ptr(job.msgs[0]),
+             _ptr(job.msgs[1]), _ptr(job.lu), job.E, _ptr(job.dist_parts), None, job.stream)
+got = job.msgs[1][: job.E * 256].cpu().numpy().reshape(job.E, 16, 16)
+sys.exit(0 if np.array_equal(got, tc) else 3)
+"""
+
+
+def test_tensor_core_kernel_as_the_default_two_stage_sweep():
+    """With BQA_GB300_TC=1 at load, bqa_bp_sweep_split at (3, 16) gives the TENSOR variant's bits."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, BQA_GB300_TC="1", PYTHONPATH=str(root))
+    r = subprocess.run([sys.executable, "-c", _DEFAULT_SCRIPT], cwd=root, env=env, timeout=600)
+    assert r.returncode == 0
+
+
+def test_tensor_core_kernel_with_diagonal_messages():
+    octx, st, job = random_state("rr3_n16_chi4", 16, seed=11)
+    rng = np.random.default_rng(5)
+    lam = rng.uniform(0.1, 1.0, size=(octx.edges_number, 16))
+    m = np.zeros((octx.edges_number, 16, 16), dtype=np.complex128)
+    m[:, np.arange(16), np.arange(16)] = lam / lam.sum(axis=1, keepdims=True)
+    m = m.astype(np.complex64).astype(np.complex128)
+    job.set_state(st.degree_to_tensor, m)
+    want = oracle_sweep(octx, m, st.degree_to_tensor)
+    got = plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
+    assert rel_err(got, want) < RTOL
+    # one off-diagonal entry of 1e-30 per message: the dense tensor-core products, same values
+    m2 = m.copy()
+    m2[:, 0, 15] = 1e-30
+    job.set_state(st.degree_to_tensor, m2)
+    dense = plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
+    assert rel_err(dense, got) < 1e-6
+
+
+def test_tensor_core_extended_messages_match_oracle():
+    octx, st, job = random_state("rr3_n16_chi4", 16, seed=7)
+    zt = 0.37
+    job.lib.call("bqa_ext_msgs_split", job._class_array(), len(job.classes), 16, job.dtype, _ptr(job.msgs[0]),
+                 _ptr(job.lu), job.E, _ptr(job.edge_j), zt, _ptr(job.ext), job.stream)
+    want = orc.get_extended_msgs(octx, zt, st)
+    got = job.ext[: want.size].cpu().numpy().reshape(want.shape)
+    assert rel_err(got, want) < RTOL
+
+
+def test_tensor_variant_refuses_other_shapes():
+    octx, st, job = random_state("rr3_n24_chi8", 8, seed=1)
+    with pytest.raises(_lib.BqaError) as e:
+        plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
+    assert e.value.status == _lib.BQA_ERR_UNSUPPORTED

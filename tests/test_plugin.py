@@ -1,6 +1,6 @@
-"""The backend registers into an installed reference bqa (skipped where bqa is absent):
-bqa's own validation accepts "gb300", and bqa.run_qa hands such configs to bqa_gb300.run_qa
-while other backends stay on the original path."""
+"""The backend registers into the reference bqa (skipped unless BQA_REFERENCE_SRC names the
+reference's ``src`` directory): bqa's own validation accepts "gb300", and bqa.run_qa hands
+such configs to bqa_gb300.run_qa while other backends stay on the original path."""
 import os
 import sys
 import tempfile
@@ -8,13 +8,13 @@ from pathlib import Path
 
 import pytest
 
-REF_SRC = Path("/root/reference/src")
+REF_SRC = Path(os.environ.get("BQA_REFERENCE_SRC", "")) if os.environ.get("BQA_REFERENCE_SRC") else None
 
 
 @pytest.fixture(scope="module")
 def bqa_mod():
-    if not REF_SRC.exists():
-        pytest.skip("reference bqa sources not present")
+    if REF_SRC is None or not (REF_SRC / "bqa").is_dir():
+        pytest.skip("BQA_REFERENCE_SRC does not name the reference bqa sources")
     shim = Path(tempfile.mkdtemp(prefix="bqa_shim_"))
     (shim / "bqa-0.1.6.dist-info").mkdir()
     (shim / "bqa-0.1.6.dist-info" / "METADATA").write_text("Metadata-Version: 2.1\nName: bqa\nVersion: 0.1.6\n")
