@@ -8,8 +8,10 @@ bond dim and the number of nodes:
 * the sweep's form: two-stage (every node writes its open-bond blocks P_0, P_1 to scratch,
   then one pass forms the messages) or one-stage (every node writes its messages);
 * per class, within a form: the register-tiled kernel (half-node CTAs in the two-stage form,
-  whole-node CTAs in the one-stage form; complex64, degree 2-4, bond dims 4/8/12/16) or the
-  generic shared-memory kernel (global-memory form for nodes beyond shared memory).
+  whole-node CTAs in the one-stage form; complex64, degree 2-4, bond dims 4/8/12/16), the
+  generic shared-memory kernel (global-memory form for nodes beyond shared memory), or, in the
+  two-stage form at degree 3, bond dim 16, the half-node kernel whose bond products run on the
+  tensor cores (tcgen05, 3xTF32).
 
 ``tune(annealer)`` times every candidate of every class on the job's live state (CUDA events
 on the job's stream, a warm-up launch then ``reps`` timed launches, each reading the current
@@ -32,7 +34,7 @@ from dataclasses import dataclass, field
 from . import _lib
 
 VARIANT_NAMES = {_lib.BQA_VARIANT_DEFAULT: "default", _lib.BQA_VARIANT_TILED: "tiled",
-                 _lib.BQA_VARIANT_GENERIC: "generic"}
+                 _lib.BQA_VARIANT_GENERIC: "generic", _lib.BQA_VARIANT_TENSOR: "tensor"}
 
 _LOCK = threading.Lock()
 _CLASS_CACHE: dict[tuple, dict] = {}     # class key -> {"best": variant, "ms": {variant: ms}}
@@ -201,7 +203,10 @@ def tune(job, reps: int = 3) -> Plan:
                     timer = timer or _Timer(job, reps)
                     one = (_lib.BqaClass * 1)(classes[i])
                     ms = {}
-                    for v in (_lib.BQA_VARIANT_TILED, _lib.BQA_VARIANT_GENERIC):
+                    cands = [_lib.BQA_VARIANT_TILED, _lib.BQA_VARIANT_GENERIC]
+                    if split and job.precision == "single" and c.degree == 3 and chis == 16:
+                        cands.insert(1, _lib.BQA_VARIANT_TENSOR)
+                    for v in cands:
                         t = timer.time(one, [v], split, min(ms.values()) if ms else None)
                         if t is not None:
                             ms[v] = t

@@ -816,7 +816,10 @@ __global__ void __launch_bounds__(tcd3::TH, 2) tc_half_kernel_d3c16(NodeArgs<flo
             tc::fence_mbar_init();
         }
         float* rf = reinterpret_cast<float*>(region);
-        tcd3::store_b(sMt, rf + tcd3::B_OPS / 4);
+        const float2* const mg[3] = {msgs_in + (size_t)a.in_pos[node * D] * N2,
+                                     msgs_in + (size_t)a.in_pos[node * D + 1] * N2,
+                                     msgs_in + (size_t)a.in_pos[node * D + 2] * N2};
+        tcd3::store_b(mg, rf + tcd3::B_OPS / 4);
         tcd3::store_a<2>(tv, rf + tcd3::A_HI / 4, rf + tcd3::A_LO / 4);
         tc::fence_proxy_async();
         tc::fence_before();
@@ -839,7 +842,7 @@ __global__ void __launch_bounds__(tcd3::TH, 2) tc_half_kernel_d3c16(NodeArgs<flo
             if (t == 0) {
                 tc::fence_after();
                 const uint32_t col = bond == 2 ? tcd3::COL_V2 : (bond == 1 ? tcd3::COL_V1 : tcd3::COL_V0);
-                tcd3::issue_product(tmem, col, rb, rb + tcd3::B_OPS + 8192 * bond);
+                tcd3::issue_product(tmem, col, rb, rb + tcd3::B_OPS + 2 * tcd3::B_BYTES * bond);
                 tc::commit(bar);
             }
             const bool ok = tc::mbar_wait(bar, parity, tcd3::WAIT_CYCLES);

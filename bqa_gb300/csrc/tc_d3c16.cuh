@@ -18,14 +18,17 @@
 // both TF32 (cvt.rna), and each K step accumulates A_lo B_hi + A_hi B_lo + A_hi B_hi in FP32
 // tensor memory; the dropped A_lo B_lo and the residual of the split are below 2^-21 |v|.
 //
-// Operands in shared memory are K-major without swizzle, [r/8][kk/4][r%8][kk%4] floats
-// (core matrices of 8 rows x 16 bytes; LBO = 128 bytes along K, SBO = 1024 bytes along M or N).
-// One 96 KB region holds, during the products, A hi/lo (2 x 32 KB) and the three messages'
-// B hi/lo (6 x 4 KB); the products run one after another through the same A space (the next
-// layout of T is written once the previous product's MMAs have completed); after the last one
-// the region becomes the three 32 KB close buffers.  The accumulators use 192 of the CTA's 256
-// tensor-memory columns: V_2 at [0, 64), V_1 at [64, 128), V_0 at [128, 192), column 32 j for
-// rows [128 j, 128 j + 128).
+// Operands in shared memory are K-major without swizzle: core matrices of 8 rows x 16 bytes,
+// element (r, kk) of a 32-column operand at byte (r/8) SBO + (kk/4) LBO + 16 (r%8) + 4 (kk%4).
+// The A operand (T) uses LBO = 128 and SBO = 1056 (= 8 x 128 + 32: each 8-row group starts two
+// 16-byte bank groups further on, which makes the three re-layout stores from the threads'
+// registers free of bank conflicts); the B operands (messages) use LBO = 144, SBO = 1152 for the
+// same reason.  One 96 KB region holds, during the products, A hi/lo (2 x 33 KB) and the three
+// messages' B hi/lo (6 x 4.5 KB); the products run one after another through the same A space
+// (the next layout of T is written once the previous product's MMAs have completed); after the
+// last one the region becomes the three 32 KB close buffers.  The accumulators use 192 of the
+// CTA's 256 tensor-memory columns: V_2 at [0, 64), V_1 at [64, 128), V_0 at [128, 192), column
+// 32 j for rows [128 j, 128 j + 128).
 #pragma once
 
 #include "tcgen05.cuh"
@@ -36,27 +39,37 @@ namespace tcd3 {
 
 constexpr int TH = 256;
 constexpr int REGION = 98304;                 // bytes
-constexpr int A_HI = 0, A_LO = 32768;         // byte offsets of the A operand (product phase)
-constexpr int B_OPS = 65536;                  // three messages x (hi, lo) x 4 KB
+constexpr uint32_t A_LBO = 128, A_SBO = 1056; // A operand strides (bytes)
+constexpr uint32_t B_LBO = 144, B_SBO = 1152; // B operand strides (bytes)
+constexpr int A_BYTES = 32 * A_SBO;           // 256 rows
+constexpr int B_BYTES = 4 * B_SBO;            // 32 rows
+constexpr int A_HI = 0, A_LO = A_BYTES;       // byte offsets of the A operand (product phase)
+constexpr int B_OPS = 2 * A_BYTES;            // three messages x (hi, lo)
+static_assert(B_OPS + 6 * B_BYTES <= REGION, "product operands exceed the region");
 constexpr uint32_t TMEM_COLS = 256;
 constexpr uint32_t IDESC = tc::idesc(tc::FMT_TF32, 128, 32);
-constexpr uint32_t LBO = 128, SBO = 1024;
 // close buffers (float2 offsets inside the region): V_1, V_2, V_0
 constexpr int X_V1 = 0, X_V2 = 4096, X_V0 = 8192;
 constexpr uint32_t COL_V2 = 0, COL_V1 = 64, COL_V0 = 128;
 // cycles a wait on the MMA barrier may take before the CTA gives up (~1 s)
 constexpr long long WAIT_CYCLES = 2000000000LL;
 
-// float offset of element (r, kk) of a K-major operand with 32 columns
-__device__ __forceinline__ int aoff(int r, int kk) { return (r >> 3) * 256 + (kk >> 2) * 32 + (r & 7) * 4 + (kk & 3); }
+// float offsets of element (r, kk) in the A and B operands
+__device__ __forceinline__ int aoff(int r, int kk) {
+    return (r >> 3) * (int)(A_SBO / 4) + (kk >> 2) * (int)(A_LBO / 4) + (r & 7) * 4 + (kk & 3);
+}
+__device__ __forceinline__ int boff(int n, int kk) {
+    return (n >> 3) * (int)(B_SBO / 4) + (kk >> 2) * (int)(B_LBO / 4) + (n & 7) * 4 + (kk & 3);
+}
 
 // Thread t's share of T_s: element pairs (a, b, c0), (a, b, c0 + 1) for a = ap + 2 m, m < 8, with
-//   b = (t & 7) + 8 ((t >> 5) & 1),  c0 = 2 (((t >> 3) & 3) + 4 ((t >> 6) & 1)),  ap = t >> 7.
-// A warp reads one a, eight b and four pairs of c: 64 contiguous bytes of eight rows.
+// lane bits 0-1 -> b bits 0-1, lane bit 2 -> ap, lane bits 3-4 -> c0 bits 1-2, and the warp
+// index giving b bits 2-3 (warp bits 0-1) and c0 bit 3 (warp bit 2).  A warp reads two values of
+// a, four of b and four pairs of c: 64 contiguous bytes of eight rows.
 struct ShareCoord {
     int b, c0, ap;
     __device__ __forceinline__ ShareCoord(int t)
-        : b((t & 7) + 8 * ((t >> 5) & 1)), c0(2 * (((t >> 3) & 3) + 4 * ((t >> 6) & 1))), ap(t >> 7) {}
+        : b((t & 3) + 4 * ((t >> 5) & 3)), c0(2 * (((t >> 3) & 3) + 4 * (t >> 7))), ap((t >> 2) & 1) {}
 };
 
 __device__ __forceinline__ void load_share(const float2* __restrict__ ts, float4 (&v)[8]) {
@@ -82,10 +95,13 @@ __device__ __forceinline__ Split split(float v) {
     return {h, tc::to_tf32(v - h)};
 }
 
-// A operand of the product on bond X (2: c, 1: b, 0: a) from the share, hi and lo
+// A operand of the product on bond X (2: c, 1: b, 0: a) from the share, hi and lo.  For X = 1, 0
+// the two elements of a pair go to different rows; lane bit 1 picks which is stored first, so
+// that each 8-byte store instruction of a warp covers all 16 bank pairs twice.
 template <int X>
 __device__ __forceinline__ void store_a(const float4 (&v)[8], float* __restrict__ ahi, float* __restrict__ alo) {
     const ShareCoord q(threadIdx.x);
+    const bool swap = (threadIdx.x >> 1) & 1;
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
         const int a = q.ap + 2 * m;
@@ -99,26 +115,32 @@ __device__ __forceinline__ void store_a(const float4 (&v)[8], float* __restrict_
             const int r0 = X == 1 ? 16 * a + q.c0 : 16 * q.b + q.c0;
             const int kk = X == 1 ? 2 * q.b : 2 * a;
             const int o0 = aoff(r0, kk), o1 = aoff(r0 + 1, kk);
-            *reinterpret_cast<float2*>(ahi + o0) = make_float2(e0.hi, e1.hi);
-            *reinterpret_cast<float2*>(alo + o0) = make_float2(e0.lo, e1.lo);
-            *reinterpret_cast<float2*>(ahi + o1) = make_float2(e2.hi, e3.hi);
-            *reinterpret_cast<float2*>(alo + o1) = make_float2(e2.lo, e3.lo);
+            const int oa = swap ? o1 : o0, ob = swap ? o0 : o1;
+            const float2 ha = swap ? make_float2(e2.hi, e3.hi) : make_float2(e0.hi, e1.hi);
+            const float2 hb = swap ? make_float2(e0.hi, e1.hi) : make_float2(e2.hi, e3.hi);
+            const float2 la = swap ? make_float2(e2.lo, e3.lo) : make_float2(e0.lo, e1.lo);
+            const float2 lb = swap ? make_float2(e0.lo, e1.lo) : make_float2(e2.lo, e3.lo);
+            *reinterpret_cast<float2*>(ahi + oa) = ha;
+            *reinterpret_cast<float2*>(ahi + ob) = hb;
+            *reinterpret_cast<float2*>(alo + oa) = la;
+            *reinterpret_cast<float2*>(alo + ob) = lb;
         }
     }
 }
 
-// B operands (hi at bops + 2048 k, lo at + 1024; float offsets) of the three messages from the
-// transposed messages Mt (Mt[k][x][y] = M_k[y][x]); thread t forms entry (y, x) = (t >> 4, t & 15).
-__device__ __forceinline__ void store_b(const float2* __restrict__ Mt, float* __restrict__ bops) {
+// B operands of the three messages (message k: hi at bops + k * 2 B_BYTES, lo B_BYTES further;
+// byte offsets) from the incoming messages in global memory (M_k[y][x] = m[k][16 y + x]);
+// thread t forms entry (y, x) = (t >> 4, t & 15).
+__device__ __forceinline__ void store_b(const float2* const (&mg)[3], float* __restrict__ bops) {
     const int t = threadIdx.x;
     const int y = t >> 4, x = t & 15;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float2 m = Mt[k * 256 + x * 16 + y];
+        const float2 m = mg[k][y * 16 + x];
         const Split re = split(m.x), im = split(m.y), nim = split(-m.y);
-        float* hi = bops + 2048 * k;
-        float* lo = hi + 1024;
-        const int o0 = aoff(2 * y, 2 * x), o1 = aoff(2 * y + 1, 2 * x);
+        float* hi = bops + k * (2 * B_BYTES / 4);
+        float* lo = hi + B_BYTES / 4;
+        const int o0 = boff(2 * y, 2 * x), o1 = boff(2 * y + 1, 2 * x);
         *reinterpret_cast<float2*>(hi + o0) = make_float2(re.hi, nim.hi);
         *reinterpret_cast<float2*>(lo + o0) = make_float2(re.lo, nim.lo);
         *reinterpret_cast<float2*>(hi + o1) = make_float2(im.hi, re.hi);
@@ -133,9 +155,9 @@ __device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint3
         const uint32_t d = tmem + col + 32 * j;
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const uint32_t ao = a_base + j * 16384 + s * 256, bo = b_base + s * 256;
-            const uint64_t ahi = tc::desc_noswz(ao + A_HI, LBO, SBO), alo = tc::desc_noswz(ao + A_LO, LBO, SBO);
-            const uint64_t bhi = tc::desc_noswz(bo, LBO, SBO), blo = tc::desc_noswz(bo + 4096, LBO, SBO);
+            const uint32_t ao = a_base + j * 16 * A_SBO + s * 2 * A_LBO, bo = b_base + s * 2 * B_LBO;
+            const uint64_t ahi = tc::desc_noswz(ao + A_HI, A_LBO, A_SBO), alo = tc::desc_noswz(ao + A_LO, A_LBO, A_SBO);
+            const uint64_t bhi = tc::desc_noswz(bo, B_LBO, B_SBO), blo = tc::desc_noswz(bo + B_BYTES, B_LBO, B_SBO);
             tc::mma_tf32(d, alo, bhi, IDESC, s > 0 ? 1u : 0u);
             tc::mma_tf32(d, ahi, blo, IDESC, 1u);
             tc::mma_tf32(d, ahi, bhi, IDESC, 1u);

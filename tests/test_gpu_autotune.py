@@ -98,7 +98,8 @@ def test_tuned_anneal_matches_oracle_and_every_driver():
     assert g.plans, "the tuner made no plan"
     for p in g.plans.values():
         assert len(p.variants) == len(g.classes)
-        assert all(v in (V.BQA_VARIANT_DEFAULT, V.BQA_VARIANT_TILED, V.BQA_VARIANT_GENERIC) for v in p.variants)
+        assert all(v in (V.BQA_VARIANT_DEFAULT, V.BQA_VARIANT_TILED, V.BQA_VARIANT_GENERIC, V.BQA_VARIANT_TENSOR)
+                   for v in p.variants)
         assert p.describe()["form"] in ("two-stage", "one-stage")
     # all three drivers ran the same plans: identical state
     ref = g.get_state()

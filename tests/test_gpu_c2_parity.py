@@ -2,7 +2,7 @@
 (random 3-regular, J = +-1, h ~ U(-0.5, 0.5), chi 16), first 66 steps of the 200-step schedule
 (past bond-dim saturation), against the REFERENCE run at FP64 (fixture written by
 tests/golden/make_golden_c2.py).  complex128 to round-off (measured 2.4e-13); complex64
-measured at 1.2e-4."""
+measured at 1.2e-4, held to 1.5x that."""
 from pathlib import Path
 
 import numpy as np
@@ -40,10 +40,10 @@ def test_complex128_matches_reference(case, monkeypatch):
 
 
 def test_complex64_within_bar(case, monkeypatch):
-    """Measured 1.2e-4 max (4.5e-6 mean on <Z>); held to 5e-4."""
+    """Measured 1.21e-4 max (4.5e-6 mean on <Z>); held to 1.8e-4."""
     conf, want = case
     got = _bloch(conf, "single", monkeypatch)
     err = np.abs(got - want).max()
     print(f"complex64 vs reference: max Bloch error {err:.3e}, mean |<Z> error| "
           f"{np.abs(got[:, 2] - want[:, 2]).mean():.3e}")
-    assert err < 5e-4, err
+    assert err < 1.8e-4, err

@@ -106,7 +106,7 @@ def test_headline_cpu_case_matches_reference():
     assert dims[-1] == list(want["dims"])[-1]
     err = np.abs(results[0] - want["result0_bloch_vectors"]).max()
     print(f"{name}: max Bloch error {err:.2e}, sweeps {[s['sweeps'] for s in job.stats][:10]}")
-    assert err < 5e-3
+    assert err < 1.4e-3      # measured 9.2e-4 (complex64 vs the reference at FP64), x 1.5
 
 
 def test_cli_streams_the_run_qa_result(tmp_path):

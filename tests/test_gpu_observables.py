@@ -3,9 +3,9 @@ oracle on the same configs (the reference computes no two-site quantity; the ora
 <Z_u Z_v> as the BP two-site contraction and the energy as sum J <ZZ> + sum h <Z>).
 
 complex128 kernels: <Z_u Z_v> within 1e-8, energy within 1e-9 relative, sign read-out
-identical wherever |<Z>| > 1e-6.  complex64 kernels: <Z_u Z_v> within 5e-3 (the pinv_eps
-threshold decisions complex64 rounding can flip carry ~1e-3, see test_gpu_end_to_end), energy
-within 2e-3 relative, read-out identical wherever |<Z>| > 2e-2.
+identical wherever |<Z>| > 1e-6.  complex64 kernels (measured over these cases: <Z_u Z_v>
+3.8e-5, energy 1.6e-6 relative): <Z_u Z_v> within 1e-4, energy within 1e-5 relative, read-out
+identical wherever |<Z>| > 1e-3.
 """
 import numpy as np
 import pytest
@@ -54,6 +54,6 @@ def test_observables_match_oracle(name, precision):
         assert zz_err < 1e-8 and e_rel < 1e-9
         sure = np.abs(z_w) > 1e-6
     else:
-        assert zz_err < 5e-3 and e_rel < 2e-3
-        sure = np.abs(z_w) > 2e-2
+        assert zz_err < 1e-4 and e_rel < 1e-5
+        sure = np.abs(z_w) > 1e-3
     assert np.array_equal(spins[sure], spins_w[sure])
