@@ -26,6 +26,11 @@ def run_qa(config, device=None, as_arrays: bool = False) -> list:
     on_gpu = torch.cuda.is_available()
     ctx = build_context(config, layout_device=(device if device is not None else "cuda") if on_gpu else None)
     log.info("Context is built")
+    return run_compiled(ctx, device=device, as_arrays=as_arrays)
+
+
+def run_compiled(ctx, device=None, as_arrays: bool = False) -> list:
+    """Execute the instruction list of a compiled context (``layout.Context``) on the GPU."""
     job = Annealer(ctx, device=device)
     total = len(ctx.instructions)
     out = []
