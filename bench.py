@@ -22,6 +22,7 @@ Under torchrun (N > 1) every rank runs an independent replica job on its own GPU
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import logging
 import os
@@ -482,8 +483,15 @@ def run_sweep_mode(args) -> None:
     cls = job._class_array()
     flops, nbytes = job.bp_sweep_cost()
 
+    variant = {"default": None, "tiled": 1, "generic": 2, "tensor": 3, "tensor-bf16": 4}[args.variant]
+    plan = None if variant is None else (ctypes.c_int32 * len(job.classes))(*([variant] * len(job.classes)))
+
     def sweep():
-        if job.split_sweeps:
+        if plan is not None:
+            job.lib.call("bqa_bp_sweep_plan", cls, len(job.classes), chi, job.dtype, plan, _ptr(job.msgs[0]),
+                         _ptr(job.msgs[1]), _ptr(job.lu) if job.split_sweeps else None, ctx.edges_number,
+                         _ptr(job.dist_parts), None, job.stream)
+        elif job.split_sweeps:
             job.lib.call("bqa_bp_sweep_split", cls, len(job.classes), chi, job.dtype, _ptr(job.msgs[0]),
                          _ptr(job.msgs[1]), _ptr(job.lu), ctx.edges_number, _ptr(job.dist_parts), None, job.stream)
         else:
@@ -502,6 +510,7 @@ def run_sweep_mode(args) -> None:
     ms = [a.elapsed_time(b) for a, b in evs]
     mean = float(np.mean(ms))
     print(json.dumps({"mode": "sweep", "n": args.n, "degree": args.degree, "chi": chi, "precision": args.precision,
+                      "variant": args.variant,
                       "sweeps": args.steps,
                       "ms_per_sweep": mean, "ms_min": float(np.min(ms)),
                       "tflops": flops / (mean / 1000) / 1e12, "algorithmic_gbs": nbytes / (mean / 1000) / 1e9,
@@ -800,6 +809,8 @@ def main() -> None:
     ap.add_argument("--rates", default="", help="serve mode: comma-separated arrival rates (jobs/s)")
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     ap.add_argument("--degree", type=int, default=3, help="sweep mode: degree of the random regular graph")
+    ap.add_argument("--variant", default="default", choices=["default", "tiled", "generic", "tensor", "tensor-bf16"],
+                    help="sweep mode: message kernel of every class (bqa_bp_sweep_plan)")
     ap.add_argument("--synthetic", action="store_true",
                     help="svd mode: random graded Hermitian PSD matrices instead of an annealed state")
     args = ap.parse_args()

@@ -13,6 +13,7 @@ ABI_VERSION = 10
 BQA_C64 = 0
 BQA_C128 = 1
 BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC, BQA_VARIANT_TENSOR = 0, 1, 2, 3
+BQA_VARIANT_TENSOR_BF16, BQA_VARIANT_MIXED = 4, 5
 
 BQA_OK = 0
 BQA_STATUS_SVD_NOT_CONVERGED = 1

@@ -34,7 +34,8 @@ from dataclasses import dataclass, field
 from . import _lib
 
 VARIANT_NAMES = {_lib.BQA_VARIANT_DEFAULT: "default", _lib.BQA_VARIANT_TILED: "tiled",
-                 _lib.BQA_VARIANT_GENERIC: "generic", _lib.BQA_VARIANT_TENSOR: "tensor"}
+                 _lib.BQA_VARIANT_GENERIC: "generic", _lib.BQA_VARIANT_TENSOR: "tensor",
+                 _lib.BQA_VARIANT_TENSOR_BF16: "tensor-bf16", _lib.BQA_VARIANT_MIXED: "mixed"}
 
 _LOCK = threading.Lock()
 _CLASS_CACHE: dict[tuple, dict] = {}     # class key -> {"best": variant, "ms": {variant: ms}}

@@ -2,12 +2,17 @@
 // allocation, shared-memory matrix descriptors, the single-thread MMA issue, commit to an
 // mbarrier, and the warp-wide tensor-memory loads of the epilogue.
 //
-// Conventions used by the kernels of this library:
-//  * operands are K-major without swizzle: an 8-row x 16-byte "core matrix" is 128
-//    contiguous bytes (row r of it at byte 16 r); core matrices adjacent along K are LBO bytes
-//    apart, adjacent along M (or N) SBO bytes apart;
-//  * the accumulator D of an M = 128 MMA (cta_group::1) puts row m in tensor-memory lane m and
-//    column n in column (base + n), 32-bit each;
+// Conventions used by the kernels of this library (each checked on GB300 against a host GEMM):
+//  * operands without swizzle: an 8-row x 16-byte "core matrix" is 128 contiguous bytes (row r
+//    of it at byte 16 r).  K-major: a core row holds 16 bytes of K for one M (or N) index;
+//    MN-major: a core row holds 16 bytes of M for one K index.  In both, core matrices adjacent
+//    along K are LBO bytes apart and core matrices adjacent along M (or N) SBO bytes apart;
+//    LBO and SBO are multiples of 16 bytes (core matrices need not be 128-byte aligned);
+//  * the tensor core reads an FP32 word of a kind::tf32 operand as the TF32 value with the low
+//    13 mantissa bits dropped (truncation);
+//  * the accumulator D of an M = 128 MMA (cta_group::1) puts row m in tensor-memory lane m; of an
+//    M = 64 MMA, row m in lane 32 (m / 16) + m % 16 (lanes 16-31 of each quarter unused); column
+//    n in column (base + n), 32-bit each;
 //  * a warp may only touch the 32-lane quarter (warp id % 4) of tensor memory.
 #pragma once
 
@@ -32,10 +37,11 @@ __device__ __forceinline__ uint64_t desc_noswz(uint32_t saddr, uint32_t lbo_byte
 
 constexpr uint32_t FMT_F16 = 0, FMT_BF16 = 1, FMT_TF32 = 2;
 
-// Instruction descriptor of kind::f16 / kind::tf32: F32 accumulator, dense, both operands
-// K-major, A and B of format `fmt`, tile M x N.
-__host__ __device__ constexpr uint32_t idesc(uint32_t fmt, int M, int N) {
-    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor of kind::f16 / kind::tf32: F32 accumulator, dense, A and B of format
+// `fmt`, tile M x N; A (and B) K-major unless a_mn (b_mn) asks for MN-major.
+__host__ __device__ constexpr uint32_t idesc(uint32_t fmt, int M, int N, bool a_mn = false, bool b_mn = false) {
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // D (tensor memory) = A * B^T (+ D when acc != 0); one thread issues.
@@ -129,6 +135,16 @@ __device__ __forceinline__ void st_32x32b_x32(uint32_t taddr, const uint32_t (&r
         : "memory");
 }
 __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// Warp-wide: thread i gets lane (quarter base + i) of columns [col, col + 16).
+__device__ __forceinline__ void ld_32x32b_x16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
 
 // x rounded to TF32 (round to nearest, ties away; low 13 mantissa bits zero)
 __device__ __forceinline__ float to_tf32(float x) {

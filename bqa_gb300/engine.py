@@ -74,7 +74,7 @@ class Annealer:
 
     def __init__(self, ctx: Context, device=None, precision: str | None = None, bp_check_every: int = 4,
                  pad_bonds: bool | None = None, native: bool = True, graphs: bool | None = None,
-                 autotune: bool | None = None, reuse_blocks: bool | None = None):
+                 autotune: bool | None = None, reuse_blocks: bool | None = None, mixed: bool | None = None):
         import torch
         self.torch = torch
         if not torch.cuda.is_available():
@@ -177,6 +177,24 @@ class Annealer:
         self.zz = torch.empty(self.half, dtype=torch.float64, device=dev)
         self.norm2 = torch.zeros(1, dtype=torch.float64, device=dev)
         self._plan_table = (ctypes.c_int32 * (33 * (len(self.classes) + 1)))()
+        # Mixed-precision BP (mixed=True or BQA_GB300_MIXED=1, complex64): at storage bond dim 16
+        # the degree-3 classes sweep with the mixed kernel (BQA_VARIANT_MIXED) -- BF16 tensor-core
+        # sweeps while the BP distance is above the library's switch, FP32 sweeps after that, so
+        # the run stops on an FP32 sweep at the reference tolerance
+        if mixed is None:
+            import os
+            mixed = os.environ.get("BQA_GB300_MIXED", "0") == "1"
+        self.mixed = bool(mixed) and self.precision == "single" and self.split_sweeps and any(
+            c.degree == 3 for c in self.classes)
+        if self.mixed:
+            from .autotune import Plan
+            chis = 16
+            row = chis * (len(self.classes) + 1)
+            variants = [_lib.BQA_VARIANT_MIXED if c.degree == 3 else _lib.BQA_VARIANT_DEFAULT for c in self.classes]
+            self._plan_table[row] = 1
+            for i, v in enumerate(variants):
+                self._plan_table[row + 1 + i] = v
+            self.plans[chis] = Plan(chis=chis, split=True, variants=variants)
         self.rng = np.random.default_rng(ctx.seed)
         self.stats: list[dict] = []
         self._events: list | None = None

@@ -49,8 +49,16 @@ enum {
     BQA_VARIANT_DEFAULT = 0,  /* the kernel bqa_bp_sweep / bqa_bp_sweep_split launch */
     BQA_VARIANT_TILED = 1,    /* register-tiled: half-node (two-stage sweep) or whole-node (one stage) */
     BQA_VARIANT_GENERIC = 2,  /* generic shared-memory kernel (global-memory form beyond shared memory) */
-    BQA_VARIANT_TENSOR = 3    /* half-node kernel with tensor-core (tcgen05, 3xTF32) bond products:
+    BQA_VARIANT_TENSOR = 3,   /* half-node kernel with tensor-core (tcgen05, 3xTF32) bond products:
                                  two-stage complex64 sweeps of degree 3 at bond dim 16 */
+    BQA_VARIANT_TENSOR_BF16 = 4, /* half-node kernel with BF16 tensor-core products AND closing
+                                    contractions (FP32 accumulation; messages ~1e-3 relative),
+                                    same shapes as TENSOR */
+    BQA_VARIANT_MIXED = 5     /* precision follows the BP loop: with a loop state, a sweep after the
+                                 first whose last distance (loop_state[5]) exceeds the switch
+                                 (2^-5, or BQA_GB300_MIXED_SWITCH at library load) runs the BF16
+                                 kernel, every other sweep the FP32 CUDA-core half-node kernel;
+                                 same shapes as TENSOR */
 };
 
 /* device status word bits (written by kernels into a caller int32) */

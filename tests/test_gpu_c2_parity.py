@@ -47,3 +47,15 @@ def test_complex64_within_bar(case, monkeypatch):
     print(f"complex64 vs reference: max Bloch error {err:.3e}, mean |<Z> error| "
           f"{np.abs(got[:, 2] - want[:, 2]).mean():.3e}")
     assert err < 1.8e-4, err
+
+
+def test_complex64_mixed_precision_within_bar(case, monkeypatch):
+    """Mixed-precision BP (BF16 tensor-core sweeps while the BP distance is above 2^-5, FP32
+    sweeps to the tolerance): held to the 1e-3 <Z> bar stated for the mixed-precision form."""
+    conf, want = case
+    monkeypatch.setenv("BQA_GB300_MIXED", "1")
+    got = _bloch(conf, "single", monkeypatch)
+    err = np.abs(got - want).max()
+    print(f"complex64 mixed vs reference: max Bloch error {err:.3e}, mean |<Z> error| "
+          f"{np.abs(got[:, 2] - want[:, 2]).mean():.3e}")
+    assert err < 1e-3, err

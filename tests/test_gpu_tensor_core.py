@@ -152,3 +152,81 @@ def test_tensor_variant_refuses_other_shapes():
     with pytest.raises(_lib.BqaError) as e:
         plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
     assert e.value.status == _lib.BQA_ERR_UNSUPPORTED
+
+
+# ---- BF16 tensor-core kernel and the mixed-precision kernel --------------------------------
+
+BF16_RTOL = 2e-2   # BF16 operands (8-bit significands), FP32 accumulation
+
+
+def plan_sweep_ls(job, variant, loop_state):
+    """One two-stage sweep through bqa_bp_sweep_plan with a device loop state (reads buffer 0)."""
+    arr = (ctypes.c_int32 * len(job.classes))(*([variant] * len(job.classes)))
+    ls = torch.as_tensor(np.asarray(loop_state, dtype=np.int32), device=job.msgs[0].device)
+    job.dist_parts.zero_()
+    job.lib.call("bqa_bp_sweep_plan", job._class_array(), len(job.classes), job.chis, job.dtype, arr,
+                 _ptr(job.msgs[0]), _ptr(job.msgs[1]), _ptr(job.lu), job.E, _ptr(job.dist_parts), _ptr(ls),
+                 job.stream)
+    return job.msgs[1][: job.E * job.chis * job.chis].cpu().numpy().reshape(job.E, job.chis, job.chis)
+
+
+def loop_state(sweeps, dist):
+    ls = np.zeros(8, dtype=np.int32)
+    ls[1] = sweeps
+    ls[5] = np.array([dist], dtype=np.float32).view(np.int32)[0]
+    return ls
+
+
+def test_bf16_sweep_matches_oracle_to_bf16_precision():
+    octx, st, job = random_state("rr3_n16_chi4", 16, seed=4)
+    want = oracle_sweep(octx, st.msgs, st.degree_to_tensor)
+    got = plan_sweep(job, _lib.BQA_VARIANT_TENSOR_BF16)
+    err = rel_err(got, want)
+    print(f"bf16 tensor-core sweep vs oracle: {err:.2e}")
+    assert err < BF16_RTOL
+    assert job.lib.tc_faults(job.stream) == 0
+
+
+@pytest.mark.parametrize("n,seed", [(64, 1), (512, 2)])
+def test_bf16_sweep_matches_fp32_kernel(n, seed):
+    ctx, tens, m, job = dense_state(n, seed)
+    lo = plan_sweep(job, _lib.BQA_VARIANT_TENSOR_BF16)
+    hi = plan_sweep(job, _lib.BQA_VARIANT_TILED)
+    err = rel_err(lo, hi)
+    # messages of different slots come out of independent blocks: every slot within the bound
+    per_slot = np.abs(lo - hi).max(axis=(1, 2)) / np.abs(hi).max(axis=(1, 2))
+    print(f"n={n}: bf16 vs fp32 sweep {err:.2e} (worst slot {per_slot.max():.2e})")
+    assert err < BF16_RTOL and per_slot.max() < 5 * BF16_RTOL
+    # unit trace (the combine kernel's normalisation); Hermitian to BF16 rounding: the tensor
+    # cores form every entry of a block, not its upper triangle and a mirror (measured 6e-5)
+    assert np.abs(np.trace(lo, axis1=1, axis2=2) - 1).max() < 1e-5
+    assert np.abs(lo - np.conj(np.swapaxes(lo, 1, 2))).max() < 5e-4
+    assert job.lib.tc_faults(job.stream) == 0
+
+
+def test_bf16_kernel_with_diagonal_messages_is_exact():
+    """Diagonal incoming messages: the bond-scaling path in FP32, as in the FP32 kernels."""
+    octx, st, job = random_state("rr3_n16_chi4", 16, seed=11)
+    rng = np.random.default_rng(5)
+    lam = rng.uniform(0.1, 1.0, size=(octx.edges_number, 16))
+    m = np.zeros((octx.edges_number, 16, 16), dtype=np.complex128)
+    m[:, np.arange(16), np.arange(16)] = lam / lam.sum(axis=1, keepdims=True)
+    m = m.astype(np.complex64).astype(np.complex128)
+    job.set_state(st.degree_to_tensor, m)
+    want = oracle_sweep(octx, m, st.degree_to_tensor)
+    assert rel_err(plan_sweep(job, _lib.BQA_VARIANT_TENSOR_BF16), want) < RTOL
+    assert np.array_equal(plan_sweep(job, _lib.BQA_VARIANT_TENSOR_BF16), plan_sweep(job, _lib.BQA_VARIANT_TILED))
+
+
+def test_mixed_kernel_follows_the_loop_state():
+    """BF16 path after the first sweep while the last distance is above the switch (2^-5), the
+    FP32 CUDA-core kernel otherwise (bit-identical to it), FP32 without a loop state."""
+    ctx, tens, m, job = dense_state(128, 7)
+    fp32 = plan_sweep(job, _lib.BQA_VARIANT_TILED)
+    bf16 = plan_sweep(job, _lib.BQA_VARIANT_TENSOR_BF16)
+    assert not np.array_equal(fp32, bf16)
+    assert np.array_equal(plan_sweep(job, _lib.BQA_VARIANT_MIXED), fp32)                     # no loop state
+    assert np.array_equal(plan_sweep_ls(job, _lib.BQA_VARIANT_MIXED, loop_state(3, 0.5)), bf16)
+    assert np.array_equal(plan_sweep_ls(job, _lib.BQA_VARIANT_MIXED, loop_state(3, 1e-3)), fp32)
+    assert np.array_equal(plan_sweep_ls(job, _lib.BQA_VARIANT_MIXED, loop_state(0, 0.5)), fp32)  # first sweep
+    assert job.lib.tc_faults(job.stream) == 0
