@@ -227,7 +227,7 @@ def cpu_rate_at(cpu: dict, sweeps_per_step: float) -> float:
 ACCURACY_FIXTURE = ROOT / "tests" / "golden" / "c2_rr3_n10k_chi16.npz"
 
 
-def measured_accuracy() -> dict | None:
+def measured_accuracy(mixed: bool = False) -> dict | None:
     """<Z> / Bloch-vector error of the complex64 path against the reference at FP64, measured in
     this run: the 10,000-node instance of this workload's generator (chi 16, the first 66 steps
     of the 200-step schedule, past saturation) through bqa_gb300.run_qa, compared with the
@@ -238,21 +238,24 @@ def measured_accuracy() -> dict | None:
     from tests.golden.make_golden_c2 import config_from_fixture
     conf = config_from_fixture(ACCURACY_FIXTURE)
     want = np.load(ACCURACY_FIXTURE)["bloch"]
-    prev = os.environ.get("BQA_PRECISION")
+    saved = {k: os.environ.get(k) for k in ("BQA_PRECISION", "BQA_GB300_MIXED")}
     os.environ["BQA_PRECISION"] = "single"
+    os.environ["BQA_GB300_MIXED"] = "1" if mixed else "0"
     try:
         t0 = time.perf_counter()
         got = bqa_gb300.run_qa(dict(conf), as_arrays=True)[0][1]
         secs = time.perf_counter() - t0
     finally:
-        if prev is None:
-            os.environ.pop("BQA_PRECISION", None)
-        else:
-            os.environ["BQA_PRECISION"] = prev
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     err = np.abs(got - want)
     return {"bloch_err_max": float(err.max()), "z_err_max": float(err[:, 2].max()),
             "z_err_mean": float(err[:, 2].mean()), "seconds": round(secs, 1),
-            "where": "complex64 path vs the reference at FP64 (fixture tests/golden/c2_rr3_n10k_chi16.npz: "
+            "where": ("mixed-precision " if mixed else "") +
+                     "complex64 path vs the reference at FP64 (fixture tests/golden/c2_rr3_n10k_chi16.npz: "
                      "10,000-node instance of this generator, chi 16, first 66 steps, past saturation), "
                      "measured in this run through bqa_gb300.run_qa"}
 
@@ -382,7 +385,44 @@ def run_gpu_arm(args) -> None:
         bloch = job.bloch_vectors()
     e2e_s = time.perf_counter() - t0
 
+    # the mixed-precision form (BF16 tensor-core sweeps while the BP distance is above the
+    # switch, FP32 sweeps to the tolerance) over the same schedule window, from its own anneal
+    mixed = None
+    if args.mixed:
+        mjob = Annealer(ctx, device=dev, precision="single", mixed=True)
+        sm = 0
+        while sm < len(steps_all) - 1 and (mjob.bond_dim < args.chi or sm == 0):
+            mjob.run_layer(steps_all[sm]["xtime"], steps_all[sm]["ztime"])
+            sm += 1
+        for i in range(args.warmup):
+            mjob.run_layer(*step_at(sm + i))
+        sm += args.warmup
+        mjob.enable_kernel_timing(True)
+        mjob.stats.clear()
+        barrier()
+        torch.cuda.synchronize(dev)
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        for i in range(args.steps):
+            mjob.run_layer(*step_at(sm + i))
+        m1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        mms = m0.elapsed_time(m1)
+        mkt = mjob.kernel_times()
+        mjob.enable_kernel_timing(False)
+        msplit: dict = {}
+        for name, t, _, _ in mkt:
+            msplit[name] = msplit.get(name, 0.0) + t
+        mixed = {"ms_raw": mms, "sweeps_per_step": float(np.mean([w["sweeps"] for w in mjob.stats])),
+                 "time_split_ms": {k: round(v, 2) for k, v in sorted(msplit.items(), key=lambda kv: -kv[1])},
+                 "gpu_launches": gpu_launches(mjob, mkt, args.steps)}
+        del mjob
+        torch.cuda.empty_cache()
+
     t_max, e2e_s = max_over_ranks([ms, e2e_s], device=dev)
+    if mixed is not None:
+        mixed["ms_raw"] = max_over_ranks([mixed["ms_raw"]], device=dev)[0]
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -406,6 +446,13 @@ def run_gpu_arm(args) -> None:
                                          "value": cpu_rate_at(cpu, float(np.mean(sweeps))), "unit": "steps/s"}
     n_el = ctx.nodes_number
     accuracy = measured_accuracy()
+    if mixed is not None:
+        mms = mixed.pop("ms_raw")
+        mixed = {"value": replica_value(world, args.steps, mms), "unit": "steps/s", "ms_per_step": mms / args.steps,
+                 "vs_plain": t_max / mms, **mixed, "accuracy": measured_accuracy(mixed=True),
+                 "what": "Annealer(mixed=True): at bond dim 16 the degree-3 sweeps run the mixed kernel "
+                         "(BF16 tensor-core products and closing contractions while the last BP distance is "
+                         "above 2^-5, FP32 CUDA-core sweeps after that), same schedule window, device-timed"}
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
@@ -441,6 +488,7 @@ def run_gpu_arm(args) -> None:
                 "what": "Annealer.run_layer + bloch_vectors per step (host scalars in, all marginals out), "
                         "the timed window's steps replayed from a snapshot of its starting state"},
         "accuracy": accuracy,
+        "mixed_precision": mixed,
         "autotune": ([job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off"),
         "gpu_launches": gpu_launches(job, kt, args.steps),
         "clocks": clocks.summary(),
@@ -801,6 +849,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mixed", type=int, default=1, help="also time the mixed-precision form (1) or not (0)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: BP message kernels chosen per (degree, bond dim) by the autotuner; 0: built-in choice")
     ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout", "small", "mixed"])
