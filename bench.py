@@ -531,7 +531,7 @@ def run_sweep_mode(args) -> None:
     cls = job._class_array()
     flops, nbytes = job.bp_sweep_cost()
 
-    variant = {"default": None, "tiled": 1, "generic": 2, "tensor": 3, "tensor-bf16": 4}[args.variant]
+    variant = {"default": None, "tiled": 1, "generic": 2, "tensor": 3, "tensor-bf16": 4, "mixed": 5}[args.variant]
     plan = None if variant is None else (ctypes.c_int32 * len(job.classes))(*([variant] * len(job.classes)))
 
     def sweep():
@@ -858,7 +858,8 @@ def main() -> None:
     ap.add_argument("--rates", default="", help="serve mode: comma-separated arrival rates (jobs/s)")
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     ap.add_argument("--degree", type=int, default=3, help="sweep mode: degree of the random regular graph")
-    ap.add_argument("--variant", default="default", choices=["default", "tiled", "generic", "tensor", "tensor-bf16"],
+    ap.add_argument("--variant", default="default",
+                    choices=["default", "tiled", "generic", "tensor", "tensor-bf16", "mixed"],
                     help="sweep mode: message kernel of every class (bqa_bp_sweep_plan)")
     ap.add_argument("--synthetic", action="store_true",
                     help="svd mode: random graded Hermitian PSD matrices instead of an annealed state")

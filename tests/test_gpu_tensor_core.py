@@ -230,3 +230,34 @@ def test_mixed_kernel_follows_the_loop_state():
     assert np.array_equal(plan_sweep_ls(job, _lib.BQA_VARIANT_MIXED, loop_state(3, 1e-3)), fp32)
     assert np.array_equal(plan_sweep_ls(job, _lib.BQA_VARIANT_MIXED, loop_state(0, 0.5)), fp32)  # first sweep
     assert job.lib.tc_faults(job.stream) == 0
+
+
+def test_bf16_kernel_mixes_diagonal_and_dense_nodes():
+    """Nodes whose incoming messages are all diagonal take the FP32 bond-scaling path
+    (bit-identical to the CUDA-core kernel), the others the BF16 tensor-core path, within one
+    launch."""
+    ctx, tens, m, job = dense_state(2048, 9)
+    L = ctx.degree_to_layout[3]
+    diag_nodes = np.arange(L.batch_size) % 3 == 0
+    m = m.copy()
+    for k in range(3):
+        slots = L.input_msgs_position[k][diag_nodes]
+        d = np.real(np.diagonal(m[slots], axis1=1, axis2=2))
+        m[slots] = 0
+        m[slots[:, None], np.arange(16), np.arange(16)] = d / d.sum(axis=1, keepdims=True)
+    m = m.astype(np.complex64).astype(np.complex128)
+    job.set_state(tens, m)
+    all_diag = np.ones(L.batch_size, dtype=bool)
+    for k in range(3):
+        sl = L.input_msgs_position[k]
+        off = np.abs(m[sl] - np.einsum("eii->ei", m[sl])[:, :, None] * np.eye(16)).max(axis=(1, 2))
+        all_diag &= off == 0
+    assert all_diag.sum() > 0 and (~all_diag).sum() > 0
+    lo = plan_sweep(job, _lib.BQA_VARIANT_TENSOR_BF16)
+    hi = plan_sweep(job, _lib.BQA_VARIANT_TILED)
+    exact = L.output_msgs_position[:, all_diag].ravel()
+    approx = L.output_msgs_position[:, ~all_diag].ravel()
+    # a slot's message is (P_0 + P_1) of one node: exact where that node took the FP32 path
+    assert np.array_equal(lo[exact], hi[exact])
+    assert rel_err(lo[approx], hi[approx]) < BF16_RTOL
+    assert job.lib.tc_faults(job.stream) == 0
