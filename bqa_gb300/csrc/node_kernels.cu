@@ -65,7 +65,17 @@ struct NodeArgs {
     const int32_t* loop_state;
     typename Cx<R>::Bits* dist_parts;
     double ztime;
+    // mixed-precision BP: 0 = always run; 1 = run only on low-precision sweeps, 2 = only on the
+    // others (low_precision_sweep); the two kernels of a mixed sweep share the decision
+    int mixed_role = 0;
+    float mixed_switch = 0.f;
 };
+
+// A sweep of a BP run is a low-precision (BF16) sweep when it is not the run's first and the
+// distance of the previous sweep (loop_state[5], float bits) is above the switch.
+__device__ __forceinline__ bool low_precision_sweep(const int32_t* ls, float switch_dist) {
+    return ls != nullptr && ls[1] >= 1 && __int_as_float(ls[5]) > switch_dist;
+}
 
 // Y[s][l][i][r] = sum_j M_s[i][j] X[s][l][j][r]; X is [2][L][nin][R], Y is [2][L][nout][R],
 // M_s row-major nout x nin.  One thread owns one (s, l, r) fibre and keeps it in registers.
@@ -655,6 +665,7 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         if (a.loop_state[0]) return;
         if (a.loop_state[2]) msgs_in = a.msgs_b;
     }
+    if (a.mixed_role == 2 && low_precision_sweep(a.loop_state, a.mixed_switch)) return;
     const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
     {
         const float4* tg = reinterpret_cast<const float4*>(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS);
@@ -893,17 +904,21 @@ __global__ void __launch_bounds__(tcd3::TH, 2) tc_half_kernel_d3c16(NodeArgs<flo
 }
 
 // Half-node kernel of degree 3, bond dim 16 with BF16 tensor-core products and closing
-// contractions (tc_bf16_d3c16.cuh).  MIXED: the precision follows the BP loop -- a sweep after
-// the first of a run whose last distance (loop_state[5]) is above `switch_dist` takes the BF16
-// tensor-core path, any other sweep the FP32 CUDA-core path of the specialised half-node
-// kernel (without a loop state: FP32).  Diagonal incoming messages take the bond-scaling path
-// in FP32 either way.  Same outputs as the other half-node kernels (blocks P_s into pm).
+// contractions (tc_bf16_d3c16.cuh).  MIXED: the kernel does the low-precision sweeps of a mixed
+// BP run (low_precision_sweep) and returns at once on the others, which the specialised
+// CUDA-core half-node kernel, launched next with mixed_role 2, does in FP32.  Diagonal
+// incoming messages take the FP32 bond-scaling path.  Same outputs as the other half-node
+// kernels (blocks P_s into pm).
+//
+// Grid-stride: at most two CTAs per SM walk the `halves` half-nodes (CTA b takes b,
+// b + gridDim.x, ...), so a mixed sweep that is not this kernel's returns after a few hundred
+// CTAs; tensor memory is allocated once per CTA and the mbarrier runs two phases per half-node.
 template <bool MIXED>
-__global__ void __launch_bounds__(tcb::TH, 2) tcb_half_kernel_d3c16(NodeArgs<float> a, float switch_dist) {
+__global__ void __launch_bounds__(tcb::TH, 2) tcb_half_kernel_d3c16(NodeArgs<float> a, float switch_dist, int halves) {
     constexpr int CHI = 16, D = 3, N2 = CHI * CHI, PS = CHI * CHI * CHI, TH = tcb::TH;
     extern __shared__ double4 smem_raw[];
     unsigned char* reg = reinterpret_cast<unsigned char*>(smem_raw);
-    float2* const V1 = reinterpret_cast<float2*>(reg);   // FP32 buffers of the CUDA-core paths
+    float2* const V1 = reinterpret_cast<float2*>(reg);   // FP32 buffers of the bond-scaling path
     float2* const V2 = V1 + PS;
     float2* const V0 = V1 + 2 * PS;
     float2* const sP = V1 + 3 * PS;
@@ -911,118 +926,127 @@ __global__ void __launch_bounds__(tcb::TH, 2) tcb_half_kernel_d3c16(NodeArgs<flo
     uint64_t* bar = reinterpret_cast<uint64_t*>(reg + tcb::REGION);
     uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
     const float2* msgs_in = a.msgs_a;
-    bool low = !MIXED;
     if (a.loop_state != nullptr) {
         if (a.loop_state[0]) return;
         if (a.loop_state[2]) msgs_in = a.msgs_b;
-        if (MIXED) low = a.loop_state[1] >= 1 && __int_as_float(a.loop_state[5]) > switch_dist;
     }
+    if (MIXED && !low_precision_sweep(a.loop_state, switch_dist)) return;
     const int t = threadIdx.x, warp = t >> 5;
-    const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
-    float4 tv[8];
-    tcd3::load_share(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS, tv);
-    int offdiag = 0;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
-        const int j = t / CHI, i = t - j * CHI;
-        const float2 v = mg[i * CHI + j];
-        sMt[k * N2 + t] = v;
-        offdiag |= (i != j) && (v.x != 0.f || v.y != 0.f);
+    if (t == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_mbar_init();
     }
-    const bool diag = !__syncthreads_or(offdiag);
-    auto out_block = [&](int idx) { return a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2; };
-    if (!diag && low) {
-        if (warp == 0) {
-            tc::alloc(slot, tcb::TMEM_COLS);
-            tc::relinquish();
+    const uint32_t rb = tc::smem_u32(reg);
+    uint32_t tmem = 0;
+    bool tmem_held = false;
+    namespace q = tiled::d3c16;
+    constexpr int CT = 160;
+    for (int h = blockIdx.x; h < halves; h += gridDim.x) {
+        const int node = h >> 1, s = h & 1;
+        float4 tv[8];
+        tcd3::load_share(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS, tv);
+        int offdiag = 0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const float2* mg = msgs_in + (size_t)a.in_pos[node * D + k] * N2;
+            const int j = t / CHI, i = t - j * CHI;
+            const float2 v = mg[i * CHI + j];
+            sMt[k * N2 + t] = v;
+            offdiag |= (i != j) && (v.x != 0.f || v.y != 0.f);
         }
-        if (t == 0) {
-            tc::mbar_init(bar, 1);
-            tc::fence_mbar_init();
-        }
-        tcb::store_products_b(sMt, reg);
-        tcb::store_products_a(tv, reg);
-        tc::fence_proxy_async();
-        tc::fence_before();
-        __syncthreads();
-        tc::fence_after();
-        const uint32_t tmem = *slot;
-        const uint32_t rb = tc::smem_u32(reg);
-        if (t == 0) {
-            tcb::issue_products(tmem, rb);
-            tc::commit(bar);
-        }
-        // phase 0: the products; phase 1: the closing contractions
-        int late = __syncthreads_or(!tc::mbar_wait(bar, 0, tcb::WAIT_CYCLES)) ? 1 : 0;
-        if (!late) {
-            tc::fence_after();
-            tcb::epilogue_products(tmem, reg);
+        const bool diag = !__syncthreads_or(offdiag);
+        auto out_block = [&](int idx) { return a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2; };
+        if (!diag) {
+            if (!tmem_held) {
+                if (warp == 0) {
+                    tc::alloc(slot, tcb::TMEM_COLS);
+                    tc::relinquish();
+                }
+                tc::fence_before();
+                __syncthreads();
+                tc::fence_after();
+                tmem = *slot;
+                tmem_held = true;
+            }
+            tcb::store_products_b(sMt, reg);
+            tcb::store_products_a(tv, reg);
             tc::fence_proxy_async();
             tc::fence_before();
             __syncthreads();
+            tc::fence_after();
             if (t == 0) {
-                tc::fence_after();
-                tcb::issue_closes(tmem, rb);
+                tcb::issue_products(tmem, rb);
                 tc::commit(bar);
             }
-            late = __syncthreads_or(!tc::mbar_wait(bar, 1, tcb::WAIT_CYCLES)) ? 2 : 0;
+            // phase 0: the products; phase 1: the closing contractions
+            int late = __syncthreads_or(!tc::mbar_wait(bar, 0, tcb::WAIT_CYCLES)) ? 1 : 0;
             if (!late) {
                 tc::fence_after();
-                if ((warp & 3) < 2) {
-                    // warps 0, 1: P_0 (columns 0-31) and P_1 (64-95); warps 4, 5: P_2 (32-63)
-                    if (warp < 4) {
-                        tcb::epilogue_close(tmem, 0, reinterpret_cast<float*>(out_block(0)));
-                        tcb::epilogue_close(tmem, 2, reinterpret_cast<float*>(out_block(1)));
-                    } else {
-                        tcb::epilogue_close(tmem, 1, reinterpret_cast<float*>(out_block(2)));
+                tcb::epilogue_products(tmem, reg);
+                tc::fence_proxy_async();
+                tc::fence_before();
+                __syncthreads();
+                if (t == 0) {
+                    tc::fence_after();
+                    tcb::issue_closes(tmem, rb);
+                    tc::commit(bar);
+                }
+                late = __syncthreads_or(!tc::mbar_wait(bar, 1, tcb::WAIT_CYCLES)) ? 2 : 0;
+                if (!late) {
+                    tc::fence_after();
+                    if ((warp & 3) < 2) {
+                        // warps 0, 1: P_0 (columns 0-31) and P_1 (64-95); warps 4, 5: P_2 (32-63)
+                        if (warp < 4) {
+                            tcb::epilogue_close(tmem, 0, reinterpret_cast<float*>(out_block(0)));
+                            tcb::epilogue_close(tmem, 2, reinterpret_cast<float*>(out_block(1)));
+                        } else {
+                            tcb::epilogue_close(tmem, 1, reinterpret_cast<float*>(out_block(2)));
+                        }
                     }
                 }
             }
+            if (late) {
+                // the MMAs did not complete in time: count the fault, give them one more bounded
+                // wait and stop this CTA (its remaining blocks stay unwritten)
+                if (t == 0) atomicAdd(&g_tc_faults, 1);
+                tc::mbar_wait(bar, late - 1, tcb::WAIT_CYCLES);
+                break;
+            }
+            tc::fence_before();   // this half-node's tensor-memory reads precede the next MMAs
+            __syncthreads();
+            continue;
         }
-        if (late) {
-            // the MMAs did not complete in time: count the fault and give them one more bounded
-            // wait before the tensor memory is released; this CTA's blocks stay unwritten
-            if (t == 0) atomicAdd(&g_tc_faults, 1);
-            tc::mbar_wait(bar, late - 1, tcb::WAIT_CYCLES);
-        }
-        tc::fence_before();
+        // all incoming messages diagonal: bond scalings in FP32, closing contractions on the CUDA cores
+        tcd3::store_share_swizzled(tv, V0);
         __syncthreads();
-        if (warp == 0) tc::dealloc(tmem, tcb::TMEM_COLS);
-        return;
-    }
-    namespace q = tiled::d3c16;
-    tcd3::store_share_swizzled(tv, V0);
-    __syncthreads();
-    if (diag) {
         tiled::diag_scale3<CHI, TH, 7>(V0, V1, sMt + N2, 1);
         tiled::diag_scale3<CHI, TH, 7>(V0, V2, sMt + 2 * N2, 2);
         __syncthreads();
         tiled::diag_scale3<CHI, TH, 7>(V0, V0, sMt, 0);
-    } else {
-        q::prod1(V0, V1, sMt + N2);
         __syncthreads();
-        q::prod2(V0, V2, sMt + 2 * N2);
+        float2* const sPb[2] = {sP, sP + N2};
+        int pend = -1, cur = 0;
+        auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
+            constexpr int IDX = decltype(idx_tag)::value;
+            if (t < CT) q::close<IDX>(X, R, sPb[cur]);
+            else if (pend >= 0)
+                tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t - CT,
+                                             TH - CT);
+            __syncthreads();
+            pend = IDX;
+            cur ^= 1;
+        };
+        emit_s(std::integral_constant<int, 0>{}, V1, V2);
+        emit_s(std::integral_constant<int, 2>{}, V0, V1);
+        emit_s(std::integral_constant<int, 1>{}, V0, V2);
+        tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t, TH);
         __syncthreads();
-        q::prod0_inplace(V0, sMt);
     }
-    __syncthreads();
-    constexpr int CT = 160;
-    float2* const sPb[2] = {sP, sP + N2};
-    int pend = -1, cur = 0;
-    auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
-        constexpr int IDX = decltype(idx_tag)::value;
-        if (t < CT) q::close<IDX>(X, R, sPb[cur]);
-        else if (pend >= 0)
-            tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t - CT, TH - CT);
+    if (tmem_held) {
+        tc::fence_before();
         __syncthreads();
-        pend = IDX;
-        cur ^= 1;
-    };
-    emit_s(std::integral_constant<int, 0>{}, V1, V2);
-    emit_s(std::integral_constant<int, 2>{}, V0, V1);
-    emit_s(std::integral_constant<int, 1>{}, V0, V2);
-    tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t, TH);
+        if (warp == 0) tc::dealloc(tmem, tcb::TMEM_COLS);
+    }
 }
 
 // BP distance above which the mixed-precision (3, 16) kernel takes its BF16 path; the
@@ -1032,12 +1056,27 @@ static const float g_mixed_switch = [] {
     return v ? (float)atof(v) : 0.03125f;
 }();
 
+// multiprocessors of the current device (cached per device ordinal)
+static int sm_count() {
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 152;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
 template <bool MIXED>
 static int launch_tcb_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
     const size_t smem = (size_t)tcb::REGION + 16;
     int rc = ensure_smem((const void*)tcb_half_kernel_d3c16<MIXED>, smem, "bf16 tensor-core half kernel");
     if (rc) return rc;
-    tcb_half_kernel_d3c16<MIXED><<<2 * count, tcb::TH, smem, st>>>(args, g_mixed_switch);
+    const int halves = 2 * count;
+    tcb_half_kernel_d3c16<MIXED><<<std::min(halves, 2 * sm_count()), tcb::TH, smem, st>>>(args, g_mixed_switch,
+                                                                                             halves);
     return check_launch("bf16 tensor-core half kernel");
 }
 
@@ -1485,9 +1524,21 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t c
                 return set_error(BQA_ERR_UNSUPPORTED, "bqa_bp_sweep_plan: the tensor-core kernels serve the two-stage "
                                  "complex64 sweep of degree 3 at bond dim 16 (got degree %d, bond dim %d)", k.degree, chi);
             const NodeArgs<float> ca = class_args<float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state);
-            rc = v == BQA_VARIANT_TENSOR ? launch_tc_half(ca, k.count, st)
-                 : v == BQA_VARIANT_TENSOR_BF16 ? launch_tcb_half<false>(ca, k.count, st)
-                                                : launch_tcb_half<true>(ca, k.count, st);
+            if (v == BQA_VARIANT_TENSOR) {
+                rc = launch_tc_half(ca, k.count, st);
+            } else if (v == BQA_VARIANT_TENSOR_BF16) {
+                rc = launch_tcb_half<false>(ca, k.count, st);
+            } else {
+                // the BF16 kernel takes the low-precision sweeps, the CUDA-core kernel the others
+                rc = launch_tcb_half<true>(ca, k.count, st);
+                if (!rc) {
+                    NodeArgs<float> cb = ca;
+                    cb.mixed_role = 2;
+                    cb.mixed_switch = g_mixed_switch;
+                    rc = g_use_specialized ? launch_half_k<3, 16, true>(cb, k.count, st)
+                                           : launch_half_k<3, 16, false>(cb, k.count, st);
+                }
+            }
         } else if (v == BQA_VARIANT_TILED && pm && dtype == BQA_C64 && k.degree == 3 && chi == 16) {
             // the CUDA-core half-node kernel, whatever the default (3, 16) kernel is
             rc = g_use_specialized
