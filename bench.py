@@ -64,10 +64,12 @@ def peaks() -> tuple[dict, str]:
     return FALLBACK_PEAKS, "fallback"
 
 
-def fp32_peak_tflops(lib, dev) -> float:
+def fp32_peak_tflops(dev) -> float:
     """FP32 FMA throughput of this GPU (bqa_fp32_fma_probe: 16 independent FMA chains per
     thread, 8 CTAs of 256 per SM), median of 5 timed launches after 2 untimed."""
     import torch
+    from bqa_gb300 import _lib
+    probes = _lib.load_probes()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     blocks, iters = 8 * sms, 4000
     out = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
@@ -76,7 +78,8 @@ def fp32_peak_tflops(lib, dev) -> float:
     for i in range(7):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(st)
-        lib.call("bqa_fp32_fma_probe", blocks, iters, out.data_ptr(), st.cuda_stream)
+        if probes.bqa_fp32_fma_probe(blocks, iters, out.data_ptr(), st.cuda_stream) != 0:
+            raise RuntimeError("bqa_fp32_fma_probe failed")
         b.record(st)
         torch.cuda.synchronize(dev)
         if i >= 2:
@@ -85,10 +88,12 @@ def fp32_peak_tflops(lib, dev) -> float:
     return flops / (float(np.median(ts)) / 1e3) / 1e12
 
 
-def mma_peak_tflops(lib, dev, kind: int) -> float:
+def mma_peak_tflops(dev, kind: int) -> float:
     """Warp-level mma.sync throughput (bqa_mma_probe; kind 0 bf16 m16n8k16, 1 tf32 m16n8k8), 8
     CTAs of 256 per SM, best of 5 timed launches after 1 untimed."""
     import torch
+    from bqa_gb300 import _lib
+    probes = _lib.load_probes()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     blocks, iters = 8 * sms, 2000
     out = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
@@ -97,7 +102,8 @@ def mma_peak_tflops(lib, dev, kind: int) -> float:
     for i in range(6):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(st)
-        lib.call("bqa_mma_probe", kind, blocks, iters, out.data_ptr(), st.cuda_stream)
+        if probes.bqa_mma_probe(kind, blocks, iters, out.data_ptr(), st.cuda_stream) != 0:
+            raise RuntimeError("bqa_mma_probe failed")
         b.record(st)
         torch.cuda.synchronize(dev)
         if i >= 1:
@@ -438,7 +444,7 @@ def run_gpu_arm(args) -> None:
     for name, t, _, _ in kt:
         by_name[name] = by_name.get(name, 0.0) + t
     pk, pk_kind = peaks()
-    fp32_peak = fp32_peak_tflops(job.lib, dev)
+    fp32_peak = fp32_peak_tflops(dev)
     achieved = bp_flops / (bp_ms / 1000.0) / 1e12 if bp_ms > 0 else 0.0
     cpu = cpu_reference(args.steps, args.warmup, args.n, args.chi) if not args.no_cpu_baseline else None
     if cpu is not None:
@@ -480,8 +486,8 @@ def run_gpu_arm(args) -> None:
                                    "achieved_executed": achieved * EXECUTED_FRACTION.get(args.chi, 1.0),
                                    "frac": achieved * EXECUTED_FRACTION.get(args.chi, 1.0) / fp32_peak,
                                    "probe": "bqa_fp32_fma_probe, 16 independent FMA chains per thread"},
-                     "legacy_mma_peaks_measured": {"bf16_m16n8k16": mma_peak_tflops(job.lib, dev, 0),
-                                                   "tf32_m16n8k8": mma_peak_tflops(job.lib, dev, 1),
+                     "legacy_mma_peaks_measured": {"bf16_m16n8k16": mma_peak_tflops(dev, 0),
+                                                   "tf32_m16n8k8": mma_peak_tflops(dev, 1),
                                                    "unit": "TFLOP/s", "probe": "bqa_mma_probe"}},
         "e2e": {"value": replica_value(world, args.steps, 1000.0 * e2e_s), "unit": "steps/s", "h2d_bytes_per_step": 16,
                 "d2h_bytes_per_step": int(n_el * 4 * 8 + 2 * args.chi * 4 + 64),

@@ -9,7 +9,7 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 10
+ABI_VERSION = 11
 BQA_C64 = 0
 BQA_C128 = 1
 BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC, BQA_VARIANT_TENSOR = 0, 1, 2, 3
@@ -93,8 +93,6 @@ SIGNATURES = {
                                     c_void_p]),
     "bqa_canonicalize_noalloc": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_void_p]),
-    "bqa_fp32_fma_probe": (c_int32, [c_int32, c_int32, c_void_p, c_void_p]),
-    "bqa_mma_probe": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p]),
     "bqa_run_layer": (c_int32, [POINTER(BqaJob), c_double, c_double, POINTER(BqaLayerInfo), c_void_p]),
     "bqa_graph_cache_create": (c_int32, [POINTER(c_void_p)]),
     "bqa_graph_cache_destroy": (c_int32, [c_void_p]),
@@ -161,3 +159,26 @@ def load() -> Library:
     if _LIB is None:
         _LIB = Library()
     return _LIB
+
+
+PROBE_LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300_probes.so"
+PROBE_SIGNATURES = {
+    "bqa_fp32_fma_probe": (c_int32, [c_int32, c_int32, c_void_p, c_void_p]),
+    "bqa_mma_probe": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p]),
+}
+_PROBES = None
+
+
+def load_probes():
+    """The measurement probes' library (include/bqa_gb300_probes.h), separate from the backend."""
+    global _PROBES
+    if _PROBES is None:
+        if not PROBE_LIB_PATH.exists():
+            raise BqaError(f"{PROBE_LIB_PATH} is missing: build it with python -m bqa_gb300.build")
+        dll = ctypes.CDLL(str(PROBE_LIB_PATH))
+        for name, (res, args) in PROBE_SIGNATURES.items():
+            fn = getattr(dll, name)
+            fn.restype = res
+            fn.argtypes = args
+        _PROBES = dll
+    return _PROBES

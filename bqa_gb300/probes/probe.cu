@@ -1,8 +1,13 @@
+// Measurement-only probes, built into their own library (libbqa_gb300_probes.so, declared in
+// include/bqa_gb300_probes.h) so that the backend's ABI holds only the hot path.
+//
 // FP32 FMA throughput probe: the compute ceiling of the complex64 CUDA-core kernels.
 // Every thread runs 16 independent FMA chains (no memory traffic in the loop) and writes one
 // sum so the work cannot be removed; FLOPs = 2 * 16 * iters * blocks * 256.
-#include "common.cuh"
-#include "internal.h"
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/bqa_gb300_probes.h"
 
 namespace bqa {
 
@@ -61,16 +66,18 @@ __global__ void __launch_bounds__(256) mma_probe_kernel(float* __restrict__ out,
 
 }  // namespace bqa
 
+static int32_t launch_status() { return cudaGetLastError() == cudaSuccess ? 0 : 3; }
+
 extern "C" int32_t bqa_mma_probe(int32_t kind, int32_t blocks, int32_t iters, float* out, void* stream) {
-    if (blocks < 1 || iters < 1 || !out || (kind != 0 && kind != 1))
-        return bqa::set_error(BQA_ERR_ARG, "bqa_mma_probe: bad argument");
-    if (kind == 0) bqa::mma_probe_kernel<0><<<blocks, 256, 0, bqa::as_stream(stream)>>>(out, iters);
-    else bqa::mma_probe_kernel<1><<<blocks, 256, 0, bqa::as_stream(stream)>>>(out, iters);
-    return bqa::check_launch("mma_probe");
+    if (blocks < 1 || iters < 1 || !out || (kind != 0 && kind != 1)) return 1;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (kind == 0) bqa::mma_probe_kernel<0><<<blocks, 256, 0, st>>>(out, iters);
+    else bqa::mma_probe_kernel<1><<<blocks, 256, 0, st>>>(out, iters);
+    return launch_status();
 }
 
 extern "C" int32_t bqa_fp32_fma_probe(int32_t blocks, int32_t iters, float* out, void* stream) {
-    if (blocks < 1 || iters < 1 || !out) return bqa::set_error(BQA_ERR_ARG, "bqa_fp32_fma_probe: bad argument");
-    bqa::fma_probe_kernel<<<blocks, 256, 0, bqa::as_stream(stream)>>>(out, iters, 0.999f);
-    return bqa::check_launch("fp32_fma_probe");
+    if (blocks < 1 || iters < 1 || !out) return 1;
+    bqa::fma_probe_kernel<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(out, iters, 0.999f);
+    return launch_status();
 }

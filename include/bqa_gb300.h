@@ -407,24 +407,6 @@ int32_t bqa_layout_class(int32_t degree, int32_t count, const int32_t* deg, cons
                          const double* node_field, int32_t* node_ids, int32_t* position, int32_t* in_pos,
                          int32_t* out_pos, int32_t* lmbd_pos, double* edge_ampl, double* node_ampl, void* stream);
 
-/*
- * FP32 FMA throughput probe (no reference counterpart; measurement only): `blocks` CTAs of 256
- * threads each run 16 independent FMA chains for `iters` iterations, 2 * 16 * iters *
- * blocks * 256 FLOP in all, and write one float per thread to out[blocks * 256].  Timed by
- * the caller, it gives the FP32 CUDA-core peak the complex64 kernels are measured against.
- */
-int32_t bqa_fp32_fma_probe(int32_t blocks, int32_t iters, float* out, void* stream);
-
-/*
- * Warp-level tensor-core throughput probe (no reference counterpart; measurement only):
- * `blocks` CTAs of 256 threads, every warp running 8 independent mma.sync accumulator chains
- * for `iters` iterations on register operands -- kind 0: m16n8k16 bf16 inputs, f32
- * accumulate (4096 FLOP per instruction); kind 1: m16n8k8 tf32 (2048 FLOP).  FLOPs =
- * per-instruction FLOP * 8 * iters * blocks * 8; one float per thread goes to
- * out[blocks * 256].  The legacy tensor path's ceiling, next to the FP32 one.
- */
-int32_t bqa_mma_probe(int32_t kind, int32_t blocks, int32_t iters, float* out, void* stream);
-
 #ifdef __cplusplus
 }
 #endif

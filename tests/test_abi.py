@@ -10,10 +10,11 @@ from bqa_gb300 import _lib
 from bqa_gb300.build import build_library
 
 HEADER = Path(__file__).resolve().parents[1] / "include" / "bqa_gb300.h"
+PROBE_HEADER = Path(__file__).resolve().parents[1] / "include" / "bqa_gb300_probes.h"
 
 
-def declared_functions() -> set:
-    text = HEADER.read_text()
+def declared_functions(header=HEADER) -> set:
+    text = header.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return set(re.findall(r"\b(bqa_[a-z0-9_]+)\s*\(", text))
 
@@ -31,6 +32,16 @@ def test_header_and_binding_agree():
 def test_every_declared_symbol_is_exported(lib):
     for name in declared_functions():
         assert hasattr(lib.dll, name), name
+
+
+def test_probes_live_in_their_own_library(lib):
+    """The measurement probes are declared and exported by the probe library only."""
+    probes = declared_functions(PROBE_HEADER)
+    assert probes == set(_lib.PROBE_SIGNATURES) == {"bqa_fp32_fma_probe", "bqa_mma_probe"}
+    dll = _lib.load_probes()
+    for name in probes:
+        assert hasattr(dll, name), name
+        assert not hasattr(lib.dll, name), name
 
 
 def test_abi_version_and_limits(lib):

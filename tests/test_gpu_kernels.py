@@ -340,27 +340,27 @@ def test_specialised_half_kernel_bit_identical_to_generic(tmp_path):
 
 
 def test_fp32_fma_probe_runs():
-    """The FP32 throughput probe launches, writes every output and gives a plausible rate."""
+    """The FP32 throughput probe (probe library) launches, writes every output and gives a
+    plausible rate."""
     import bench
-    lib = _lib.load()
+    probes = _lib.load_probes()
     out = torch.full((152 * 256,), float("nan"), device="cuda")
-    lib.call("bqa_fp32_fma_probe", 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream)
+    assert probes.bqa_fp32_fma_probe(152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream) == 0
     torch.cuda.synchronize()
     assert torch.isfinite(out).all()
-    tf = bench.fp32_peak_tflops(lib, torch.device("cuda"))
+    tf = bench.fp32_peak_tflops(torch.device("cuda"))
     assert 5.0 < tf < 500.0
 
 
 def test_mma_probe_runs():
     """The warp-level MMA probe launches both kinds, writes every output, gives plausible rates."""
     import bench
-    lib = _lib.load()
+    probes = _lib.load_probes()
     out = torch.full((152 * 256,), float("nan"), device="cuda")
     for kind in (0, 1):
-        lib.call("bqa_mma_probe", kind, 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream)
+        assert probes.bqa_mma_probe(kind, 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream) == 0
         torch.cuda.synchronize()
         assert torch.isfinite(out).all()
-    with pytest.raises(_lib.BqaError):
-        lib.call("bqa_mma_probe", 2, 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream)
+    assert probes.bqa_mma_probe(2, 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream) == 1
     for kind in (0, 1):
-        assert 10.0 < bench.mma_peak_tflops(lib, torch.device("cuda"), kind) < 5000.0
+        assert 10.0 < bench.mma_peak_tflops(torch.device("cuda"), kind) < 5000.0
