@@ -452,6 +452,10 @@ def run_gpu_arm(args) -> None:
                                          "value": cpu_rate_at(cpu, float(np.mean(sweeps))), "unit": "steps/s"}
     n_el = ctx.nodes_number
     accuracy = measured_accuracy()
+    # serving: a bounded Poisson stream of small jobs through the continuous-batching server
+    serving = None
+    if args.serve_jobs > 0:
+        serving = {"stream": SERVING_STREAM, **serving_measurement(args.serve_jobs, args.rate)}
     if mixed is not None:
         mms = mixed.pop("ms_raw")
         mixed = {"value": replica_value(world, args.steps, mms), "unit": "steps/s", "ms_per_step": mms / args.steps,
@@ -495,6 +499,7 @@ def run_gpu_arm(args) -> None:
                         "the timed window's steps replayed from a snapshot of its starting state"},
         "accuracy": accuracy,
         "mixed_precision": mixed,
+        "serving": serving,
         "autotune": ([job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off"),
         "gpu_launches": gpu_launches(job, kt, args.steps),
         "clocks": clocks.summary(),
@@ -656,12 +661,16 @@ def serving_stream(jobs: int, rate: float, seed: int = 0):
     return out
 
 
-def run_serve_mode(args) -> None:
-    """p50/p99 job latency and jobs/s of Poisson job streams (one per rate in --rates) through
-    the continuous-batching server, next to the same jobs run one at a time in arrival order
-    (each job's latency then includes its wait behind the earlier ones).  Both sides start
-    from configs already compiled into contexts, so both time device state set-up, the
-    anneal and the read-out."""
+SERVING_STREAM = "random d-regular, d in {3,4}, n log-uniform in [100, 20000], chi in {4, 8}, 20 or 50 steps"
+
+
+def serving_measurement(jobs: int, rate: float, seed: int = 1) -> dict:
+    """p50/p99 job latency and jobs/s of one Poisson job stream through the continuous-batching
+    server with packed BP runs (the jobs waiting for BP swept in shared launches), through the
+    server with each job's BP run in its own launches, and with the same jobs run one at a time
+    in arrival order (each job's latency then includes its wait behind the earlier ones).  All
+    three start from configs already compiled into contexts, so all time device state set-up,
+    the anneal and the read-out."""
     import torch
     import bqa_gb300
     from bqa_gb300 import config as cfg
@@ -682,35 +691,43 @@ def run_serve_mode(args) -> None:
         torch.cuda.synchronize()
         return out
 
-    rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
-    results = []
-    for rate in rates:
-        stream = serving_stream(args.jobs, rate, seed=1)
-        bqa_gb300.run_qa(dict(stream[0][1]))              # warm-up: compile paths and allocator
-        torch.cuda.synchronize()
-        srv = JobServer()
+    stream = serving_stream(jobs, rate, seed=seed)
+    bqa_gb300.run_qa(dict(stream[0][1]))              # warm-up: compile paths and allocator
+    torch.cuda.synchronize()
+
+    def serve(pack_bp: bool) -> dict:
+        srv = JobServer(pack_bp=pack_bp)
         for t, conf in stream:
             srv.submit(dict(conf), arrival=t)
         srv._t0 = time.perf_counter()
         srv.run(timeout=1800)
-        served = srv.stats()
-        ctxs = [(t, build_context(dict(conf))) for t, conf in stream]
-        t0 = time.perf_counter()
-        lat = []
-        for t, ctx in ctxs:
-            now = time.perf_counter() - t0
-            if now < t:
-                time.sleep(t - now)
-            run_one(ctx)
-            lat.append(time.perf_counter() - t0 - t)
-        seq_span = time.perf_counter() - t0 - ctxs[0][0]
-        results.append({"rate_per_s": rate, "served": served,
-                        "one_at_a_time": {"p50_s": float(np.percentile(lat, 50)),
-                                          "p99_s": float(np.percentile(lat, 99)),
-                                          "jobs_per_s": args.jobs / seq_span}})
-    print(json.dumps({"mode": "serve", "jobs": args.jobs,
-                      "stream": "random d-regular, d in {3,4}, n log-uniform in [100, 20000], chi in {4, 8}, "
-                                "20 or 50 steps", "rates": results}))
+        out = srv.stats()
+        srv.close()
+        return out
+
+    serve(True)                                       # warm-up of the packed kernels
+    served = serve(True)
+    unpacked = serve(False)
+    ctxs = [(t, build_context(dict(conf))) for t, conf in stream]
+    t0 = time.perf_counter()
+    lat = []
+    for t, ctx in ctxs:
+        now = time.perf_counter() - t0
+        if now < t:
+            time.sleep(t - now)
+        run_one(ctx)
+        lat.append(time.perf_counter() - t0 - t)
+    seq_span = time.perf_counter() - t0 - ctxs[0][0]
+    return {"rate_per_s": rate, "jobs": jobs, "served": served, "served_unpacked_bp": unpacked,
+            "one_at_a_time": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                              "jobs_per_s": jobs / seq_span}}
+
+
+def run_serve_mode(args) -> None:
+    """serving_measurement for every rate in --rates (or --rate)."""
+    rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+    results = [serving_measurement(args.jobs, rate) for rate in rates]
+    print(json.dumps({"mode": "serve", "jobs": args.jobs, "stream": SERVING_STREAM, "rates": results}))
 
 
 def run_layout_mode(args) -> None:
@@ -817,7 +834,7 @@ def run_mixed_mode(args) -> None:
     side = max(4, int(round(np.sqrt(1.8 * args.n))))
     ctx = build_context(instances.mixed_degree_job(rows=side, cols=side, extra=args.n, chi=args.chi))
     steps = [i for i in ctx.instructions if isinstance(i, dict)]
-    job = Annealer(ctx)
+    job = Annealer(ctx, autotune=bool(args.autotune))
     s, t0 = 0, time.perf_counter()
     while job.bond_dim < args.chi and s < 60:
         job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
@@ -843,7 +860,8 @@ def run_mixed_mode(args) -> None:
                       ctx.degree_to_layout.items()}, "chi": job.bond_dim, "prep_steps": s - args.warmup,
                       "prep_s": round(prep, 1), "steps_per_s": args.steps / (ms / 1e3),
                       "sweeps_per_step": float(np.mean([w["sweeps"] for w in job.stats])),
-                      "ms_per_step_split": split, "scratch_bytes": job.scratch_elems * 8}))
+                      "ms_per_step_split": split, "scratch_bytes": job.scratch_elems * 8,
+                      "autotune": ([job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off")}))
 
 
 def main() -> None:
@@ -856,11 +874,14 @@ def main() -> None:
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed", type=int, default=1, help="also time the mixed-precision form (1) or not (0)")
+    ap.add_argument("--serve-jobs", type=int, default=64,
+                    help="jobs of the serving stream measured beside the anneal (0: none)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: BP message kernels chosen per (degree, bond dim) by the autotuner; 0: built-in choice")
     ap.add_argument("--mode", default="anneal", choices=["anneal", "sweep", "svd", "serve", "layout", "small", "mixed"])
     ap.add_argument("--jobs", type=int, default=32)
-    ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--rate", type=float, default=200.0,
+                    help="serving stream arrival rate (jobs/s); the default is the top of the stated 1-200 sweep")
     ap.add_argument("--rates", default="", help="serve mode: comma-separated arrival rates (jobs/s)")
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     ap.add_argument("--degree", type=int, default=3, help="sweep mode: degree of the random regular graph")

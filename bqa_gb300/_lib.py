@@ -9,7 +9,7 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 11
+ABI_VERSION = 12
 BQA_C64 = 0
 BQA_C128 = 1
 BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC, BQA_VARIANT_TENSOR = 0, 1, 2, 3
@@ -99,6 +99,10 @@ SIGNATURES = {
     "bqa_run_layer_graph": (c_int32, [POINTER(BqaJob), c_void_p, c_double, c_double, POINTER(BqaLayerInfo),
                                       c_void_p]),
     "bqa_run_bp_graph": (c_int32, [POINTER(BqaJob), c_void_p, POINTER(BqaLayerInfo), c_void_p]),
+    "bqa_gate_layer": (c_int32, [POINTER(BqaJob), c_double, c_double, POINTER(BqaLayerInfo), c_void_p]),
+    "bqa_bp_begin": (c_int32, [POINTER(BqaJob), c_void_p]),
+    "bqa_bp_packed": (c_int32, [POINTER(POINTER(BqaJob)), c_int32, c_int32, c_void_p, POINTER(c_int32), c_void_p]),
+    "bqa_bp_end": (c_int32, [POINTER(BqaJob), POINTER(c_int32), POINTER(BqaLayerInfo)]),
     "bqa_layout_degrees": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
                                      c_void_p, c_void_p, c_void_p, c_void_p]),
     "bqa_layout_class": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_void_p,

@@ -11,7 +11,10 @@ bond dim and the number of nodes:
   whole-node CTAs in the one-stage form; complex64, degree 2-4, bond dims 4/8/12/16), the
   generic shared-memory kernel (global-memory form for nodes beyond shared memory), or, in the
   two-stage form at degree 3, bond dim 16, the half-node kernel whose bond products run on the
-  tensor cores (tcgen05, 3xTF32).
+  tensor cores (tcgen05, 3xTF32);
+* for the generic kernel, the warps per node (CTA size): its own choice (up to 8 warps, from
+  the node's fibre count) or 16 or 32 warps at bond dims <= 8, where large-degree nodes fill
+  so much shared memory that one or two CTAs share an SM.
 
 ``tune(annealer)`` times every candidate of every class on the job's live state (CUDA events
 on the job's stream, a warm-up launch then ``reps`` timed launches, each reading the current
@@ -36,6 +39,18 @@ from . import _lib
 VARIANT_NAMES = {_lib.BQA_VARIANT_DEFAULT: "default", _lib.BQA_VARIANT_TILED: "tiled",
                  _lib.BQA_VARIANT_GENERIC: "generic", _lib.BQA_VARIANT_TENSOR: "tensor",
                  _lib.BQA_VARIANT_TENSOR_BF16: "tensor-bf16", _lib.BQA_VARIANT_MIXED: "mixed"}
+_SPLIT = 1 << 20   # flag of a two-stage timing in the tuner's per-class records
+
+
+def generic_warps(warps: int) -> int:
+    """Plan entry of the generic kernel with CTAs of ``warps`` warps (bqa_bp_sweep_plan)."""
+    return _lib.BQA_VARIANT_GENERIC | (int(warps) << 8)
+
+
+def variant_name(v: int) -> str:
+    """``generic/16w`` for the generic kernel at 16 warps per node, else the variant's name."""
+    base = VARIANT_NAMES[v & 0xff]
+    return f"{base}/{v >> 8}w" if v >> 8 else base
 
 _LOCK = threading.Lock()
 _CLASS_CACHE: dict[tuple, dict] = {}     # class key -> {"best": variant, "ms": {variant: ms}}
@@ -54,8 +69,8 @@ class Plan:
 
     def describe(self) -> dict:
         return {"chi": self.chis, "form": "two-stage" if self.split else "one-stage",
-                "variants": [VARIANT_NAMES[v] for v in self.variants],
-                "class_ms": [{VARIANT_NAMES[int(k)]: round(v, 4) for k, v in m.items()} for m in self.class_ms],
+                "variants": [variant_name(v) for v in self.variants],
+                "class_ms": [{variant_name(int(k)): round(v, 4) for k, v in m.items()} for m in self.class_ms],
                 "form_ms": {k: (round(v, 4) if v is not None else None) for k, v in self.form_ms.items()}}
 
 
@@ -207,6 +222,8 @@ def tune(job, reps: int = 3) -> Plan:
                     cands = [_lib.BQA_VARIANT_TILED, _lib.BQA_VARIANT_GENERIC]
                     if split and job.precision == "single" and c.degree == 3 and chis == 16:
                         cands.insert(1, _lib.BQA_VARIANT_TENSOR)
+                    if chis <= 8 and c.degree >= 4:
+                        cands += [generic_warps(16), generic_warps(32)]
                     for v in cands:
                         t = timer.time(one, [v], split, min(ms.values()) if ms else None)
                         if t is not None:
@@ -215,7 +232,7 @@ def tune(job, reps: int = 3) -> Plan:
                     with _LOCK:
                         _CLASS_CACHE[key] = hit
                 picks[i] = hit["best"]
-                class_ms[i].update({(v if not split else v + 10): t for v, t in hit["ms"].items()})
+                class_ms[i].update({(v | _SPLIT if split else v): t for v, t in hit["ms"].items()})
             best[split] = picks
         with _LOCK:
             form = _FORM_CACHE.get(jkey)
@@ -228,7 +245,7 @@ def tune(job, reps: int = 3) -> Plan:
                 _FORM_CACHE[jkey] = form
                 _save()
     split = bool(form["split"])
-    per_class = [{k % 10: v for k, v in m.items() if (k >= 10) == split} for m in class_ms]
+    per_class = [{k & (_SPLIT - 1): v for k, v in m.items() if bool(k & _SPLIT) == split} for m in class_ms]
     plan = Plan(chis=chis, split=split, variants=best[split], class_ms=per_class, form_ms=dict(form["ms"]))
     with _LOCK:
         _PLAN_CACHE[jkey] = plan

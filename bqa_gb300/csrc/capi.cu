@@ -57,7 +57,7 @@ int ensure_smem(const void* kernel, size_t bytes, const char* what) {
 
 extern "C" {
 
-int32_t bqa_abi_version(void) { return 11; }
+int32_t bqa_abi_version(void) { return 12; }
 
 const char* bqa_last_error(void) { return bqa::g_last_error; }
 

@@ -133,14 +133,32 @@ static int job_sweep(bqa_job* j, void* a, void* b, void* s) {
     return bqa_bp_sweep(j->classes, j->n_classes, j->chis, j->dtype, a, b, j->dist_parts, j->loop_state, s);
 }
 
+// The host side of a finished BP run from its final loop state: which buffer holds the kept
+// messages, whether lu holds their open-bond blocks, and the run's figures.
+static void bp_conclude(bqa_job* j, const int32_t* ls, bqa_layer_info* info) {
+    if (ls[2]) j->mcur = 1 - j->mcur;
+    // converged: the kept messages are the last sweep's input, whose blocks that sweep left in lu
+    j->blocks_valid = (!ls[3] && job_two_stage(j)) ? 1 : 0;
+    info->sweeps = ls[1];
+    info->bp_exhausted = ls[3];
+    float best;
+    std::memcpy(&best, &ls[6], 4);
+    info->best_dist = best;
+}
+
+static int bp_reset(bqa_job* j, cudaStream_t st) {
+    int rc = cuda_rc(cudaMemsetAsync(j->loop_state, 0, 8 * sizeof(int32_t), st), "loop state");
+    if (!rc) rc = cuda_rc(cudaMemsetAsync(j->dist_parts, 0, 2 * sizeof(int64_t), st), "dist");
+    return rc;
+}
+
 static int run_bp(bqa_job* j, bqa_layer_info* info, cudaStream_t st) {
     if (j->max_bp_iters < 1) return set_error(BQA_ERR_ARG, "max_bp_iter_number must be >= 1 to run BP");
     void* s = reinterpret_cast<void*>(st);
     void* a = j->msgs[j->mcur];
     void* b = j->msgs[1 - j->mcur];
     int rc;
-    if ((rc = cuda_rc(cudaMemsetAsync(j->loop_state, 0, 8 * sizeof(int32_t), st), "loop state"))) return rc;
-    if ((rc = cuda_rc(cudaMemsetAsync(j->dist_parts, 0, 2 * sizeof(int64_t), st), "dist"))) return rc;
+    if ((rc = bp_reset(j, st))) return rc;
     const int64_t elems = (int64_t)j->edges * j->chis * j->chis;
     const int every = j->bp_check_every > 0 ? j->bp_check_every : 1;
     int launched = 0;
@@ -161,14 +179,7 @@ static int run_bp(bqa_job* j, bqa_layer_info* info, cudaStream_t st) {
         if (launched >= j->max_bp_iters)
             return set_error(BQA_ERR_UNSUPPORTED, "BP loop state did not finish after the iteration cap");
     }
-    if (ls[2]) j->mcur = 1 - j->mcur;
-    // converged: the kept messages are the last sweep's input, whose blocks that sweep left in lu
-    j->blocks_valid = (!ls[3] && job_two_stage(j)) ? 1 : 0;
-    info->sweeps = ls[1];
-    info->bp_exhausted = ls[3];
-    float best;
-    std::memcpy(&best, &ls[6], 4);
-    info->best_dist = best;
+    bp_conclude(j, ls, info);
     return BQA_OK;
 }
 
@@ -375,13 +386,7 @@ static int run_bp_graph(bqa_job* j, bqa_graph_cache* cache, bqa_layer_info* info
     int32_t ls[8];
     std::memcpy(ls, cache->host_ls, sizeof(ls));
     if (!ls[0]) return set_error(BQA_ERR_UNSUPPORTED, "BP graph ended without a decision after %d sweeps", ls[1]);
-    if (ls[2]) j->mcur = 1 - j->mcur;
-    j->blocks_valid = (!ls[3] && job_two_stage(j)) ? 1 : 0;
-    info->sweeps = ls[1];
-    info->bp_exhausted = ls[3];
-    float best;
-    std::memcpy(&best, &ls[6], 4);
-    info->best_dist = best;
+    bp_conclude(j, ls, info);
     return BQA_OK;
 }
 
@@ -439,4 +444,98 @@ extern "C" int32_t bqa_run_layer_graph(bqa_job* job, bqa_graph_cache* cache, dou
     cudaStream_t st = as_stream(stream);
     if ((rc = gate_layer(job, xtime, ztime, info, st))) return rc;
     return run_bp_graph(job, cache, info, st);
+}
+
+// ---- packed BP runs: the sweeps of several jobs in shared launches ---------------------------
+//
+// A job server keeps many jobs resident; after each job's gate layer (bqa_gate_layer, on the
+// job's own stream) the jobs waiting for BP are swept together: every sweep issues each node
+// kernel once for all their classes of that kernel, one combine for all their two-stage
+// sweeps and one decision kernel for all their loop states (pack_execute).  Each job keeps
+// its own loop state, so it stops, damps or swaps buffers exactly as in a run of its own, and
+// its messages are the same bits; the caller takes a job out once its loop state says done
+// (bqa_bp_end) and may add newly waiting jobs between calls (bqa_bp_begin).
+
+namespace bqa {
+
+constexpr int kMaxPackedJobs = 64;
+
+struct LoopStates {
+    const int32_t* ls[kMaxPackedJobs];
+    int n;
+};
+
+__global__ void gather_loop_states_kernel(const __grid_constant__ LoopStates t, int32_t* out) {
+    const int i = threadIdx.x;
+    if (i < 8 * t.n) out[i] = t.ls[i >> 3][i & 7];
+}
+
+// restores the thread's launch mode when a collection ends, also on an early return
+struct CollectGuard {
+    explicit CollectGuard(PackList* l) { pack_collect(l); }
+    ~CollectGuard() { pack_collect(nullptr); }
+};
+
+}  // namespace bqa
+
+extern "C" int32_t bqa_gate_layer(bqa_job* job, double xtime, double ztime, bqa_layer_info* info, void* stream) {
+    if (!info) return set_error(BQA_ERR_ARG, "bqa_gate_layer: bad argument");
+    int rc = check_job(job);
+    if (rc) return rc;
+    std::memset(info, 0, sizeof(*info));
+    return gate_layer(job, xtime, ztime, info, as_stream(stream));
+}
+
+extern "C" int32_t bqa_bp_begin(bqa_job* job, void* stream) {
+    int rc = check_job(job);
+    if (rc) return rc;
+    if (job->max_bp_iters < 1) return set_error(BQA_ERR_ARG, "max_bp_iter_number must be >= 1 to run BP");
+    return bp_reset(job, as_stream(stream));
+}
+
+extern "C" int32_t bqa_bp_packed(bqa_job* const* jobs, int32_t n_jobs, int32_t sweeps, int32_t* loop_states,
+                                 int32_t* host_loop_states, void* stream) {
+    if (!jobs || n_jobs < 1 || n_jobs > kMaxPackedJobs || sweeps < 1 || !loop_states || !host_loop_states)
+        return set_error(BQA_ERR_ARG, "bqa_bp_packed: bad argument (1 <= n_jobs <= %d, sweeps >= 1)", kMaxPackedJobs);
+    for (int i = 0; i < n_jobs; ++i) {
+        int rc = check_job(jobs[i]);
+        if (rc) return rc;
+        if (jobs[i]->dtype != jobs[0]->dtype) return set_error(BQA_ERR_ARG, "bqa_bp_packed: jobs of different dtypes");
+    }
+    cudaStream_t st = as_stream(stream);
+    void* s = stream;
+    PackList list;
+    {
+        CollectGuard guard(&list);
+        for (int i = 0; i < n_jobs; ++i) {
+            bqa_job* j = jobs[i];
+            void* a = j->msgs[j->mcur];
+            void* b = j->msgs[1 - j->mcur];
+            int rc = job_sweep(j, a, b, s);
+            if (!rc)
+                rc = bqa_bp_finalize(a, b, (int64_t)j->edges * j->chis * j->chis, j->dtype, j->dist_parts,
+                                     j->loop_state, j->bp_eps, j->damping, j->max_bp_iters, s);
+            if (rc) return rc;
+        }
+    }
+    int rc;
+    for (int k = 0; k < sweeps; ++k)
+        if ((rc = pack_execute(list, st))) return rc;
+    LoopStates t;
+    t.n = n_jobs;
+    for (int i = 0; i < n_jobs; ++i) t.ls[i] = jobs[i]->loop_state;
+    gather_loop_states_kernel<<<1, 8 * kMaxPackedJobs, 0, st>>>(t, loop_states);
+    if ((rc = check_launch("gather loop states"))) return rc;
+    if ((rc = cuda_rc(cudaMemcpyAsync(host_loop_states, loop_states, 8 * sizeof(int32_t) * n_jobs,
+                                      cudaMemcpyDeviceToHost, st),
+                      "loop states read")))
+        return rc;
+    return cuda_rc(cudaStreamSynchronize(st), "sync");
+}
+
+extern "C" int32_t bqa_bp_end(bqa_job* job, const int32_t* loop_state, bqa_layer_info* info) {
+    if (!job || !loop_state || !info) return set_error(BQA_ERR_ARG, "bqa_bp_end: bad argument");
+    if (!loop_state[0]) return set_error(BQA_ERR_ARG, "bqa_bp_end: the BP run is not done (%d sweeps)", loop_state[1]);
+    bp_conclude(job, loop_state, info);
+    return BQA_OK;
 }

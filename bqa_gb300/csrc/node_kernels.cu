@@ -12,6 +12,8 @@
 // All kernels are templated on the real type R: float (complex64 path) or double
 // (complex128 path, the reference's BQA_PRECISION=double arithmetic).
 #include <cstdlib>
+#include <cstring>
+#include <new>
 
 #include "common.cuh"
 #include "internal.h"
@@ -21,6 +23,7 @@
 #include "tc_bf16_d3c16.cuh"
 
 #include <algorithm>
+#include <vector>
 #include <type_traits>
 
 namespace bqa {
@@ -75,6 +78,67 @@ struct NodeArgs {
 // distance of the previous sweep (loop_state[5], float bits) is above the switch.
 __device__ __forceinline__ bool low_precision_sweep(const int32_t* ls, float switch_dist) {
     return ls != nullptr && ls[1] >= 1 && __int_as_float(ls[5]) > switch_dist;
+}
+
+// ---- packed sweeps (internal.h) ---------------------------------------------------------------
+
+static thread_local PackList* g_pack = nullptr;
+
+void pack_collect(PackList* list) { g_pack = list; }
+
+void PackList::push(const PackEntry& e) {
+    if (n == cap) {
+        const int nc = cap ? 2 * cap : 64;
+        PackEntry* grown = new (std::nothrow) PackEntry[nc];
+        if (!grown) {
+            error = set_error(BQA_ERR_ARG, "packed sweep: out of host memory");
+            return;
+        }
+        for (int i = 0; i < n; ++i) grown[i] = items[i];
+        delete[] items;
+        items = grown;
+        cap = nc;
+    }
+    items[n++] = e;
+}
+
+// While a PackList collects on this thread, record the launch (launcher, phase, key, nodes,
+// arguments) and return true: the caller then returns without launching.
+template <typename A>
+static bool pack_record(int (*fn)(const PackEntry*, int, cudaStream_t), int phase, int key, int count, const A& args) {
+    static_assert(sizeof(A) <= sizeof(PackEntry::args) && std::is_trivially_copyable<A>::value,
+                  "packed launch arguments must be a small trivially copyable block");
+    if (!g_pack) return false;
+    PackEntry e;
+    e.launch = fn;
+    e.phase = phase;
+    e.key = key;
+    e.count = count;
+    std::memcpy(e.args, &args, sizeof(A));
+    g_pack->push(e);
+    return true;
+}
+
+int pack_execute(const PackList& l, cudaStream_t st) {
+    if (l.error) return l.error;
+    std::vector<char> issued(l.n, 0);
+    std::vector<PackEntry> group;
+    for (int phase = 0; phase < 4; ++phase)
+        for (int i = 0; i < l.n; ++i) {
+            const PackEntry& head = l.items[i];
+            if (issued[i] || head.phase != phase) continue;
+            group.clear();
+            for (int k = i; k < l.n; ++k) {
+                const PackEntry& x = l.items[k];
+                if (!issued[k] && x.phase == phase && x.launch == head.launch && x.key == head.key) {
+                    group.push_back(x);
+                    issued[k] = 1;
+                }
+            }
+            const int rc = head.launch(group.data(), (int)group.size(), st);
+            if (rc) return rc;
+        }
+    return BQA_OK;
 }
 
 // Y[s][l][i][r] = sum_j M_s[i][j] X[s][l][j][r]; X is [2][L][nin][R], Y is [2][L][nout][R],
@@ -177,7 +241,7 @@ __device__ __forceinline__ void write_outputs(const NodeArgs<R>& a, int node, in
 }
 
 template <int CM, int MODE, typename R>
-__global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
+__device__ __forceinline__ void node_body(const NodeArgs<R>& a, int node) {
     using C = typename Cx<R>::T;
     extern __shared__ double4 smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
@@ -198,7 +262,6 @@ __global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
         if (a.loop_state[2]) { msgs_in = a.msgs_b; msgs_out = const_cast<C*>(a.msgs_a); }
     }
 
-    const int node = blockIdx.x;
     const C* Tg = a.tensors + (size_t)node * NT;
     for (int i = threadIdx.x; i < NT; i += blockDim.x) sT[i] = Tg[i];
     for (int k = 0; k < d; ++k) {
@@ -260,6 +323,46 @@ __global__ void __launch_bounds__(256) node_kernel(NodeArgs<R> a) {
             atomic_max_nonneg(a.dist_parts + 1, den2);
         }
     }
+}
+
+// The generic kernel takes one or several classes (of one job or of several) per launch: CTA b
+// belongs to class c with first[c] <= b < first[c + 1] (first counts CTAs).  Shared memory and
+// threads are the largest any of the launch's classes needs; each CTA lays out its class's
+// buffers in it.  The register-tiled half-node kernels have the same form for packed sweeps.
+constexpr int kMaxMergedClasses = 32;   // 32 x 104-byte argument blocks: under 4 KB of parameters
+template <typename R>
+struct MergedClasses {
+    NodeArgs<R> cls[kMaxMergedClasses];
+    int first[kMaxMergedClasses + 1];
+    int n;
+};
+
+// the class of this CTA: the last c with first[c] <= blockIdx.x (classes are never empty)
+__device__ __forceinline__ int merged_class(const int* first, int n) {
+    int lo = 0, hi = n - 1;
+    const int b = (int)blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int CM, int MODE, typename R>
+__global__ void __launch_bounds__(256) node_kernel_merged(const __grid_constant__ MergedClasses<R> m) {
+    const int c = merged_class(m.first, m.n);
+    node_body<CM, MODE, R>(m.cls[c], (int)blockIdx.x - m.first[c]);
+}
+
+// The same kernel built for CTAs of up to 1024 threads (BP and open-bond modes, bond dims
+// <= 8): for nodes whose shared memory allows one or two CTAs per SM, more warps per node
+// hide more latency.  A node's outputs do not depend on the CTA size (every output is formed
+// by one thread in a fixed order; the BP maxima are order-free).
+template <int CM, int MODE, typename R>
+__global__ void __launch_bounds__(1024) node_kernel_merged_wide(const __grid_constant__ MergedClasses<R> m) {
+    const int c = merged_class(m.first, m.n);
+    node_body<CM, MODE, R>(m.cls[c], (int)blockIdx.x - m.first[c]);
 }
 
 
@@ -485,9 +588,22 @@ __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int cou
     }
 }
 
+template <typename R>
+struct GlobalArgs {
+    NodeArgs<R> a;
+    void* scratch;
+    int64_t scratch_elems;
+};
+
+template <int MODE, typename R>
+static int launch_global_solo(const PackEntry* e, int n, cudaStream_t st);
+
 template <int MODE, typename R>
 static int launch_node_global(const NodeArgs<R>& args, int count, void* scratch, int64_t scratch_elems,
                               cudaStream_t st) {
+    // packed sweeps issue these one class at a time (a job's classes share its scratch)
+    if (pack_record(launch_global_solo<MODE, R>, 0, 0, count, GlobalArgs<R>{args, scratch, scratch_elems}))
+        return BQA_OK;
     using C = typename Cx<R>::T;
     const int chi = args.chi, d = args.d;
     const int64_t need = 4 * (int64_t)ipow(chi, d);   // two work tensors
@@ -509,6 +625,29 @@ static int launch_node_global(const NodeArgs<R>& args, int count, void* scratch,
     if (rc) return rc;
     kern<<<(int)ctas, threads, smem, st>>>(args, count, static_cast<C*>(scratch));
     return check_launch("node kernel (global)");
+}
+
+template <int MODE, typename R>
+static int launch_global_solo(const PackEntry* e, int n, cudaStream_t st) {
+    for (int i = 0; i < n; ++i) {
+        GlobalArgs<R> g;
+        std::memcpy(&g, e[i].args, sizeof(g));
+        const int rc = launch_node_global<MODE, R>(g.a, e[i].count, g.scratch, g.scratch_elems, st);
+        if (rc) return rc;
+    }
+    return BQA_OK;
+}
+
+// packed sweeps: launches without a merged form, issued one entry at a time through `launch`
+template <int (*LAUNCH)(const NodeArgs<float>&, int, cudaStream_t)>
+static int launch_solo_f32(const PackEntry* e, int n, cudaStream_t st) {
+    for (int i = 0; i < n; ++i) {
+        NodeArgs<float> a;
+        std::memcpy(&a, e[i].args, sizeof(a));
+        const int rc = LAUNCH(a, e[i].count, st);
+        if (rc) return rc;
+    }
+    return BQA_OK;
 }
 
 // Register-tiled complex64 kernel for compile-time (D, CHI): BP messages, extended messages,
@@ -620,6 +759,7 @@ __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kern
 
 template <int D, int CHI, int MODE>
 static int launch_tiled(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    if (pack_record(launch_solo_f32<launch_tiled<D, CHI, MODE>>, 0, 0, count, args)) return BQA_OK;
     using S = tiled::Shape<D, CHI>;
     const size_t smem = (size_t)S::SMEM_ELEMS * sizeof(float2);
     int rc = ensure_smem((const void*)tiled_node_kernel<D, CHI, MODE>, smem, "tiled node kernel");
@@ -647,7 +787,7 @@ static int try_tiled(const NodeArgs<float>& a, int count, cudaStream_t st, int* 
 // P_0 + P_1 into messages.  Same contraction schedules as tiled_node_kernel.
 // SPEC: the (3, 16) shape with the address arithmetic of tiled_d3c16.cuh (same operations).
 template <int D, int CHI, bool SPEC>
-__global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_kernel(NodeArgs<float> a) {
+__device__ __forceinline__ void tiled_half_body(const NodeArgs<float>& a, int node, int s) {
     using S = tiled::HalfShape<D, CHI>;
     static_assert(CHI % 4 == 0 && D >= 2 && D <= 4, "half kernel shapes");
     static_assert(!SPEC || (D == 3 && CHI == 16 && S::THREADS == tiled::d3c16::TH && S::KS == 16),
@@ -666,7 +806,6 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
         if (a.loop_state[2]) msgs_in = a.msgs_b;
     }
     if (a.mixed_role == 2 && low_precision_sweep(a.loop_state, a.mixed_switch)) return;
-    const int node = blockIdx.x >> 1, s = blockIdx.x & 1;
     {
         const float4* tg = reinterpret_cast<const float4*>(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS);
         if constexpr (SPEC) {
@@ -767,13 +906,51 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_
 }
 
 template <int D, int CHI, bool SPEC>
+__global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_half_kernel(NodeArgs<float> a) {
+    tiled_half_body<D, CHI, SPEC>(a, blockIdx.x >> 1, blockIdx.x & 1);
+}
+
+// the half-node kernel over several classes (first counts CTAs: two per node)
+template <int D, int CHI, bool SPEC>
+__global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS)
+    tiled_half_kernel_merged(const __grid_constant__ MergedClasses<float> m) {
+    const int c = merged_class(m.first, m.n);
+    const int local = (int)blockIdx.x - m.first[c];
+    tiled_half_body<D, CHI, SPEC>(m.cls[c], local >> 1, local & 1);
+}
+
+template <int D, int CHI, bool SPEC>
+static int launch_half_packed(const PackEntry* e, int n, cudaStream_t st);
+
+template <int D, int CHI, bool SPEC>
 static int launch_half_k(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    if (pack_record(launch_half_packed<D, CHI, SPEC>, 0, 0, count, args)) return BQA_OK;
     using S = tiled::HalfShape<D, CHI>;
     const size_t smem = (size_t)S::SMEM_ELEMS * sizeof(float2);
     int rc = ensure_smem((const void*)tiled_half_kernel<D, CHI, SPEC>, smem, "tiled half kernel");
     if (rc) return rc;
     tiled_half_kernel<D, CHI, SPEC><<<2 * count, S::THREADS, smem, st>>>(args);
     return check_launch("tiled half kernel");
+}
+
+template <int D, int CHI, bool SPEC>
+static int launch_half_packed(const PackEntry* e, int n, cudaStream_t st) {
+    using S = tiled::HalfShape<D, CHI>;
+    const size_t smem = (size_t)S::SMEM_ELEMS * sizeof(float2);
+    int rc = ensure_smem((const void*)tiled_half_kernel_merged<D, CHI, SPEC>, smem, "tiled half kernel (merged)");
+    if (rc) return rc;
+    for (int i0 = 0; i0 < n; i0 += kMaxMergedClasses) {
+        MergedClasses<float> m;
+        m.n = std::min(kMaxMergedClasses, n - i0);
+        m.first[0] = 0;
+        for (int c = 0; c < m.n; ++c) {
+            std::memcpy(&m.cls[c], e[i0 + c].args, sizeof(NodeArgs<float>));
+            m.first[c + 1] = m.first[c] + 2 * e[i0 + c].count;
+        }
+        tiled_half_kernel_merged<D, CHI, SPEC><<<m.first[m.n], S::THREADS, smem, st>>>(m);
+        if ((rc = check_launch("tiled half kernel (merged)"))) return rc;
+    }
+    return BQA_OK;
 }
 
 // Half-node kernel of degree 3, bond dim 16 with the bond products on the tensor cores
@@ -1071,6 +1248,7 @@ static int sm_count() {
 
 template <bool MIXED>
 static int launch_tcb_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    if (pack_record(launch_solo_f32<launch_tcb_half<MIXED>>, 0, 0, count, args)) return BQA_OK;
     const size_t smem = (size_t)tcb::REGION + 16;
     int rc = ensure_smem((const void*)tcb_half_kernel_d3c16<MIXED>, smem, "bf16 tensor-core half kernel");
     if (rc) return rc;
@@ -1081,6 +1259,7 @@ static int launch_tcb_half(const NodeArgs<float>& args, int count, cudaStream_t 
 }
 
 static int launch_tc_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    if (pack_record(launch_solo_f32<launch_tc_half>, 0, 0, count, args)) return BQA_OK;
     const size_t smem = (size_t)tcd3::REGION + (3 + 2) * 256 * sizeof(float2) + 16;
     int rc = ensure_smem((const void*)tc_half_kernel_d3c16, smem, "tensor-core half kernel");
     if (rc) return rc;
@@ -1146,19 +1325,31 @@ __global__ void __launch_bounds__(256) ext_combine_kernel(const typename Cx<R>::
 // BP messages from the open-bond blocks: msg[e] = (P_0 + P_1)/tr, with the convergence maxima
 // max|new-old|^2 and max|new+old|^2 folded per block into dist_parts.  One warp per slot.
 template <typename R>
-__global__ void __launch_bounds__(256) bp_combine_kernel(const typename Cx<R>::T* __restrict__ pm, int E, int chi,
-                                                         const typename Cx<R>::T* msgs_a, typename Cx<R>::T* msgs_b,
-                                                         const int32_t* loop_state, typename Cx<R>::Bits* dist_parts) {
+struct CombineArgs {
+    const typename Cx<R>::T* pm;
+    int E, chi;
+    const typename Cx<R>::T* msgs_a;
+    typename Cx<R>::T* msgs_b;
+    const int32_t* loop_state;
+    typename Cx<R>::Bits* dist_parts;
+};
+
+// block `blk` of the combine of one job
+template <typename R>
+__device__ __forceinline__ void bp_combine_body(const CombineArgs<R>& x, int blk) {
     using C = typename Cx<R>::T;
     __shared__ R sRed[32];
-    const C* msgs_in = msgs_a;
-    C* msgs_out = msgs_b;
-    if (loop_state != nullptr) {
-        if (loop_state[0]) return;
-        if (loop_state[2]) { msgs_in = msgs_b; msgs_out = const_cast<C*>(msgs_a); }
+    const C* __restrict__ pm = x.pm;
+    const int E = x.E, chi = x.chi;
+    const C* msgs_in = x.msgs_a;
+    C* msgs_out = x.msgs_b;
+    if (x.loop_state != nullptr) {
+        if (x.loop_state[0]) return;
+        if (x.loop_state[2]) { msgs_in = x.msgs_b; msgs_out = const_cast<C*>(x.msgs_a); }
     }
+    typename Cx<R>::Bits* dist_parts = x.dist_parts;
     const int lane = threadIdx.x & 31;
-    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int slot = (blk * blockDim.x + threadIdx.x) >> 5;
     const int n2 = chi * chi;
     R num2 = 0, den2 = 0;
     if (slot < E) {
@@ -1186,26 +1377,129 @@ __global__ void __launch_bounds__(256) bp_combine_kernel(const typename Cx<R>::T
     }
 }
 
-// The generic shared-memory node kernel (any degree and bond dim <= 32 whose node fits).
-template <int MODE, typename R>
-static int launch_node_generic(const NodeArgs<R>& args, int count, cudaStream_t st) {
-    const int chi = args.chi, d = args.d;
-    const size_t smem = node_smem_elems(d, chi) * sizeof(typename Cx<R>::T);
+template <typename R>
+__global__ void __launch_bounds__(256) bp_combine_kernel(const CombineArgs<R> x) {
+    bp_combine_body<R>(x, blockIdx.x);
+}
+
+// the combines of several jobs in one launch (first counts blocks)
+template <typename R>
+struct MergedCombine {
+    CombineArgs<R> job[kMaxMergedClasses];
+    int first[kMaxMergedClasses + 1];
+    int n;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256) bp_combine_kernel_merged(const __grid_constant__ MergedCombine<R> m) {
+    const int c = merged_class(m.first, m.n);
+    bp_combine_body<R>(m.job[c], (int)blockIdx.x - m.first[c]);
+}
+
+template <typename R>
+static int launch_combine_packed(const PackEntry* e, int n, cudaStream_t st) {
+    for (int i0 = 0; i0 < n; i0 += kMaxMergedClasses) {
+        MergedCombine<R> m;
+        m.n = std::min(kMaxMergedClasses, n - i0);
+        m.first[0] = 0;
+        for (int c = 0; c < m.n; ++c) {
+            std::memcpy(&m.job[c], e[i0 + c].args, sizeof(CombineArgs<R>));
+            m.first[c + 1] = m.first[c] + e[i0 + c].count;
+        }
+        bp_combine_kernel_merged<R><<<m.first[m.n], 256, 0, st>>>(m);
+        const int rc = check_launch("bp_combine (merged)");
+        if (rc) return rc;
+    }
+    return BQA_OK;
+}
+
+// threads of a generic-kernel CTA for degree d at bond dim chi
+static int generic_threads(int d, int chi) {
     const int fib = 2 * ipow(chi, d > 0 ? d - 1 : 0);
     int threads = ((max(fib, 2 * chi * chi) + 31) / 32) * 32;
-    threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
-    void (*kern)(NodeArgs<R>) = nullptr;
-    if (chi <= 1) kern = node_kernel<1, MODE, R>;
-    else if (chi <= 2) kern = node_kernel<2, MODE, R>;
-    else if (chi <= 4) kern = node_kernel<4, MODE, R>;
-    else if (chi <= 8) kern = node_kernel<8, MODE, R>;
-    else if (chi <= 16) kern = node_kernel<16, MODE, R>;
-    else if (chi <= 32) kern = node_kernel<32, MODE, R>;
-    else return set_error(BQA_ERR_UNSUPPORTED, "node kernel: bond dim %d > 32", chi);
+    return threads < 32 ? 32 : (threads > 256 ? 256 : threads);
+}
+
+// The generic kernel's build for bond dim chi and CTAs of `threads` threads (0: none).
+template <typename A, int MODE, typename R, template <int, int, typename> class Pick>
+static void (*generic_build(int chi, int threads))(A) {
+    if (threads > 256) {
+        if constexpr (MODE == MODE_BP || MODE == MODE_PSPLIT) {
+            if (chi <= 1) return Pick<1, MODE, R>::wide;
+            if (chi <= 2) return Pick<2, MODE, R>::wide;
+            if (chi <= 4) return Pick<4, MODE, R>::wide;
+            if (chi <= 8) return Pick<8, MODE, R>::wide;
+        }
+        return nullptr;
+    }
+    if (chi <= 1) return Pick<1, MODE, R>::narrow;
+    if (chi <= 2) return Pick<2, MODE, R>::narrow;
+    if (chi <= 4) return Pick<4, MODE, R>::narrow;
+    if (chi <= 8) return Pick<8, MODE, R>::narrow;
+    if (chi <= 16) return Pick<16, MODE, R>::narrow;
+    if (chi <= 32) return Pick<32, MODE, R>::narrow;
+    return nullptr;
+}
+
+template <int CM, int MODE, typename R>
+struct MergedBuilds {
+    static constexpr void (*narrow)(MergedClasses<R>) = node_kernel_merged<CM, MODE, R>;
+    static constexpr void (*wide)(MergedClasses<R>) = node_kernel_merged_wide<CM, MODE, R>;
+};
+
+static int no_generic_build(int chi, int threads) {
+    if (chi > 32) return set_error(BQA_ERR_UNSUPPORTED, "node kernel: bond dim %d > 32", chi);
+    return set_error(BQA_ERR_UNSUPPORTED, "node kernel: no %d-thread build at bond dim %d (above 256 threads: bond "
+                     "dims <= 8, BP and open-bond passes)", threads, chi);
+}
+
+static bool valid_cta(int threads) { return threads >= 32 && threads <= 1024 && threads % 32 == 0; }
+
+// One launch of the generic shared-memory node kernel (any degree and bond dim <= 32 whose
+// node fits) over classes args[0..n) (counts[c] nodes each, same bond dim); threads = 0 takes
+// the largest generic_threads of the classes.
+template <int MODE, typename R>
+static int launch_node_generic_merged(const NodeArgs<R>* args, const int* counts, int n, cudaStream_t st,
+                                      int threads = 0) {
+    const int chi = args[0].chi;
+    MergedClasses<R> m;
+    m.n = n;
+    m.first[0] = 0;
+    size_t smem = 0;
+    int own = 32;
+    for (int c = 0; c < n; ++c) {
+        m.cls[c] = args[c];
+        m.first[c + 1] = m.first[c] + counts[c];
+        smem = std::max(smem, node_smem_elems(args[c].d, chi) * sizeof(typename Cx<R>::T));
+        own = std::max(own, generic_threads(args[c].d, chi));
+    }
+    if (threads == 0) threads = own;
+    if (!valid_cta(threads)) return set_error(BQA_ERR_ARG, "node kernel: %d threads per CTA", threads);
+    void (*kern)(MergedClasses<R>) = generic_build<MergedClasses<R>, MODE, R, MergedBuilds>(chi, threads);
+    if (!kern) return no_generic_build(chi, threads);
     int rc = ensure_smem((const void*)kern, smem, "node kernel");
     if (rc) return rc;
-    kern<<<count, threads, smem, st>>>(args);
+    kern<<<m.first[n], threads, smem, st>>>(m);
     return check_launch("node kernel");
+}
+
+// the generic kernel over one class
+template <int MODE, typename R>
+static int launch_node_generic(const NodeArgs<R>& args, int count, cudaStream_t st, int threads = 0) {
+    return launch_node_generic_merged<MODE, R>(&args, &count, 1, st, threads);
+}
+
+// the generic kernel's classes of a sweep go out in one launch unless BQA_GB300_MERGE_CLASSES=0
+// was set when the library loaded (then one launch per class; the outputs are the same bits)
+static const bool g_merge_classes = [] {
+    const char* v = getenv("BQA_GB300_MERGE_CLASSES");
+    return !(v && v[0] == '0');
+}();
+
+// a register-tiled complex64 kernel exists for (d, chi) (the pairs of try_tiled)
+static bool tiled_covers(int d, int chi) {
+    return (d == 2 && (chi == 8 || chi == 12 || chi == 16)) ||
+           (d == 3 && (chi == 4 || chi == 8 || chi == 12 || chi == 16)) || (d == 4 && (chi == 4 || chi == 8));
 }
 
 template <int MODE, typename R>
@@ -1219,11 +1513,89 @@ static int launch_node_mode(const NodeArgs<R>& args, int count, cudaStream_t st)
     return launch_node_generic<MODE, R>(args, count, st);
 }
 
+template <int MODE, typename R>
+static int launch_merged_mode(const NodeArgs<R>* args, const int* counts, int n, cudaStream_t st, int threads) {
+    return launch_node_generic_merged<MODE, R>(args, counts, n, st, threads);
+}
+
+// packed sweeps: generic-kernel classes of one (degree, bond dim, CTA size), any jobs
+template <int MODE, typename R>
+static int launch_generic_packed(const PackEntry* e, int n, cudaStream_t st) {
+    NodeArgs<R> a[kMaxMergedClasses];
+    int cnt[kMaxMergedClasses];
+    const int threads = 32 * (e[0].key >> 16);
+    for (int i0 = 0; i0 < n; i0 += kMaxMergedClasses) {
+        const int m = std::min(kMaxMergedClasses, n - i0);
+        for (int c = 0; c < m; ++c) {
+            std::memcpy(&a[c], e[i0 + c].args, sizeof(NodeArgs<R>));
+            cnt[c] = e[i0 + c].count;
+        }
+        const int rc = launch_node_generic_merged<MODE, R>(a, cnt, m, st, threads);
+        if (rc) return rc;
+    }
+    return BQA_OK;
+}
+
+// grouping key of a packed generic class: CTA size (warps; 0 = own), degree, bond dim
+template <typename R>
+static int key_of(const NodeArgs<R>& a, int threads) { return ((threads / 32) << 16) | (a.d << 8) | a.chi; }
+
+// Every class of a sweep (or pass) with the kernel it needs: the global-memory form for node
+// tensors beyond shared memory, the register-tiled kernel where one exists (allow_tiled), and
+// the generic kernel for the rest -- those in one launch (launch_node_generic_merged).
 template <typename R>
 static int run_classes(int mode, const bqa_class* classes, int n_classes, int chi, const void* msgs_a, void* msgs_b,
-                       void* out, void* dist_parts, const int32_t* loop_state, double ztime, cudaStream_t st) {
+                       void* out, void* dist_parts, const int32_t* loop_state, double ztime, cudaStream_t st,
+                       bool allow_tiled = true, const int* cta_threads = nullptr) {
     using C = typename Cx<R>::T;
     if (!classes || n_classes < 0 || chi < 1) return set_error(BQA_ERR_ARG, "bad class list or bond dim");
+    NodeArgs<R> gen[kMaxMergedClasses];
+    int gen_count[kMaxMergedClasses];
+    int n_gen = 0;
+    int gen_threads = 0;   // CTA size chosen for the pending classes (0: their own)
+    auto flush = [&]() -> int {
+        int rc = BQA_OK;
+        if (n_gen == 0) return rc;
+        switch (mode) {
+            case MODE_BP: rc = launch_merged_mode<MODE_BP, R>(gen, gen_count, n_gen, st, gen_threads); break;
+            case MODE_EXT: rc = launch_merged_mode<MODE_EXT, R>(gen, gen_count, n_gen, st, gen_threads); break;
+            case MODE_PSPLIT: rc = launch_merged_mode<MODE_PSPLIT, R>(gen, gen_count, n_gen, st, gen_threads); break;
+            default: rc = launch_merged_mode<MODE_DENS, R>(gen, gen_count, n_gen, st, gen_threads); break;
+        }
+        n_gen = 0;
+        return rc;
+    };
+    // A class joins the pending launch when that costs no class an extra wave: with the
+    // launch's shared memory and threads (the largest of its classes) every class still has
+    // its solo occupancy, or its nodes fit in one wave of the merged kernel anyway.  Density
+    // passes merge only classes of equal thread counts (their block sums then add in the same
+    // order as in a launch of their own).
+    const int sms = sm_count();
+    auto occupancy = [](size_t smem, int threads) {
+        const int by_smem = (int)((228u * 1024u) / (smem + 1024u));
+        return std::max(1, std::min(std::min(by_smem, 2048 / threads), 32));
+    };
+    auto joins = [&](const NodeArgs<R>& a, int count, int want) {
+        if (n_gen == 0) return true;
+        if (n_gen == kMaxMergedClasses || want != gen_threads) return false;
+        auto own = [&](int d) { return want ? want : generic_threads(d, chi); };
+        const size_t es = sizeof(C);
+        size_t smem = node_smem_elems(a.d, chi) * es;
+        int threads = own(a.d);
+        for (int c = 0; c < n_gen; ++c) {
+            if (mode == MODE_DENS && own(gen[c].d) != own(a.d)) return false;
+            smem = std::max(smem, node_smem_elems(gen[c].d, chi) * es);
+            threads = std::max(threads, own(gen[c].d));
+        }
+        const int merged = occupancy(smem, threads);
+        auto fine = [&](int d, int cnt) {
+            return merged >= occupancy(node_smem_elems(d, chi) * es, own(d)) || (int64_t)cnt <= (int64_t)merged * sms;
+        };
+        if (!fine(a.d, count)) return false;
+        for (int c = 0; c < n_gen; ++c)
+            if (!fine(gen[c].d, gen_count[c])) return false;
+        return true;
+    };
     for (int c = 0; c < n_classes; ++c) {
         const bqa_class& k = classes[c];
         if (k.count <= 0) continue;
@@ -1244,6 +1616,9 @@ static int run_classes(int mode, const bqa_class* classes, int n_classes, int ch
         a.dist_parts = static_cast<typename Cx<R>::Bits*>(dist_parts);
         a.ztime = ztime;
         int rc = BQA_OK;
+        const int want = cta_threads ? cta_threads[c] : 0;   // generic kernel's CTA size (0: its own)
+        const bool tiled = allow_tiled && sizeof(R) == 4 && g_use_tiled && mode != MODE_PSPLIT &&
+                           tiled_covers(k.degree, chi);
         if (global) {
             switch (mode) {
                 case MODE_BP: rc = launch_node_global<MODE_BP>(a, k.count, k.scratch, k.scratch_elems, st); break;
@@ -1253,33 +1628,50 @@ static int run_classes(int mode, const bqa_class* classes, int n_classes, int ch
                     break;
                 default: rc = launch_node_global<MODE_DENS>(a, k.count, k.scratch, k.scratch_elems, st); break;
             }
-        } else {
+        } else if (tiled) {
             switch (mode) {
                 case MODE_BP: rc = launch_node_mode<MODE_BP>(a, k.count, st); break;
                 case MODE_EXT: rc = launch_node_mode<MODE_EXT>(a, k.count, st); break;
-                case MODE_PSPLIT: rc = launch_node_mode<MODE_PSPLIT>(a, k.count, st); break;
                 default: rc = launch_node_mode<MODE_DENS>(a, k.count, st); break;
             }
+        } else if (g_pack) {   // packed sweep: merged with the same (degree, bond dim, CTA size) of other jobs
+            const int key = key_of(a, want);
+            switch (mode) {
+                case MODE_BP: pack_record(launch_generic_packed<MODE_BP, R>, 0, key, k.count, a); break;
+                case MODE_EXT: pack_record(launch_generic_packed<MODE_EXT, R>, 0, key, k.count, a); break;
+                case MODE_PSPLIT: pack_record(launch_generic_packed<MODE_PSPLIT, R>, 0, key, k.count, a); break;
+                default: pack_record(launch_generic_packed<MODE_DENS, R>, 0, key, k.count, a); break;
+            }
+        } else {
+            if (!g_merge_classes || !joins(a, k.count, want)) rc = flush();
+            if (rc) return rc;
+            gen[n_gen] = a;
+            gen_count[n_gen] = k.count;
+            gen_threads = want;
+            ++n_gen;
         }
         if (rc) return rc;
     }
-    return BQA_OK;
+    return flush();
 }
 
 static int run_classes_dt(int dtype, int mode, const bqa_class* classes, int n_classes, int chi, const void* msgs_a,
                           void* msgs_b, void* out, void* dist_parts, const int32_t* loop_state, double ztime,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool allow_tiled = true, const int* cta_threads = nullptr) {
     if (dtype == BQA_C64)
-        return run_classes<float>(mode, classes, n_classes, chi, msgs_a, msgs_b, out, dist_parts, loop_state, ztime, st);
+        return run_classes<float>(mode, classes, n_classes, chi, msgs_a, msgs_b, out, dist_parts, loop_state, ztime, st,
+                                  allow_tiled, cta_threads);
     if (dtype == BQA_C128)
-        return run_classes<double>(mode, classes, n_classes, chi, msgs_a, msgs_b, out, dist_parts, loop_state, ztime, st);
+        return run_classes<double>(mode, classes, n_classes, chi, msgs_a, msgs_b, out, dist_parts, loop_state, ztime, st,
+                                   allow_tiled, cta_threads);
     return set_error(BQA_ERR_ARG, "unknown dtype %d", dtype);
 }
 
 // ---- BP loop control -------------------------------------------------------------------------
 
 template <typename R>
-__global__ void bp_decide_kernel(typename Cx<R>::Bits* parts, int32_t* ls, double eps, double damping, int max_iters) {
+__device__ __forceinline__ void bp_decide(typename Cx<R>::Bits* parts, int32_t* ls, double eps, double damping,
+                                          int max_iters) {
     ls[4] = 0;
     if (ls[0]) return;
     const R num = sqrt(bits_to_real(parts[0]));
@@ -1296,6 +1688,45 @@ __global__ void bp_decide_kernel(typename Cx<R>::Bits* parts, int32_t* ls, doubl
     if (sweeps >= max_iters) { ls[0] = 1; ls[3] = 1; ls[2] ^= 1; return; }  // raw last output
     if (damping == 0.0) ls[2] ^= 1;
     else ls[4] = 1;
+}
+
+template <typename R>
+__global__ void bp_decide_kernel(typename Cx<R>::Bits* parts, int32_t* ls, double eps, double damping, int max_iters) {
+    bp_decide<R>(parts, ls, eps, damping, max_iters);
+}
+
+template <typename R>
+struct DecideArgs {
+    typename Cx<R>::Bits* parts;
+    int32_t* ls;
+    double eps, damping;
+    int max_iters;
+};
+
+template <typename R>
+struct MergedDecide {
+    DecideArgs<R> job[kMaxMergedClasses];
+    int n;
+};
+
+// the decisions of several jobs' BP runs: thread t decides job t
+template <typename R>
+__global__ void bp_decide_kernel_merged(const __grid_constant__ MergedDecide<R> m) {
+    const int t = threadIdx.x;
+    if (t < m.n) bp_decide<R>(m.job[t].parts, m.job[t].ls, m.job[t].eps, m.job[t].damping, m.job[t].max_iters);
+}
+
+template <typename R>
+static int launch_decide_packed(const PackEntry* e, int n, cudaStream_t st) {
+    for (int i0 = 0; i0 < n; i0 += kMaxMergedClasses) {
+        MergedDecide<R> m;
+        m.n = std::min(kMaxMergedClasses, n - i0);
+        for (int c = 0; c < m.n; ++c) std::memcpy(&m.job[c], e[i0 + c].args, sizeof(DecideArgs<R>));
+        bp_decide_kernel_merged<R><<<1, 32, 0, st>>>(m);
+        const int rc = check_launch("bp_decide (merged)");
+        if (rc) return rc;
+    }
+    return BQA_OK;
 }
 
 template <typename R>
@@ -1363,16 +1794,46 @@ __global__ void lmbds_truncate_kernel(R* lam, int stride, int rows, int dim) {
 }
 
 template <typename R>
-static int finalize(void* a, void* b, int64_t n, void* parts, int32_t* ls, double eps, double damping, int max_iters,
-                    cudaStream_t st) {
+static int launch_damp(void* a, void* b, int64_t n, const int32_t* ls, double damping, cudaStream_t st) {
     using C = typename Cx<R>::T;
-    bp_decide_kernel<R><<<1, 1, 0, st>>>(static_cast<typename Cx<R>::Bits*>(parts), ls, eps, damping, max_iters);
-    int rc = check_launch("bp_decide");
-    if (rc || damping == 0.0 || n == 0) return rc;
     int blocks = (int)((n + 255) / 256);
     blocks = blocks > 4 * 152 * 8 ? 4 * 152 * 8 : blocks;
     bp_damp_kernel<R><<<blocks, 256, 0, st>>>(static_cast<C*>(a), static_cast<C*>(b), n, ls, (R)damping);
     return check_launch("bp_damp");
+}
+
+struct DampArgs {
+    void* a;
+    void* b;
+    int64_t n;
+    const int32_t* ls;
+    double damping;
+};
+
+template <typename R>
+static int launch_damp_solo(const PackEntry* e, int n, cudaStream_t st) {
+    for (int i = 0; i < n; ++i) {
+        DampArgs x;
+        std::memcpy(&x, e[i].args, sizeof(x));
+        const int rc = launch_damp<R>(x.a, x.b, x.n, x.ls, x.damping, st);
+        if (rc) return rc;
+    }
+    return BQA_OK;
+}
+
+template <typename R>
+static int finalize(void* a, void* b, int64_t n, void* parts, int32_t* ls, double eps, double damping, int max_iters,
+                    cudaStream_t st) {
+    using Bits = typename Cx<R>::Bits;
+    if (pack_record(launch_decide_packed<R>, 2, 0, 0, DecideArgs<R>{static_cast<Bits*>(parts), ls, eps, damping,
+                                                                     max_iters})) {
+        if (damping != 0.0 && n != 0) pack_record(launch_damp_solo<R>, 3, 0, 0, DampArgs{a, b, n, ls, damping});
+        return BQA_OK;
+    }
+    bp_decide_kernel<R><<<1, 1, 0, st>>>(static_cast<Bits*>(parts), ls, eps, damping, max_iters);
+    int rc = check_launch("bp_decide");
+    if (rc || damping == 0.0 || n == 0) return rc;
+    return launch_damp<R>(a, b, n, ls, damping, st);
 }
 
 template <typename R>
@@ -1396,34 +1857,23 @@ static NodeArgs<R> class_args(const bqa_class& k, int chi, const void* msgs_a, v
     return a;
 }
 
-// BP sweep of one class with the generic shared-memory kernel (MODE_BP: messages and
-// convergence maxima; MODE_PSPLIT: open-bond blocks into pm).  Classes whose nodes exceed
-// shared memory have only the global-memory form, which run_classes picks.
-template <int MODE, typename R>
-static int sweep_class_generic(const bqa_class& k, int chi, const void* msgs_a, void* msgs_b, void* out,
-                               void* dist_parts, const int32_t* loop_state, cudaStream_t st) {
+template <typename R>
+static int launch_bp_combine_t(const void* pm, int edges, int chi, void* msgs_a, void* msgs_b,
+                               const int32_t* loop_state, void* dist_parts, cudaStream_t st) {
     using C = typename Cx<R>::T;
-    if (node_smem_elems(k.degree, chi) * sizeof(C) > kMaxSmem) {
-        bqa_class one = k;
-        return run_classes<R>(MODE, &one, 1, chi, msgs_a, msgs_b, out, dist_parts, loop_state, 0.0, st);
-    }
-    return launch_node_generic<MODE, R>(class_args<R>(k, chi, msgs_a, msgs_b, out, dist_parts, loop_state), k.count,
-                                        st);
+    const CombineArgs<R> x{static_cast<const C*>(pm), edges, chi, static_cast<const C*>(msgs_a), static_cast<C*>(msgs_b),
+                           loop_state, static_cast<typename Cx<R>::Bits*>(dist_parts)};
+    const int blocks = (int)(((int64_t)edges * 32 + 255) / 256);
+    if (pack_record(launch_combine_packed<R>, 1, 0, blocks, x)) return BQA_OK;
+    bp_combine_kernel<R><<<blocks, 256, 0, st>>>(x);
+    return check_launch("bp_combine");
 }
 
 static int launch_bp_combine(int dtype, const void* pm, int edges, int chi, void* msgs_a, void* msgs_b,
                              const int32_t* loop_state, void* dist_parts, cudaStream_t st) {
-    const int blocks = (int)(((int64_t)edges * 32 + 255) / 256);
-    if (dtype == BQA_C64)
-        bp_combine_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float2*>(pm), edges, chi,
-                                                          static_cast<const float2*>(msgs_a), static_cast<float2*>(msgs_b),
-                                                          loop_state, static_cast<uint32_t*>(dist_parts));
-    else
-        bp_combine_kernel<double><<<blocks, 256, 0, st>>>(static_cast<const double2*>(pm), edges, chi,
-                                                           static_cast<const double2*>(msgs_a),
-                                                           static_cast<double2*>(msgs_b), loop_state,
-                                                           static_cast<unsigned long long*>(dist_parts));
-    return check_launch("bp_combine");
+    return dtype == BQA_C64
+               ? launch_bp_combine_t<float>(pm, edges, chi, msgs_a, msgs_b, loop_state, dist_parts, st)
+               : launch_bp_combine_t<double>(pm, edges, chi, msgs_a, msgs_b, loop_state, dist_parts, st);
 }
 
 }  // namespace bqa
@@ -1468,6 +1918,7 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes, int32_t n_classes, int32_t 
         return set_error(BQA_ERR_ARG, "bqa_bp_sweep_split: bad argument");
     if (dtype != BQA_C64 && dtype != BQA_C128) return set_error(BQA_ERR_ARG, "bqa_bp_sweep_split: unknown dtype %d", dtype);
     cudaStream_t st = as_stream(stream);
+    std::vector<bqa_class> rest;
     for (int c = 0; c < n_classes; ++c) {
         const bqa_class& k = classes[c];
         if (k.count <= 0 || k.degree == 0) continue;
@@ -1484,21 +1935,14 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes, int32_t n_classes, int32_t 
                 continue;
             }
         }
-        bqa_class one = k;
-        rc = run_classes_dt(dtype, MODE_PSPLIT, &one, 1, chi, msgs_a, msgs_b, pm, nullptr, loop_state, 0.0, st);
+        rest.push_back(k);
+    }
+    if (!rest.empty()) {   // classes without a half-node kernel: their open-bond blocks in one pass
+        const int rc = run_classes_dt(dtype, MODE_PSPLIT, rest.data(), (int)rest.size(), chi, msgs_a, msgs_b, pm,
+                                      nullptr, loop_state, 0.0, st);
         if (rc) return rc;
     }
-    const int blocks = (int)(((int64_t)edges * 32 + 255) / 256);
-    if (dtype == BQA_C64)
-        bp_combine_kernel<float><<<blocks, 256, 0, st>>>(static_cast<const float2*>(pm), edges, chi,
-                                                          static_cast<const float2*>(msgs_a), static_cast<float2*>(msgs_b),
-                                                          loop_state, static_cast<uint32_t*>(dist_parts));
-    else
-        bp_combine_kernel<double><<<blocks, 256, 0, st>>>(static_cast<const double2*>(pm), edges, chi,
-                                                           static_cast<const double2*>(msgs_a),
-                                                           static_cast<double2*>(msgs_b), loop_state,
-                                                           static_cast<unsigned long long*>(dist_parts));
-    return check_launch("bp_combine");
+    return launch_bp_combine(dtype, pm, edges, chi, msgs_a, msgs_b, loop_state, dist_parts, st);
 }
 
 int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t chi, int32_t dtype,
@@ -1512,12 +1956,15 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t c
         return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: bad argument");
     if (dtype != BQA_C64 && dtype != BQA_C128) return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: unknown dtype %d", dtype);
     cudaStream_t st = as_stream(stream);
+    std::vector<bqa_class> def_rest, gen_rest;   // classes of the generic kernel: one launch each list
+    std::vector<int> gen_threads;                 // their CTA sizes (0: the kernel's own)
     for (int c = 0; c < n_classes; ++c) {
         const bqa_class& k = classes[c];
         if (k.count <= 0 || k.degree == 0) continue;
-        const int v = variants[c];
-        if (v < BQA_VARIANT_DEFAULT || v > BQA_VARIANT_MIXED)
-            return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: unknown variant %d", v);
+        const int v = variants[c] & 0xff, warps = (variants[c] >> 8) & 0xff;
+        if (v < BQA_VARIANT_DEFAULT || v > BQA_VARIANT_MIXED || (variants[c] >> 16) != 0 || warps > 32 ||
+            (warps && v != BQA_VARIANT_GENERIC))
+            return set_error(BQA_ERR_ARG, "bqa_bp_sweep_plan: unknown variant %d", variants[c]);
         int rc = BQA_OK;
         if (v == BQA_VARIANT_TENSOR || v == BQA_VARIANT_TENSOR_BF16 || v == BQA_VARIANT_MIXED) {
             if (dtype != BQA_C64 || !pm || k.degree != 3 || chi != 16)
@@ -1548,20 +1995,12 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t c
                                                    k.count, st);
         } else if (v == BQA_VARIANT_DEFAULT) {
             // the kernel bqa_bp_sweep_split / bqa_bp_sweep would launch for this class
-            bqa_class one = k;
-            if (pm) {
-                int hit = 0;
-                if (dtype == BQA_C64 && g_use_tiled) {
-                    NodeArgs<float> a = class_args<float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state);
-                    hit = try_half(a, k.count, st, &rc);
-                }
-                if (!hit)
-                    rc = run_classes_dt(dtype, MODE_PSPLIT, &one, 1, chi, msgs_a, msgs_b, pm, nullptr, loop_state, 0.0,
-                                        st);
-            } else {
-                rc = run_classes_dt(dtype, MODE_BP, &one, 1, chi, msgs_a, msgs_b, nullptr, dist_parts, loop_state, 0.0,
-                                    st);
+            int hit = 0;
+            if (pm && dtype == BQA_C64 && g_use_tiled) {
+                NodeArgs<float> a = class_args<float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state);
+                hit = try_half(a, k.count, st, &rc);
             }
+            if (!hit) def_rest.push_back(k);
         } else if (v == BQA_VARIANT_TILED) {
             if (dtype != BQA_C64)
                 return set_error(BQA_ERR_UNSUPPORTED, "bqa_bp_sweep_plan: no register-tiled complex128 kernel");
@@ -1570,13 +2009,23 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t c
             if (!hit)
                 return set_error(BQA_ERR_UNSUPPORTED, "bqa_bp_sweep_plan: no register-tiled kernel for degree %d, "
                                  "bond dim %d", k.degree, chi);
-        } else if (dtype == BQA_C64) {
-            rc = pm ? sweep_class_generic<MODE_PSPLIT, float>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state, st)
-                    : sweep_class_generic<MODE_BP, float>(k, chi, msgs_a, msgs_b, nullptr, dist_parts, loop_state, st);
         } else {
-            rc = pm ? sweep_class_generic<MODE_PSPLIT, double>(k, chi, msgs_a, msgs_b, pm, nullptr, loop_state, st)
-                    : sweep_class_generic<MODE_BP, double>(k, chi, msgs_a, msgs_b, nullptr, dist_parts, loop_state, st);
+            gen_rest.push_back(k);   // the generic kernel (global-memory form beyond shared memory)
+            gen_threads.push_back(32 * warps);
         }
+        if (rc) return rc;
+    }
+    const int mode = pm ? MODE_PSPLIT : MODE_BP;
+    void* out = pm ? pm : nullptr;
+    void* dist = pm ? nullptr : dist_parts;
+    if (!def_rest.empty()) {
+        const int rc = run_classes_dt(dtype, mode, def_rest.data(), (int)def_rest.size(), chi, msgs_a, msgs_b, out, dist,
+                                      loop_state, 0.0, st);
+        if (rc) return rc;
+    }
+    if (!gen_rest.empty()) {
+        const int rc = run_classes_dt(dtype, mode, gen_rest.data(), (int)gen_rest.size(), chi, msgs_a, msgs_b, out, dist,
+                                      loop_state, 0.0, st, false, gen_threads.data());
         if (rc) return rc;
     }
     return pm ? launch_bp_combine(dtype, pm, edges, chi, msgs_a, msgs_b, loop_state, dist_parts, st) : BQA_OK;
@@ -1619,6 +2068,7 @@ int32_t bqa_ext_msgs_split(const bqa_class* classes, int32_t n_classes, int32_t 
         return set_error(BQA_ERR_ARG, "bqa_ext_msgs_split: bad argument");
     if (dtype != BQA_C64 && dtype != BQA_C128) return set_error(BQA_ERR_ARG, "bqa_ext_msgs_split: unknown dtype %d", dtype);
     cudaStream_t st = as_stream(stream);
+    std::vector<bqa_class> rest;
     for (int c = 0; c < n_classes; ++c) {
         const bqa_class& k = classes[c];
         if (k.count <= 0 || k.degree == 0) continue;
@@ -1635,8 +2085,11 @@ int32_t bqa_ext_msgs_split(const bqa_class* classes, int32_t n_classes, int32_t 
                 continue;
             }
         }
-        bqa_class one = k;
-        rc = run_classes_dt(dtype, MODE_PSPLIT, &one, 1, chi, msgs, nullptr, pm, nullptr, nullptr, 0.0, st);
+        rest.push_back(k);
+    }
+    if (!rest.empty()) {
+        const int rc = run_classes_dt(dtype, MODE_PSPLIT, rest.data(), (int)rest.size(), chi, msgs, nullptr, pm,
+                                      nullptr, nullptr, 0.0, st);
         if (rc) return rc;
     }
     return bqa_ext_combine(pm, edges, chi, dtype, edge_j, ztime, ext_out, stream);

@@ -483,6 +483,24 @@ class Annealer:
                           self.stream)
         else:
             self.lib.call("bqa_run_layer", ctypes.byref(j), xtime, ztime, ctypes.byref(res), self.stream)
+        return self._adopt(j, res)
+
+    def run_layer_packed(self, xtime: float, ztime: float, packer) -> dict:
+        """One step whose BP run is swept together with other jobs' (``packer``, a
+        ``serve.BpPacker``): the gate layer through bqa_gate_layer on this job's stream, then
+        the BP run in the packer's shared launches.  The state afterwards is the same bits as
+        after ``run_layer``."""
+        if self.ctx.max_bp_iters_number < 1:
+            raise ValueError("max_bp_iter_number must be >= 1 to run belief propagation")
+        j, cls = self._job_struct()
+        res = _lib.BqaLayerInfo()
+        self.lib.call("bqa_gate_layer", ctypes.byref(j), xtime, ztime, ctypes.byref(res), self.stream)
+        self.torch.cuda.current_stream(self.device).synchronize()
+        packer.run_bp(j, res)
+        return self._adopt(j, res)
+
+    def _adopt(self, j, res) -> dict:
+        """Take over the job struct's state after a native step and log / record its figures."""
         self.chi, self.chis, self.lam_stride, self.mcur, self.tcur = j.chi, j.chis, j.lam_stride, j.mcur, j.tcur
         self.blocks_valid = bool(j.blocks_valid)
         if res.svd_not_converged:

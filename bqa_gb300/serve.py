@@ -8,13 +8,22 @@ stream: the library calls and device synchronisations release the interpreter lo
 the kernels of concurrent jobs overlap on the device while every job keeps its own device
 state (tensors, messages, scratch).  A job's footprint is released when it finishes.
 
+BP runs are packed (``pack_bp=True``, the default): after its gate layer a job hands its BP
+run to the server's ``BpPacker``, which sweeps the runs of all the jobs waiting at that
+moment in shared launches -- each node kernel once per sweep for the degree classes of every
+job that uses it, one combine and one decision kernel for all of them (bqa_bp_packed) --
+takes each job out when its own loop state says done and lets newly waiting jobs join
+between sweep groups.
+
 Results are the ``run_qa`` result lists; ``stats()`` reports per-job latency (arrival to
 result) percentiles and the throughput of the whole stream.  A job's result is the same
-whether it runs alone or in a mix: the kernels are deterministic and jobs share no device
+whether it runs alone or in a mix, packed or not: the kernels are deterministic, a CTA
+computes the same values in a shared launch as in the job's own, and jobs share no device
 buffers.
 """
 from __future__ import annotations
 
+import ctypes
 import heapq
 import itertools
 import threading
@@ -64,6 +73,137 @@ def job_footprint(ctx: Context, precision: str | None = None, sm_count: int | No
     return int(total) + (1 << 20)
 
 
+class _BpRun:
+    """One job's BP run handed to the packer."""
+
+    def __init__(self, job, info):
+        self.job = job            # the job's bqa_job struct (kept alive by the job's thread)
+        self.info = info          # its bqa_layer_info, filled in by bqa_bp_end
+        self.launched = 0
+        self.error: BaseException | None = None
+        self.done = threading.Event()
+
+
+class BpPacker:
+    """Sweeps the BP runs of the jobs waiting for one in shared launches (bqa_bp_packed).
+
+    Job threads call ``run_bp`` after their gate layer (their stream synchronised) and block
+    until their run is done.  One packer thread takes every waiting run (up to 64 at once),
+    zeroes its loop state (bqa_bp_begin), launches ``sweeps_per_call`` packed sweeps, reads all
+    loop states with one copy, and concludes the runs that are done (bqa_bp_end); runs that are
+    not go on with the next sweep group, joined by runs that arrived meanwhile."""
+
+    MAX_JOBS = 64
+
+    def __init__(self, device=None, sweeps_per_call: int = 4):
+        import torch
+        self.torch = torch
+        self.lib = _lib.load()
+        dev = torch.device(device if device is not None else "cuda")
+        self.device = torch.device("cuda", dev.index if dev.index is not None else torch.cuda.current_device())
+        self.sweeps_per_call = max(1, int(sweeps_per_call))
+        self.stream = torch.cuda.Stream(device=self.device)
+        self.ls_dev = torch.zeros(8 * self.MAX_JOBS, dtype=torch.int32, device=self.device)
+        self.ls_host = (ctypes.c_int32 * (8 * self.MAX_JOBS))()
+        self._cond = threading.Condition()
+        self._waiting: list[_BpRun] = []
+        self._stop = False
+        self._died: BaseException | None = None
+        self.calls = 0
+        self.packed_runs = 0        # sum over calls of the runs swept together
+        self.max_packed = 0
+        self._thread = threading.Thread(target=self._loop, daemon=True)
+        self._thread.start()
+
+    def run_bp(self, job, info) -> None:
+        run = _BpRun(job, info)
+        with self._cond:
+            if self._stop or self._died is not None:
+                raise RuntimeError("the BP packer is closed") from self._died
+            self._waiting.append(run)
+            self._cond.notify_all()
+        while not run.done.wait(1.0):
+            if not self._thread.is_alive():
+                raise RuntimeError("the BP packer's thread ended") from self._died
+        if run.error is not None:
+            raise run.error
+
+    def close(self) -> None:
+        with self._cond:
+            self._stop = True
+            self._cond.notify_all()
+        self._thread.join()
+
+    def stats(self) -> dict:
+        return {"packed_calls": self.calls, "sweeps_per_call": self.sweeps_per_call,
+                "mean_runs_per_call": self.packed_runs / self.calls if self.calls else 0.0,
+                "max_runs_per_call": self.max_packed}
+
+    def _fail(self, runs, e: BaseException) -> None:
+        for r in runs:
+            r.error = e
+            r.done.set()
+
+    def _loop(self) -> None:
+        active: list[_BpRun] = []
+        try:
+            self._serve(active)
+        except BaseException as e:   # noqa: BLE001 -- every waiting job learns of it
+            self._died = e
+            with self._cond:
+                waiting, self._waiting = self._waiting, []
+            self._fail(active + waiting, e)
+
+    def _serve(self, active: list) -> None:
+        torch, lib = self.torch, self.lib
+        torch.cuda.set_device(self.device)
+        st = self.stream.cuda_stream
+        while True:
+            with self._cond:
+                while not self._waiting and not active and not self._stop:
+                    self._cond.wait()
+                if self._stop and not active:
+                    self._fail(self._waiting, RuntimeError("the BP packer is closed"))
+                    self._waiting = []
+                    return
+                room = self.MAX_JOBS - len(active)
+                new, self._waiting = self._waiting[:room], self._waiting[room:]
+            for r in new:
+                try:
+                    lib.call("bqa_bp_begin", ctypes.byref(r.job), st)
+                    active.append(r)
+                except BaseException as e:   # noqa: BLE001 -- reported to the job's thread
+                    self._fail([r], e)
+            if not active:
+                continue
+            n = len(active)
+            jobs = (ctypes.POINTER(_lib.BqaJob) * n)(*[ctypes.pointer(r.job) for r in active])
+            try:
+                lib.call("bqa_bp_packed", jobs, n, self.sweeps_per_call, self.ls_dev.data_ptr(), self.ls_host, st)
+            except BaseException as e:   # noqa: BLE001
+                self._fail(active, e)
+                active.clear()
+                continue
+            self.calls += 1
+            self.packed_runs += n
+            self.max_packed = max(self.max_packed, n)
+            still = []
+            for i, r in enumerate(active):
+                r.launched += self.sweeps_per_call
+                ls = (ctypes.c_int32 * 8)(*self.ls_host[8 * i: 8 * i + 8])
+                if ls[0]:
+                    try:
+                        lib.call("bqa_bp_end", ctypes.byref(r.job), ls, ctypes.byref(r.info))
+                    except BaseException as e:   # noqa: BLE001
+                        r.error = e
+                    r.done.set()
+                elif r.launched >= r.job.max_bp_iters + self.sweeps_per_call:
+                    self._fail([r], RuntimeError("BP loop state did not finish after the iteration cap"))
+                else:
+                    still.append(r)
+            active[:] = still
+
+
 @dataclass(order=True)
 class _Job:
     arrival: float
@@ -81,7 +221,7 @@ class JobServer:
     """Admit jobs by HBM footprint, run them concurrently, one stream and host thread each."""
 
     def __init__(self, hbm_budget: int | None = None, device=None, precision: str | None = None,
-                 max_active: int = 64):
+                 max_active: int = 64, pack_bp: bool = True):
         import torch
         self.torch = torch
         self.device = torch.device(device if device is not None else "cuda")
@@ -103,6 +243,7 @@ class JobServer:
         self.peak_active = 0
         self.peak_bytes = 0
         self._t0 = time.perf_counter()
+        self.packer = BpPacker(self.device) if pack_bp and self.device.type == "cuda" else None
 
     # ---- submission --------------------------------------------------------------------
     def now(self) -> float:
@@ -131,7 +272,10 @@ class JobServer:
                 out = []
                 for ins in job.ctx.instructions:
                     if isinstance(ins, dict):
-                        annealer.run_layer(ins["xtime"], ins["ztime"])
+                        if self.packer is not None:
+                            annealer.run_layer_packed(ins["xtime"], ins["ztime"], self.packer)
+                        else:
+                            annealer.run_layer(ins["xtime"], ins["ztime"])
                     elif ins == cfg.MEASURE:
                         out.append(["measurement_outcomes", annealer.measure()])
                     else:
@@ -189,7 +333,16 @@ class JobServer:
             return {}
         lat = np.array([j.end - j.arrival for j in jobs])
         span = max(j.end for j in jobs) - min(j.arrival for j in jobs)
-        return {"jobs": len(jobs), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-                "mean_s": float(lat.mean()), "jobs_per_s": len(jobs) / span if span > 0 else None,
-                "steps": int(sum(sum(isinstance(i, dict) for i in j.ctx.instructions) for j in jobs)),
-                "peak_active": self.peak_active, "peak_bytes": self.peak_bytes}
+        out = {"jobs": len(jobs), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+               "mean_s": float(lat.mean()), "jobs_per_s": len(jobs) / span if span > 0 else None,
+               "steps": int(sum(sum(isinstance(i, dict) for i in j.ctx.instructions) for j in jobs)),
+               "peak_active": self.peak_active, "peak_bytes": self.peak_bytes}
+        if self.packer is not None:
+            out["bp_packing"] = self.packer.stats()
+        return out
+
+    def close(self) -> None:
+        """Stop the BP packer's thread (the server takes no jobs afterwards)."""
+        if self.packer is not None:
+            self.packer.close()
+            self.packer = None

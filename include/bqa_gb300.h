@@ -172,6 +172,35 @@ int32_t bqa_run_layer_graph(bqa_job* job, bqa_graph_cache* cache, double xtime, 
  * best_dist are filled in, bond_dim is the job's current bond dim. */
 int32_t bqa_run_bp_graph(bqa_job* job, bqa_graph_cache* cache, bqa_layer_info* info, void* stream);
 
+/*
+ * Packed BP runs: the BP loops of several resident jobs (src/bqa/state.py:97-124, whose per
+ * degree-class sweep is the loop at :105-112) in shared launches, for a server that keeps many
+ * jobs on one GPU.
+ *
+ * bqa_gate_layer: the gate layer of bqa_run_layer alone (extended messages, truncation,
+ * tensor update, messages from the new lambdas); blocks at its one read (column maxima).
+ * bqa_bp_begin: zero the job's loop state and convergence maxima on `stream` (the start of a
+ * BP run).  bqa_bp_packed: `sweeps` sweeps of every listed job (1 <= n_jobs <= 64, one dtype);
+ * each sweep launches each node kernel ONCE for the classes of all the jobs that use it (the
+ * register-tiled half-node kernels, the generic kernel per (degree, bond dim); kernels with
+ * per-class scratch or tensor memory one class at a time), one combine for all two-stage
+ * jobs and one decision kernel for all loop states, then damping where a job damps.  A job
+ * whose loop state says done returns at once from the later sweeps.  Afterwards the jobs'
+ * loop states are gathered into loop_states (device, 8 * n_jobs int32) and copied to
+ * host_loop_states (8 * n_jobs int32, job i at 8 i); the call blocks until then.
+ * bqa_bp_end (host only): conclude a job's BP run whose loop state (host copy, 8 int32) says
+ * done: current message buffer, reusable open-bond blocks, info->sweeps / bp_exhausted /
+ * best_dist.  A job's state after bqa_gate_layer + bqa_bp_begin + bqa_bp_packed until done +
+ * bqa_bp_end is bit-identical to bqa_run_layer's: every CTA computes what it computes in the
+ * job's own launches.  Each job's gate layer must be complete (its stream synchronised)
+ * before its first packed sweep, and the packed stream's work before the job's next step.
+ */
+int32_t bqa_gate_layer(bqa_job* job, double xtime, double ztime, bqa_layer_info* info, void* stream);
+int32_t bqa_bp_begin(bqa_job* job, void* stream);
+int32_t bqa_bp_packed(bqa_job* const* jobs /* host array */, int32_t n_jobs, int32_t sweeps,
+                      int32_t* loop_states /* device */, int32_t* host_loop_states, void* stream);
+int32_t bqa_bp_end(bqa_job* job, const int32_t* loop_state /* host */, bqa_layer_info* info);
+
 /* ABI version of this header (bumped on any signature change). */
 int32_t bqa_abi_version(void);
 
@@ -227,10 +256,17 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_
  * (complex64, degree 2-4, chi in {4, 8, 12, 16} minus (2, 4) and (4, 12+)); at degree 3, bond dim
  * 16 it is the CUDA-core half-node kernel.  TENSOR is the tensor-core half-node kernel (two-stage,
  * complex64, degree 3, bond dim 16 only; BQA_ERR_UNSUPPORTED elsewhere), which is also what
- * DEFAULT launches there when BQA_GB300_TC=1 was set when the library loaded.  variants == NULL is
+ * DEFAULT launches there when BQA_GB300_TC=1 was set when the library loaded.  GENERIC may carry
+ * the CTA size of the shared-memory generic kernel as warps per node in bits 8-15
+ * (GENERIC | (w << 8), 1 <= w <= 32; 0 keeps the kernel's own choice of at most 8 warps); above
+ * 8 warps only at bond dims <= 8 (BQA_ERR_UNSUPPORTED otherwise), and the CTA size does not
+ * change the messages (every output is formed by one thread in a fixed order).  Classes whose
+ * nodes exceed shared memory keep the global-memory kernel's 256 threads.  variants == NULL is
  * bqa_bp_sweep_split (pm != NULL) or bqa_bp_sweep.  The choices are the search space of the
  * host-side autotuner (bqa_gb300/autotune.py); every variant computes the same messages up to
- * rounding.  Same loop_state and dist_parts behaviour as bqa_bp_sweep.
+ * rounding.  Generic-kernel classes of one CTA size go out in one launch where that costs no
+ * class an extra wave (BQA_GB300_MERGE_CLASSES=0 at library load: one launch per class; the
+ * messages are the same bits).  Same loop_state and dist_parts behaviour as bqa_bp_sweep.
  */
 int32_t bqa_bp_sweep_plan(const bqa_class* classes /* host array */, int32_t n_classes, int32_t chi, int32_t dtype,
                           const int32_t* variants /* host */, void* msgs_a, void* msgs_b, void* pm, int32_t edges,

@@ -112,3 +112,28 @@ def test_tuned_anneal_matches_oracle_and_every_driver():
     want = gc.arrays(name)["result0_bloch_vectors"]
     err = np.abs(g.bloch_vectors() - want).max()
     assert err < 1e-3, err
+
+
+@pytest.mark.parametrize("name,chi", [("mixed_n18_chi3", 3), ("rr4_n20_chi4", 4), ("grid3x4_chi4_damped", 5),
+                                      ("rr3_n24_chi8", 8), ("mixed_n18_chi3", 4)])
+@pytest.mark.parametrize("two_stage", [True, False])
+def test_generic_cta_size_gives_the_same_messages(name, chi, two_stage):
+    """The generic kernel at 2, 16 or 32 warps per node writes the bits of its own CTA size,
+    and equals the oracle; above 8 warps bond dims beyond 8 are refused."""
+    from bqa_gb300.autotune import generic_warps
+    octx, st, job = random_state(name, chi, seed=4)
+    want = oracle_sweep(octx, st)
+    ref = plan_sweep(job, [V.BQA_VARIANT_GENERIC] * len(job.classes), two_stage)
+    assert rel_err(ref, want) < RTOL
+    for w in (2, 16, 32):
+        got = plan_sweep(job, [generic_warps(w)] * len(job.classes), two_stage)
+        assert np.array_equal(got, ref), w
+
+
+def test_generic_cta_size_above_8_warps_refused_beyond_bond_dim_8():
+    from bqa_gb300.autotune import generic_warps
+    _, _, job = random_state("rr3_n16_chi4", 12, seed=4)
+    with pytest.raises(_lib.BqaError, match="no 512-thread build"):
+        plan_sweep(job, [generic_warps(16)] * len(job.classes), True)
+    with pytest.raises(_lib.BqaError, match="unknown variant"):
+        plan_sweep(job, [V.BQA_VARIANT_TILED | (4 << 8)] * len(job.classes), True)

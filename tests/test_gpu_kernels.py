@@ -364,3 +364,49 @@ def test_mma_probe_runs():
     assert probes.bqa_mma_probe(2, 152, 10, _ptr(out), torch.cuda.current_stream().cuda_stream) == 1
     for kind in (0, 1):
         assert 10.0 < bench.mma_peak_tflops(torch.device("cuda"), kind) < 5000.0
+
+
+_MERGE_SCRIPT = """
+import sys, numpy as np
+from bqa_gb300 import _lib
+from tests.test_gpu_kernels import random_state
+from tests.test_gpu_autotune import plan_sweep
+out = {}
+for name, chi, prec in (("mixed_n18_chi3", 3, "single"), ("grid3x4_chi4_damped", 5, "single"),
+                        ("tree9", 2, "single"), ("mixed_n18_chi3", 3, "double")):
+    octx, st, job = random_state(name, chi, seed=5, precision=prec)
+    key = f"{name}_{chi}_{prec}"
+    for v in (_lib.BQA_VARIANT_GENERIC, _lib.BQA_VARIANT_DEFAULT):
+        for two_stage in (True, False):
+            out[f"{key}_plan{v}{two_stage}"] = plan_sweep(job, [v] * len(job.classes), two_stage)
+            out[f"{key}_dist{v}{two_stage}"] = job.dist_parts.cpu().numpy()
+    out[key + "_rho"] = job.density_matrices()
+    out[key + "_zz"] = job.edge_zz()
+    job.run_layer(0.07, 0.11)
+    tens, msgs, lam = job.get_state()
+    out[key + "_msgs"] = msgs
+    out[key + "_lam"] = lam
+    out[key + "_bloch"] = job.bloch_vectors()
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_merged_class_launch_bit_identical_to_per_class(tmp_path):
+    """One launch of the generic kernel over several degree classes (the default) gives the
+    bits of one launch per class (BQA_GB300_MERGE_CLASSES=0): BP sweeps, extended messages,
+    open-bond blocks and densities, through a whole gate layer, in both precisions."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    out = {}
+    for flag in ("1", "0"):
+        env = dict(os.environ, BQA_GB300_MERGE_CLASSES=flag, PYTHONPATH=str(root))
+        f = tmp_path / f"merge{flag}.npz"
+        subprocess.run([sys.executable, "-c", _MERGE_SCRIPT, str(f)], cwd=root, env=env, check=True, timeout=600)
+        out[flag] = np.load(f)
+    assert sorted(out["1"].files) == sorted(out["0"].files)
+    for k in out["1"].files:
+        assert np.array_equal(out["1"][k], out["0"][k]), k
+        assert np.isfinite(out["1"][k]).all(), k

@@ -36,20 +36,27 @@ def test_too_large_job_is_rejected_at_submission():
 
 
 @pytest.mark.gpu
-def test_results_alone_equal_results_in_the_mix():
+@pytest.mark.timeout(600)
+@pytest.mark.parametrize("pack_bp", [True, False])
+def test_results_alone_equal_results_in_the_mix(pack_bp):
+    """Packed (BP runs of waiting jobs swept in shared launches) or not, every job's results in
+    the mix are the bits of its run alone."""
     import bqa_gb300
     from bqa_gb300.serve import JobServer, job_footprint
     jobs = small_jobs()
     alone = [bqa_gb300.run_qa(dict(j)) for j in jobs]
     fps = [job_footprint(build_context(dict(j))) for j in jobs]
     budget = sum(sorted(fps)[-3:])          # at most ~3 jobs resident: admission must queue
-    srv = JobServer(hbm_budget=budget)
+    srv = JobServer(hbm_budget=budget, pack_bp=pack_bp)
     ids = [srv.submit(dict(j), arrival=0.01 * k) for k, j in enumerate(jobs)]
-    out = srv.run(timeout=600)
+    out = srv.run(timeout=300)
+    st = srv.stats()
+    srv.close()
     for i, want in zip(ids, alone):
         got = out[i]
         assert [g[0] for g in got] == [w[0] for w in want]
         for g, w in zip(got, want):
             assert np.array_equal(np.asarray(g[1]), np.asarray(w[1]))
-    st = srv.stats()
     assert st["jobs"] == len(jobs) and st["p99_s"] >= st["p50_s"] > 0
+    if pack_bp:
+        assert st["bp_packing"]["packed_calls"] > 0 and st["bp_packing"]["max_runs_per_call"] >= 1
