@@ -847,11 +847,13 @@ def run_mixed_mode(args) -> None:
     job.stats.clear()
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed_steps")
     a.record()
     for i in range(args.steps):
         job.run_layer(steps[s + i]["xtime"], steps[s + i]["ztime"])
     b.record()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     ms = a.elapsed_time(b)
     split: dict = {}
     for name, t, _, _ in job.kernel_times():
