@@ -168,24 +168,64 @@ __device__ __forceinline__ void mode_product(const C* __restrict__ X, C* __restr
     }
 }
 
-// P[s][a][b] = sum_{l, r} conj(T[s][l][a][r]) X[s][l][b][r]; T, X are [2][L][n][R].
+// Parts of a closing contraction's sum over L * R = chi^(d-1) terms: up to 256 (output, part)
+// items, at least 16 terms per part.  A function of the shape only, so a node's outputs do
+// not depend on the CTA size.
+__host__ __device__ inline int close_parts(int d, int chi) {
+    const int outs = 2 * chi * chi;
+    const int terms = ipow(chi, d > 0 ? d - 1 : 0);
+    int g = 256 / outs;
+    if (g > terms / 16) g = terms / 16;
+    return g < 1 ? 1 : g;
+}
+
+// P[s][a][b] = sum_{l, r} conj(T[s][l][a][r]) X[s][l][b][r]; T, X are [2][L][n][R].  With G > 1
+// parts, item (g, o) sums the g-th contiguous chunk of the (l, r) terms of output o into
+// scratch[g][o] (G * 2 n^2 elements), and the parts are then added in the order g = 0..G-1.
 template <typename C>
 __device__ __forceinline__ void close_psplit(const C* __restrict__ T, const C* __restrict__ X, C* __restrict__ P,
-                                             int L, int n, int Rr) {
+                                             int L, int n, int Rr, C* __restrict__ scratch, int G) {
     const int n2 = n * n;
     const size_t per_s = (size_t)L * n * Rr;
-    for (int o = threadIdx.x; o < 2 * n2; o += blockDim.x) {
+    if (G == 1) {
+        for (int o = threadIdx.x; o < 2 * n2; o += blockDim.x) {
+            const int s = o >= n2;
+            const int ab = o - s * n2;
+            const int a = ab / n, b = ab - a * n;
+            const C* tp = T + s * per_s + (size_t)a * Rr;
+            const C* xp = X + s * per_s + (size_t)b * Rr;
+            C acc = c_zero<C>();
+            for (int l = 0; l < L; ++l) {
+                for (int r = 0; r < Rr; ++r) acc = c_fma_conj(tp[r], xp[r], acc);
+                tp += (size_t)n * Rr;
+                xp += (size_t)n * Rr;
+            }
+            P[o] = acc;
+        }
+        return;
+    }
+    const int terms = L * Rr, chunk = (terms + G - 1) / G;
+    for (int w = threadIdx.x; w < 2 * n2 * G; w += blockDim.x) {
+        const int g = w / (2 * n2), o = w - g * 2 * n2;
         const int s = o >= n2;
         const int ab = o - s * n2;
         const int a = ab / n, b = ab - a * n;
+        const int t0 = g * chunk, t1 = min(terms, t0 + chunk);
+        int l = t0 / Rr, r = t0 - l * Rr;
         const C* tp = T + s * per_s + (size_t)a * Rr;
         const C* xp = X + s * per_s + (size_t)b * Rr;
         C acc = c_zero<C>();
-        for (int l = 0; l < L; ++l) {
-            for (int r = 0; r < Rr; ++r) acc = c_fma_conj(tp[r], xp[r], acc);
-            tp += (size_t)n * Rr;
-            xp += (size_t)n * Rr;
+        for (int t = t0; t < t1; ++t) {
+            const size_t off = (size_t)l * n * Rr + r;
+            acc = c_fma_conj(tp[off], xp[off], acc);
+            if (++r == Rr) { r = 0; ++l; }
         }
+        scratch[w] = acc;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < 2 * n2; o += blockDim.x) {
+        C acc = scratch[o];
+        for (int g = 1; g < G; ++g) acc = c_add(acc, scratch[g * 2 * n2 + o]);
         P[o] = acc;
     }
 }
@@ -309,7 +349,9 @@ __device__ __forceinline__ void node_body(const NodeArgs<R>& a, int node) {
             __syncthreads();
             cur = nxt;
         }
-        close_psplit(sT, cur, sP, ipow(chi, idx), chi, ipow(chi, d - 1 - idx));
+        // the ping-pong buffer cur is not holds the closing contraction's partial sums
+        close_psplit(sT, cur, sP, ipow(chi, idx), chi, ipow(chi, d - 1 - idx), cur == sA ? sB : sA,
+                     close_parts(d, chi));
         __syncthreads();
 
         write_outputs<MODE, R>(a, node, idx, sP, msgs_in, msgs_out, num2, den2);
