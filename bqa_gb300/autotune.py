@@ -12,14 +12,16 @@ bond dim and the number of nodes:
   generic shared-memory kernel (global-memory form for nodes beyond shared memory), or, in the
   two-stage form at degree 3, bond dim 16, the half-node kernel whose bond products run on the
   tensor cores (tcgen05, 3xTF32);
-* for the generic kernel, the warps per node (CTA size): its own choice (up to 8 warps, from
-  the node's fibre count) or 16 or 32 warps at bond dims <= 8, where large-degree nodes fill
-  so much shared memory that one or two CTAs share an SM.
+* for the generic kernel, the warps per node (CTA size): its own choice (one thread per fibre,
+  up to 8 warps, or up to 32 for nodes whose shared memory leaves room for at most two CTAs
+  per SM) or 16 or 32 warps at bond dims <= 8.
 
 ``tune(annealer)`` times every candidate of every class on the job's live state (CUDA events
 on the job's stream, a warm-up launch then ``reps`` timed launches, each reading the current
 messages and writing the idle message buffer, so the job's state is untouched), keeps the
-fastest per class and form, then times the two complete sweeps and keeps the faster form.
+fastest per class and form, then times the two complete sweeps and keeps the faster form (on
+the complex64 path the two-stage form unless the one-stage sweep is over 15% faster: a
+converged two-stage run also hands the next step's extended messages their open-bond blocks).
 Results are cached per process by (device, precision, degree, bond dim, class size rounded up
 to a power of two), and optionally in a JSON file named by the environment variable
 BQA_GB300_TUNE_CACHE, so a job pays for tuning only at (degree, bond dim) pairs no earlier job
@@ -40,6 +42,7 @@ VARIANT_NAMES = {_lib.BQA_VARIANT_DEFAULT: "default", _lib.BQA_VARIANT_TILED: "t
                  _lib.BQA_VARIANT_GENERIC: "generic", _lib.BQA_VARIANT_TENSOR: "tensor",
                  _lib.BQA_VARIANT_TENSOR_BF16: "tensor-bf16", _lib.BQA_VARIANT_MIXED: "mixed"}
 _SPLIT = 1 << 20   # flag of a two-stage timing in the tuner's per-class records
+SPLIT_BONUS = 1.15  # two-stage sweeps win unless one-stage ones are faster by more than 15%
 
 
 def generic_warps(warps: int) -> int:
@@ -240,7 +243,12 @@ def tune(job, reps: int = 3) -> Plan:
             timer = timer or _Timer(job, reps)
             ms = {"split": timer.time(classes, best[True], True), "whole": timer.time(classes, best[False], False)}
             inf = float("inf")
-            form = {"split": (ms["split"] or inf) <= (ms["whole"] or inf), "ms": ms}
+            # a two-stage run that converges leaves the open-bond blocks the next step's extended
+            # messages start from (one combine pass instead of a sweep-like pass); on the
+            # complex64 path that is worth about one sweep per step, so the two-stage form is kept
+            # unless the one-stage sweep is faster by more than SPLIT_BONUS
+            bonus = SPLIT_BONUS if job.split_sweeps and job.reuse_blocks else 1.0
+            form = {"split": (ms["split"] or inf) <= bonus * (ms["whole"] or inf), "ms": ms}
             with _LOCK:
                 _FORM_CACHE[jkey] = form
                 _save()

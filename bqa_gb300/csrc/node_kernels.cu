@@ -1455,11 +1455,17 @@ static int launch_combine_packed(const PackEntry* e, int n, cudaStream_t st) {
     return BQA_OK;
 }
 
-// threads of a generic-kernel CTA for degree d at bond dim chi
-static int generic_threads(int d, int chi) {
+// threads of a generic-kernel CTA for degree d at bond dim chi: one per fibre of a mode
+// product (or output of a closing contraction), at most 256 -- or, for the BP and open-bond
+// passes of nodes whose shared memory leaves room for at most two CTAs per SM, at most 1024
+// (bond dims <= 8: the 1024-thread build), so such nodes still run 16-32 warps per SM
+static int generic_threads(int d, int chi, int mode, size_t elem_bytes) {
     const int fib = 2 * ipow(chi, d > 0 ? d - 1 : 0);
     int threads = ((max(fib, 2 * chi * chi) + 31) / 32) * 32;
-    return threads < 32 ? 32 : (threads > 256 ? 256 : threads);
+    const size_t smem = node_smem_elems(d, chi) * elem_bytes;
+    const bool crowded = (228u * 1024u) / (smem + 1024u) <= 2;
+    const int cap = (crowded && chi <= 8 && (mode == MODE_BP || mode == MODE_PSPLIT)) ? 1024 : 256;
+    return threads < 32 ? 32 : (threads > cap ? cap : threads);
 }
 
 // The generic kernel's build for bond dim chi and CTAs of `threads` threads (0: none).
@@ -1513,7 +1519,7 @@ static int launch_node_generic_merged(const NodeArgs<R>* args, const int* counts
         m.cls[c] = args[c];
         m.first[c + 1] = m.first[c] + counts[c];
         smem = std::max(smem, node_smem_elems(args[c].d, chi) * sizeof(typename Cx<R>::T));
-        own = std::max(own, generic_threads(args[c].d, chi));
+        own = std::max(own, generic_threads(args[c].d, chi, MODE, sizeof(typename Cx<R>::T)));
     }
     if (threads == 0) threads = own;
     if (!valid_cta(threads)) return set_error(BQA_ERR_ARG, "node kernel: %d threads per CTA", threads);
@@ -1620,7 +1626,7 @@ static int run_classes(int mode, const bqa_class* classes, int n_classes, int ch
     auto joins = [&](const NodeArgs<R>& a, int count, int want) {
         if (n_gen == 0) return true;
         if (n_gen == kMaxMergedClasses || want != gen_threads) return false;
-        auto own = [&](int d) { return want ? want : generic_threads(d, chi); };
+        auto own = [&](int d) { return want ? want : generic_threads(d, chi, mode, sizeof(C)); };
         const size_t es = sizeof(C);
         size_t smem = node_smem_elems(a.d, chi) * es;
         int threads = own(a.d);

@@ -258,8 +258,10 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_
  * complex64, degree 3, bond dim 16 only; BQA_ERR_UNSUPPORTED elsewhere), which is also what
  * DEFAULT launches there when BQA_GB300_TC=1 was set when the library loaded.  GENERIC may carry
  * the CTA size of the shared-memory generic kernel as warps per node in bits 8-15
- * (GENERIC | (w << 8), 1 <= w <= 32; 0 keeps the kernel's own choice of at most 8 warps); above
- * 8 warps only at bond dims <= 8 (BQA_ERR_UNSUPPORTED otherwise), and the CTA size does not
+ * (GENERIC | (w << 8), 1 <= w <= 32; 0 keeps the kernel's own choice: one thread per fibre, at
+ * most 8 warps, or 32 for nodes whose shared memory leaves room for at most two CTAs per SM at
+ * bond dims <= 8); above 8 warps only at bond dims <= 8 (BQA_ERR_UNSUPPORTED otherwise), and the
+ * CTA size does not
  * change the messages (every output is formed by one thread in a fixed order).  Classes whose
  * nodes exceed shared memory keep the global-memory kernel's 256 threads.  variants == NULL is
  * bqa_bp_sweep_split (pm != NULL) or bqa_bp_sweep.  The choices are the search space of the
