@@ -301,14 +301,11 @@ def replica_value(world: int, steps: int, t_max_ms: float) -> float:
     return world * steps / (t_max_ms / 1000.0)
 
 
-def gpu_launches(job, kt, steps: int) -> int:
-    """Kernels of this library launched in the timed region: node kernels launch once per
-    degree class, the SVD kernels once per call; every sweep adds its finalize kernel and
-    every step its messages-from-lambdas kernel."""
-    ncls = sum(1 for c in job.classes if c.count > 0 and c.degree > 0)
-    per = {"bp_sweep": ncls + 1, "bp_sweep_skipped": ncls + 1, "ext_msgs": ncls, "apply_update": ncls,
-           "env_factor": 1, "bond_canon": 1}
-    return sum(per.get(k[0], 1) for k in kt) + steps
+def launch_count() -> int:
+    """Kernel launches the backend library has issued so far (bqa_launch_count; the timed steps
+    run Python-driven, without graphs, so every launch counts)."""
+    from bqa_gb300 import _lib
+    return int(_lib.load().dll.bqa_launch_count())
 
 
 def run_gpu_arm(args) -> None:
@@ -361,6 +358,7 @@ def run_gpu_arm(args) -> None:
     job.stats.clear()
     barrier()
     torch.cuda.synchronize(dev)
+    launches0 = launch_count()
     stream = torch.cuda.current_stream(dev)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clocks:
@@ -374,6 +372,7 @@ def run_gpu_arm(args) -> None:
         torch.cuda.nvtx.range_pop()
     barrier()
     ms = ev0.elapsed_time(ev1)
+    launches = launch_count() - launches0
     s += args.steps
     kt = job.kernel_times()
     job.enable_kernel_timing(False)
@@ -407,12 +406,14 @@ def run_gpu_arm(args) -> None:
         mjob.stats.clear()
         barrier()
         torch.cuda.synchronize(dev)
+        mlaunches0 = launch_count()
         m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         m0.record(stream)
         for i in range(args.steps):
             mjob.run_layer(*step_at(sm + i))
         m1.record(stream)
         torch.cuda.synchronize(dev)
+        mlaunches = launch_count() - mlaunches0
         barrier()
         mms = m0.elapsed_time(m1)
         mkt = mjob.kernel_times()
@@ -422,7 +423,7 @@ def run_gpu_arm(args) -> None:
             msplit[name] = msplit.get(name, 0.0) + t
         mixed = {"ms_raw": mms, "sweeps_per_step": float(np.mean([w["sweeps"] for w in mjob.stats])),
                  "time_split_ms": {k: round(v, 2) for k, v in sorted(msplit.items(), key=lambda kv: -kv[1])},
-                 "gpu_launches": gpu_launches(mjob, mkt, args.steps)}
+                 "gpu_launches": mlaunches}
         del mjob
         torch.cuda.empty_cache()
 
@@ -456,6 +457,23 @@ def run_gpu_arm(args) -> None:
     serving = None
     if args.serve_jobs > 0:
         serving = {"stream": SERVING_STREAM, **serving_measurement(args.serve_jobs, args.rate)}
+    # the other configurations' shapes, short: the mixed-degree job at bond dim 4 (every node in
+    # shared memory) and the degree-4 bond-dim-32 sweep (global-memory kernels)
+    tuned = [job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off"
+    secondary = None
+    if args.secondary:
+        del job
+        torch.cuda.empty_cache()
+        mx = mixed_measurement(50000, 4, 3, 2, True)
+        sw = sweep_measurement(2000, 4, 32, "single", "default", 3, 1)
+        secondary = {
+            "mixed_degree_chi4": {"what": "300x300 periodic grid + 50,000 nodes of degree 2/3/5/6 (140k nodes), bond "
+                                          "dim 4, saturated steps, autotuned, device-timed",
+                                  "steps_per_s": mx["steps_per_s"], "ms_per_step_split": mx["ms_per_step_split"],
+                                  "sweeps_per_step": mx["sweeps_per_step"]},
+            "degree4_chi32_sweep": {"what": "one BP sweep, random 4-regular 2,000 nodes, bond dim 32 (16 MB node "
+                                            "tensors, global-memory kernels), random Hermitian messages",
+                                    "ms_per_sweep": sw["ms_per_sweep"], "tflops_algorithmic": sw["tflops"]}}
     if mixed is not None:
         mms = mixed.pop("ms_raw")
         mixed = {"value": replica_value(world, args.steps, mms), "unit": "steps/s", "ms_per_step": mms / args.steps,
@@ -500,8 +518,9 @@ def run_gpu_arm(args) -> None:
         "accuracy": accuracy,
         "mixed_precision": mixed,
         "serving": serving,
-        "autotune": ([job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off"),
-        "gpu_launches": gpu_launches(job, kt, args.steps),
+        "secondary": secondary,
+        "autotune": tuned,
+        "gpu_launches": launches,
         "clocks": clocks.summary(),
         "prep": {"steps": prep_steps, "seconds": round(prep_s, 1)},
         "cpu_baseline": cpu,
@@ -516,14 +535,20 @@ def run_sweep_mode(args) -> None:
     random normalised node tensors with random Hermitian positive-definite trace-normalised
     messages (not diagonal: diagonal incoming messages take the kernels' bond-scaling path,
     which only the first sweep after a truncation sees).  Prints one JSON line."""
+    print(json.dumps(sweep_measurement(args.n, args.degree, args.chi, args.precision, args.variant, args.steps,
+                                       args.warmup)))
+
+
+def sweep_measurement(n: int, degree: int, chi: int, precision: str = "single", variant_name: str = "default",
+                      steps: int = 3, warmup: int = 1) -> dict:
+    """run_sweep_mode's measurement: mean CUDA-event time of `steps` sweeps after `warmup`."""
     import torch
     from bqa_gb300 import instances
     from bqa_gb300.engine import Annealer, _ptr
     from bqa_gb300.layout import build_context
-    conf = instances.headline_gpu_job(n=args.n, seed=0, chi=args.chi, degree=args.degree)
+    conf = instances.headline_gpu_job(n=n, seed=0, chi=chi, degree=degree)
     ctx = build_context(conf)
-    job = Annealer(ctx, precision=args.precision)
-    chi = args.chi
+    job = Annealer(ctx, precision=precision)
     gen = torch.Generator(device="cuda").manual_seed(0)
     for c in job.classes:
         size = c.count * 2 * chi ** c.degree
@@ -542,7 +567,7 @@ def run_sweep_mode(args) -> None:
     cls = job._class_array()
     flops, nbytes = job.bp_sweep_cost()
 
-    variant = {"default": None, "tiled": 1, "generic": 2, "tensor": 3, "tensor-bf16": 4, "mixed": 5}[args.variant]
+    variant = {"default": None, "tiled": 1, "generic": 2, "tensor": 3, "tensor-bf16": 4, "mixed": 5}[variant_name]
     plan = None if variant is None else (ctypes.c_int32 * len(job.classes))(*([variant] * len(job.classes)))
 
     def sweep():
@@ -557,10 +582,10 @@ def run_sweep_mode(args) -> None:
             job.lib.call("bqa_bp_sweep", cls, len(job.classes), chi, job.dtype, _ptr(job.msgs[0]), _ptr(job.msgs[1]),
                          _ptr(job.dist_parts), None, job.stream)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         sweep()
     torch.cuda.synchronize()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     for a, b in evs:
         a.record()
         sweep()
@@ -568,13 +593,13 @@ def run_sweep_mode(args) -> None:
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in evs]
     mean = float(np.mean(ms))
-    print(json.dumps({"mode": "sweep", "n": args.n, "degree": args.degree, "chi": chi, "precision": args.precision,
-                      "variant": args.variant,
-                      "sweeps": args.steps,
-                      "ms_per_sweep": mean, "ms_min": float(np.min(ms)),
-                      "tflops": flops / (mean / 1000) / 1e12, "algorithmic_gbs": nbytes / (mean / 1000) / 1e9,
-                      "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": nbytes,
-                      "msg_updates_per_s": ctx.edges_number / (mean / 1000)}))
+    del job
+    torch.cuda.empty_cache()
+    return {"mode": "sweep", "n": n, "degree": degree, "chi": chi, "precision": precision, "variant": variant_name,
+            "sweeps": steps, "ms_per_sweep": mean, "ms_min": float(np.min(ms)),
+            "tflops": flops / (mean / 1000) / 1e12, "algorithmic_gbs": nbytes / (mean / 1000) / 1e9,
+            "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": nbytes,
+            "msg_updates_per_s": ctx.edges_number / (mean / 1000)}
 
 
 def run_svd_mode(args) -> None:
@@ -827,20 +852,25 @@ def run_mixed_mode(args) -> None:
     {2, 3, 5, 6}) at bond dim --chi: anneal until the bond dim saturates (at most 60 steps),
     then time --steps steps; per-kernel split by CUDA events.  --n sets the extra nodes and the
     grid side (sqrt(1.8 n)), the full mixed configuration being n = 50,000 (300 x 300)."""
+    print(json.dumps(mixed_measurement(args.n, args.chi, args.steps, args.warmup, bool(args.autotune))))
+
+
+def mixed_measurement(n: int, chi: int, n_steps: int, warmup: int, autotune: bool) -> dict:
+    """run_mixed_mode's measurement."""
     import torch
     from bqa_gb300 import instances
     from bqa_gb300.engine import Annealer
     from bqa_gb300.layout import build_context
-    side = max(4, int(round(np.sqrt(1.8 * args.n))))
-    ctx = build_context(instances.mixed_degree_job(rows=side, cols=side, extra=args.n, chi=args.chi))
+    side = max(4, int(round(np.sqrt(1.8 * n))))
+    ctx = build_context(instances.mixed_degree_job(rows=side, cols=side, extra=n, chi=chi))
     steps = [i for i in ctx.instructions if isinstance(i, dict)]
-    job = Annealer(ctx, autotune=bool(args.autotune))
+    job = Annealer(ctx, autotune=autotune)
     s, t0 = 0, time.perf_counter()
-    while job.bond_dim < args.chi and s < 60:
+    while job.bond_dim < chi and s < 60:
         job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
         s += 1
     prep = time.perf_counter() - t0
-    for i in range(args.warmup):
+    for i in range(warmup):
         job.run_layer(steps[s]["xtime"], steps[s]["ztime"])
         s += 1
     job.enable_kernel_timing(True)
@@ -849,7 +879,7 @@ def run_mixed_mode(args) -> None:
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("timed_steps")
     a.record()
-    for i in range(args.steps):
+    for i in range(n_steps):
         job.run_layer(steps[s + i]["xtime"], steps[s + i]["ztime"])
     b.record()
     torch.cuda.synchronize()
@@ -857,13 +887,16 @@ def run_mixed_mode(args) -> None:
     ms = a.elapsed_time(b)
     split: dict = {}
     for name, t, _, _ in job.kernel_times():
-        split[name] = round(split.get(name, 0.0) + t / args.steps, 2)
-    print(json.dumps({"mode": "mixed", "nodes": ctx.nodes_number, "classes": {int(d): L.batch_size for d, L in
-                      ctx.degree_to_layout.items()}, "chi": job.bond_dim, "prep_steps": s - args.warmup,
-                      "prep_s": round(prep, 1), "steps_per_s": args.steps / (ms / 1e3),
-                      "sweeps_per_step": float(np.mean([w["sweeps"] for w in job.stats])),
-                      "ms_per_step_split": split, "scratch_bytes": job.scratch_elems * 8,
-                      "autotune": ([job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off")}))
+        split[name] = round(split.get(name, 0.0) + t / n_steps, 2)
+    out = {"mode": "mixed", "nodes": ctx.nodes_number, "classes": {int(d): L.batch_size for d, L in
+           ctx.degree_to_layout.items()}, "chi": job.bond_dim, "prep_steps": s - warmup,
+           "prep_s": round(prep, 1), "steps_per_s": n_steps / (ms / 1e3),
+           "sweeps_per_step": float(np.mean([w["sweeps"] for w in job.stats])),
+           "ms_per_step_split": split, "scratch_bytes": job.scratch_elems * 8,
+           "autotune": ([job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off")}
+    del job
+    torch.cuda.empty_cache()
+    return out
 
 
 def main() -> None:
@@ -876,6 +909,8 @@ def main() -> None:
     ap.add_argument("--chi", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed", type=int, default=1, help="also time the mixed-precision form (1) or not (0)")
+    ap.add_argument("--secondary", type=int, default=1,
+                    help="also time the mixed-degree chi-4 job and a degree-4 chi-32 sweep (1) or not (0)")
     ap.add_argument("--serve-jobs", type=int, default=64,
                     help="jobs of the serving stream measured beside the anneal (0: none)")
     ap.add_argument("--autotune", type=int, default=1,

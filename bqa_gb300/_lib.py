@@ -9,7 +9,7 @@ from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libbqa_gb300.so"
-ABI_VERSION = 12
+ABI_VERSION = 13
 BQA_C64 = 0
 BQA_C128 = 1
 BQA_VARIANT_DEFAULT, BQA_VARIANT_TILED, BQA_VARIANT_GENERIC, BQA_VARIANT_TENSOR = 0, 1, 2, 3
@@ -62,6 +62,7 @@ class BqaLayerInfo(ctypes.Structure):
 # name -> (restype, argtypes); every exported symbol of the header
 SIGNATURES = {
     "bqa_abi_version": (c_int32, []),
+    "bqa_launch_count": (c_int64, []),
     "bqa_last_error": (ctypes.c_char_p, []),
     "bqa_max_bond_dim": (c_int32, [c_int32, c_int32]),
     "bqa_node_scratch_elems": (c_int64, [c_int32, c_int32, c_int32]),

@@ -1,4 +1,5 @@
 // Library-wide entry points of the C ABI: version, error text, size limits.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -12,6 +13,8 @@
 namespace bqa {
 
 static thread_local char g_last_error[512] = "";
+// kernel launches issued by this library (every launch is followed by check_launch)
+static std::atomic<long long> g_launches{0};
 
 int set_error(int code, const char* fmt, ...) {
     va_list ap;
@@ -22,6 +25,7 @@ int set_error(int code, const char* fmt, ...) {
 }
 
 int check_launch(const char* what) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(BQA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     return BQA_OK;
@@ -57,7 +61,9 @@ int ensure_smem(const void* kernel, size_t bytes, const char* what) {
 
 extern "C" {
 
-int32_t bqa_abi_version(void) { return 12; }
+int32_t bqa_abi_version(void) { return 13; }
+
+int64_t bqa_launch_count(void) { return bqa::g_launches.load(std::memory_order_relaxed); }
 
 const char* bqa_last_error(void) { return bqa::g_last_error; }
 

@@ -204,6 +204,10 @@ int32_t bqa_bp_end(bqa_job* job, const int32_t* loop_state /* host */, bqa_layer
 /* ABI version of this header (bumped on any signature change). */
 int32_t bqa_abi_version(void);
 
+/* Kernel launches this library has issued in the process so far, all threads together (a
+ * launch captured into a CUDA graph counts once, at capture; graph replays do not count). */
+int64_t bqa_launch_count(void);
+
 /*
  * Complex elements of scratch one CTA needs to process a class of degree `degree` at bond
  * dim chi (updates to dims <= chi) when its node tensors exceed shared memory, 0 when they

@@ -410,3 +410,17 @@ def test_merged_class_launch_bit_identical_to_per_class(tmp_path):
     for k in out["1"].files:
         assert np.array_equal(out["1"][k], out["0"][k]), k
         assert np.isfinite(out["1"][k]).all(), k
+
+
+def test_launch_count_counts_each_kernel_launch():
+    """bqa_launch_count grows by one per kernel the library launches: a densities pass of a
+    single-class job is one launch, a two-stage sweep of it two (half-node kernel + combine)."""
+    _, _, job = random_state("rr3_n16_chi4", 4, seed=2)
+    lib = job.lib
+    n0 = lib.dll.bqa_launch_count()
+    job.density_matrices()
+    assert lib.dll.bqa_launch_count() - n0 == 1
+    n1 = lib.dll.bqa_launch_count()
+    lib.call("bqa_bp_sweep_split", job._class_array(), len(job.classes), 4, job.dtype, _ptr(job.msgs[0]),
+             _ptr(job.msgs[1]), _ptr(job.lu), job.E, _ptr(job.dist_parts), None, job.stream)
+    assert lib.dll.bqa_launch_count() - n1 == 2
