@@ -163,7 +163,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_reference(steps: int, warmup: int, n_full: int, chi: int) -> dict:
+def cpu_reference(steps: int, warmup: int, n_full: int, chi: int, dtype=None) -> dict:
     """Time the oracle port of the reference algorithm on the bounded sample, in the same regime
     as the GPU arm: a SAMPLE_N-node instance of the benchmark generator is annealed from the
     start of the schedule until its bond dim reaches ``chi`` (untimed; it saturates at the same
@@ -174,7 +174,8 @@ def cpu_reference(steps: int, warmup: int, n_full: int, chi: int) -> dict:
     from bqa_gb300 import instances
     from oracle import bqa_oracle as orc
     _logging.getLogger("oracle.bqa_oracle").setLevel(_logging.ERROR)
-    octx = orc.make_context(instances.headline_gpu_job(n=SAMPLE_N, seed=0, chi=chi))
+    dtype = np.complex128 if dtype is None else dtype
+    octx = orc.make_context(instances.headline_gpu_job(n=SAMPLE_N, seed=0, chi=chi), dtype=dtype)
     st = orc.initialize_state(octx)
     sched = [i for i in octx.instructions if isinstance(i, dict)]
     t_prep = time.perf_counter()
@@ -210,13 +211,14 @@ def cpu_reference(steps: int, warmup: int, n_full: int, chi: int) -> dict:
         "value": sample_rate * scale,
         "unit": "steps/s",
         "cores": len(os.sched_getaffinity(0)),
+        "blas_threads": os.environ.get("OPENBLAS_NUM_THREADS", "library default"),
         "kind": "port",
         "scale": scale,
         "sweeps_per_step": sweeps / steps,
         "gate_layer_s_per_step": gate / steps,
         "bp_sweep_s": per_sweep,
         "bp_msg_updates_per_s": octx.edges_number / per_sweep,
-        "sample": (f"reference algorithm (numpy oracle port, complex128) on a {SAMPLE_N}-node instance of the "
+        "sample": (f"reference algorithm (numpy oracle port, {np.dtype(dtype).name}) on a {SAMPLE_N}-node instance of the "
                    f"same generator, annealed from step 0 until its bond dim reached {chi} (step {prep_steps}, "
                    f"{prep_s:.1f} s untimed), then {warmup} untimed and {steps} timed steps of the schedule: "
                    f"{gate + bp:.1f} s ({sample_rate:.3f} steps/s; gate layer {gate / steps:.3f} s/step, "
@@ -451,6 +453,10 @@ def run_gpu_arm(args) -> None:
     if cpu is not None:
         cpu["at_gpu_sweeps_per_step"] = {"sweeps_per_step": float(np.mean(sweeps)),
                                          "value": cpu_rate_at(cpu, float(np.mean(sweeps))), "unit": "steps/s"}
+        # the reference's BQA_PRECISION=single arithmetic, a shorter window (the FP32 ratio)
+        single = cpu_reference(min(args.steps, 5), 1, args.n, args.chi, dtype=np.complex64)
+        cpu["single"] = {k: single[k] for k in ("value", "unit", "sweeps_per_step", "gate_layer_s_per_step",
+                                                "bp_sweep_s", "sample")}
     n_el = ctx.nodes_number
     accuracy = measured_accuracy()
     # serving: a bounded Poisson stream of small jobs through the continuous-batching server
