@@ -472,7 +472,9 @@ def run_gpu_arm(args) -> None:
         torch.cuda.empty_cache()
         mx = mixed_measurement(50000, 4, 3, 2, True)
         sw = sweep_measurement(2000, 4, 32, "single", "default", 3, 1)
+        c1 = c1_job_measurement(not args.no_cpu_baseline)
         secondary = {
+            "c1_job": c1,
             "mixed_degree_chi4": {"what": "300x300 periodic grid + 50,000 nodes of degree 2/3/5/6 (140k nodes), bond "
                                           "dim 4, saturated steps, autotuned, device-timed",
                                   "steps_per_s": mx["steps_per_s"], "ms_per_step_split": mx["ms_per_step_split"],
@@ -543,6 +545,38 @@ def run_sweep_mode(args) -> None:
     which only the first sweep after a truncation sees).  Prints one JSON line."""
     print(json.dumps(sweep_measurement(args.n, args.degree, args.chi, args.precision, args.variant, args.steps,
                                        args.warmup)))
+
+
+def c1_job_measurement(with_cpu: bool) -> dict:
+    """The CPU-runnable configuration end to end: the 1000-qubit chi-4 job (random 3-regular,
+    J, h ~ N(0,1), 100 steps, bp_eps 1e-6) from config to result list through
+    bqa_gb300.run_qa (median of 3 after one untimed run), and through the oracle port of the
+    reference algorithm (complex128, one run on the host cores)."""
+    import logging as _logging
+    import torch
+    import bqa_gb300
+    from bqa_gb300 import instances
+    conf = instances.headline_cpu_job()
+    bqa_gb300.run_qa(dict(conf))
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        bqa_gb300.run_qa(dict(conf))
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    out = {"what": "1000-qubit random 3-regular job, chi 4, 100 steps, config to result list",
+           "gpu_run_qa_s": float(np.median(ts))}
+    if with_cpu:
+        from oracle import bqa_oracle as orc
+        level = _logging.getLogger("oracle.bqa_oracle").level
+        _logging.getLogger("oracle.bqa_oracle").setLevel(_logging.ERROR)
+        t0 = time.perf_counter()
+        orc.run_qa(dict(conf))
+        out["cpu_reference_port_s"] = time.perf_counter() - t0
+        _logging.getLogger("oracle.bqa_oracle").setLevel(level)
+        out["cpu_cores"] = len(os.sched_getaffinity(0))
+    return out
 
 
 def sweep_measurement(n: int, degree: int, chi: int, precision: str = "single", variant_name: str = "default",
@@ -916,7 +950,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed", type=int, default=1, help="also time the mixed-precision form (1) or not (0)")
     ap.add_argument("--secondary", type=int, default=1,
-                    help="also time the mixed-degree chi-4 job and a degree-4 chi-32 sweep (1) or not (0)")
+                    help="also time the 1000-qubit chi-4 job (GPU and CPU), the mixed-degree chi-4 job and a "
+                         "degree-4 chi-32 sweep (1) or not (0)")
     ap.add_argument("--serve-jobs", type=int, default=64,
                     help="jobs of the serving stream measured beside the anneal (0: none)")
     ap.add_argument("--autotune", type=int, default=1,
