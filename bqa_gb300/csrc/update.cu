@@ -16,6 +16,7 @@
 #include "common.cuh"
 #include "internal.h"
 #include "tiled_node.cuh"
+#include "tiled_d3c16.cuh"
 
 namespace bqa {
 
@@ -224,9 +225,10 @@ __global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int c
 // on bond 0, the Rz phase z_s folded in), runs the d bond products with the tiled GEMM of the
 // message kernels and writes z_s-weighted Y_s to tensor_out; apply_rx_norm_kernel then mixes the
 // two halves (Rx) and normalises each node.
-template <int D, int CHI>
+template <int D, int CHI, bool SPEC_IN>
 __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_apply_half_kernel(ApplyArgs<float> a) {
     using S = tiled::HalfShape<D, CHI>;
+    constexpr bool SPEC = SPEC_IN && D == 3 && CHI == 16;
     constexpr int PS = S::PER_S, N2 = S::N2, TH = S::THREADS, SW = S::SW, n = 2 * CHI;
     extern __shared__ double4 smem_raw[];
     float2* sX = reinterpret_cast<float2*>(smem_raw);
@@ -269,12 +271,24 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_apply
     }
     __syncthreads();
     float2* cur = sX;
-    float2* nxt = sY;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        tiled::product<D, CHI, TH, SW, 1>(cur, nxt, sW + k * N2, k);
+    if constexpr (SPEC) {
+        // the bond products with the closed-form addresses of the (3, 16) message kernel (the
+        // same operations in the same order as tiled::product): bond 0 in place, then 1 and 2
+        namespace q = tiled::d3c16;
+        q::prod0_inplace(sX, sW);
         __syncthreads();
-        float2* t = cur; cur = nxt; nxt = t;
+        q::prod1(sX, sY, sW + N2);
+        __syncthreads();
+        q::prod2(sY, sX, sW + 2 * N2);
+        __syncthreads();
+    } else {
+        float2* nxt = sY;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            tiled::product<D, CHI, TH, SW, 1>(cur, nxt, sW + k * N2, k);
+            __syncthreads();
+            float2* t = cur; cur = nxt; nxt = t;
+        }
     }
     float4* og = reinterpret_cast<float4*>(a.t_out + (size_t)node * 2 * PS + (size_t)s * PS);
     for (int i = threadIdx.x; i < PS / 2; i += TH) og[i] = *reinterpret_cast<const float4*>(cur + tiled::swz<SW>(2 * i));
@@ -298,13 +312,23 @@ __global__ void __launch_bounds__(256) apply_rx_norm_kernel(float2* t, int per_s
     for (int o = threadIdx.x; o < 2 * per_s; o += blockDim.x) tn[o] = c_scale(tn[o], inv);
 }
 
+// BQA_GB300_SPECIALIZED=0 at library load keeps the (3, 16) update on the generic addresses
+// too (the two give bit-identical tensors)
+static const bool g_apply_specialized = [] {
+    const char* v = getenv("BQA_GB300_SPECIALIZED");
+    return !(v && v[0] == '0');
+}();
+
 template <int D, int CHI>
 static int launch_apply_half(const ApplyArgs<float>& a, int count, cudaStream_t st) {
     using S = tiled::HalfShape<D, CHI>;
     const size_t smem = ((size_t)2 * S::PER_S + (size_t)D * S::N2 + 2 * D + 2) * sizeof(float2);
-    int rc = ensure_smem((const void*)tiled_apply_half_kernel<D, CHI>, smem, "tiled apply");
+    void (*kern)(ApplyArgs<float>) = tiled_apply_half_kernel<D, CHI, false>;
+    if constexpr (D == 3 && CHI == 16)
+        if (g_apply_specialized) kern = tiled_apply_half_kernel<D, CHI, true>;
+    int rc = ensure_smem((const void*)kern, smem, "tiled apply");
     if (rc) return rc;
-    tiled_apply_half_kernel<D, CHI><<<2 * count, S::THREADS, smem, st>>>(a);
+    kern<<<2 * count, S::THREADS, smem, st>>>(a);
     rc = check_launch("tiled apply");
     if (rc) return rc;
     apply_rx_norm_kernel<<<count, 256, 0, st>>>(a.t_out, S::PER_S, a.cx, a.sx);

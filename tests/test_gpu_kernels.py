@@ -316,13 +316,23 @@ msgs = job.msgs[1][: job.E * 256].cpu().numpy()
 job.lib.call("bqa_ext_msgs_split", job._class_array(), len(job.classes), 16, job.dtype, _ptr(job.msgs[0]),
              _ptr(job.lu), job.E, _ptr(job.edge_j), 0.37, _ptr(job.ext), job.stream)
 ext = job.ext[: job.E * 1024].cpu().numpy()
-np.savez(sys.argv[1], msgs=msgs, ext=ext)
+import torch
+rng = np.random.default_rng(5)
+n, E = 32, job.E
+can = (rng.normal(size=(E, n, n)) + 1j * rng.normal(size=(E, n, n))).astype(np.complex64)
+lam = np.ascontiguousarray(np.sort(rng.uniform(0.05, 1.0, size=(E // 2, n)), axis=1)[:, ::-1].astype(np.float32))
+job.ext[: can.size].copy_(torch.from_numpy(can.reshape(-1)))
+job.lmbds[: lam.size].copy_(torch.from_numpy(lam.reshape(-1)))
+job.lib.call("bqa_apply_update", job._class_array(out=True), len(job.classes), 16, 16, job.dtype, _ptr(job.ext),
+             _ptr(job.lmbds), n, 0.13, 0.41, job.stream)
+upd = job.classes[0].tensors[1][: job.classes[0].count * 2 * 4096].cpu().numpy()
+np.savez(sys.argv[1], msgs=msgs, ext=ext, upd=upd)
 """
 
 
 def test_specialised_half_kernel_bit_identical_to_generic(tmp_path):
-    """The (3, 16) CUDA-core half-node kernel with closed-form addresses gives the generic
-    kernel's bits (both with the tensor-core kernel switched off)."""
+    """The (3, 16) CUDA-core half-node kernel and tensor update with closed-form addresses give
+    the generic kernels' bits (with the tensor-core kernel switched off)."""
     import os
     import subprocess
     import sys
@@ -336,7 +346,8 @@ def test_specialised_half_kernel_bit_identical_to_generic(tmp_path):
         out[flag] = np.load(f)
     assert np.array_equal(out["1"]["msgs"], out["0"]["msgs"])
     assert np.array_equal(out["1"]["ext"], out["0"]["ext"])
-    assert np.abs(out["1"]["msgs"]).max() > 0
+    assert np.array_equal(out["1"]["upd"], out["0"]["upd"])
+    assert np.abs(out["1"]["msgs"]).max() > 0 and np.abs(out["1"]["upd"]).max() > 0
 
 
 def test_fp32_fma_probe_runs():
