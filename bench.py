@@ -462,7 +462,9 @@ def run_gpu_arm(args) -> None:
     # serving: a bounded Poisson stream of small jobs through the continuous-batching server
     serving = None
     if args.serve_jobs > 0:
-        serving = {"stream": SERVING_STREAM, **serving_measurement(args.serve_jobs, args.rate)}
+        wide = args.serve_stream == "wide"
+        serving = {"stream": SERVING_STREAM_WIDE if wide else SERVING_STREAM,
+                   **serving_measurement(args.serve_jobs, args.rate, wide=wide)}
     # the other configurations' shapes, short: the mixed-degree job at bond dim 4 (every node in
     # shared memory) and the degree-4 bond-dim-32 sweep (global-memory kernels)
     tuned = [job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off"
@@ -703,10 +705,11 @@ def run_svd_mode(args) -> None:
     print(json.dumps(out))
 
 
-def serving_stream(jobs: int, rate: float, seed: int = 0):
+def serving_stream(jobs: int, rate: float, seed: int = 0, wide: bool = False):
     """Poisson stream of annealing jobs (arrival time, config): random d-regular graphs with
-    n log-uniform in [100, 20000], d in {3, 4}, J = +-1, h ~ N(0, 0.5), bond dim in {4, 8},
-    20 or 50 steps over T = steps / 10."""
+    n log-uniform in [100, 20000], J = +-1, h ~ N(0, 0.5), 20 or 50 steps over T = steps / 10;
+    d in {3, 4} and bond dim in {4, 8}, or (wide) d in {3, 4, 5} and bond dim in {4, 8, 16} with
+    n capped at 4,000 for bond dim 16 and degree 5 kept at bond dims 4 and 8."""
     from bqa_gb300 import instances
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -714,9 +717,11 @@ def serving_stream(jobs: int, rate: float, seed: int = 0):
     for k in range(jobs):
         t += rng.exponential(1.0 / rate)
         n = int(np.exp(rng.uniform(np.log(100), np.log(20000))))
-        d = int(rng.choice([3, 4]))
+        d = int(rng.choice([3, 4, 5] if wide else [3, 4]))
+        chi = int(rng.choice(([4, 8] if d == 5 else [4, 8, 16]) if wide else [4, 8]))
+        if chi == 16:
+            n = min(n, 4000)
         n += (n * d) % 2
-        chi = int(rng.choice([4, 8]))
         steps = int(rng.choice([20, 50]))
         e = instances.random_regular_edges(n, d, seed * 100003 + k)
         conf = instances.qubo_config(e, 2.0 * rng.integers(0, 2, len(e)) - 1, rng.normal(0, 0.5, n),
@@ -727,9 +732,11 @@ def serving_stream(jobs: int, rate: float, seed: int = 0):
 
 
 SERVING_STREAM = "random d-regular, d in {3,4}, n log-uniform in [100, 20000], chi in {4, 8}, 20 or 50 steps"
+SERVING_STREAM_WIDE = ("random d-regular, d in {3,4,5}, n log-uniform in [100, 20000] (at most 4,000 at chi 16), "
+                       "chi in {4, 8, 16} (4 or 8 at degree 5), 20 or 50 steps")
 
 
-def serving_measurement(jobs: int, rate: float, seed: int = 1) -> dict:
+def serving_measurement(jobs: int, rate: float, seed: int = 1, wide: bool = False) -> dict:
     """p50/p99 job latency and jobs/s of one Poisson job stream through the continuous-batching
     server with packed BP runs (the jobs waiting for BP swept in shared launches), through the
     server with each job's BP run in its own launches, and with the same jobs run one at a time
@@ -756,7 +763,7 @@ def serving_measurement(jobs: int, rate: float, seed: int = 1) -> dict:
         torch.cuda.synchronize()
         return out
 
-    stream = serving_stream(jobs, rate, seed=seed)
+    stream = serving_stream(jobs, rate, seed=seed, wide=wide)
     bqa_gb300.run_qa(dict(stream[0][1]))              # warm-up: compile paths and allocator
     torch.cuda.synchronize()
 
@@ -791,8 +798,10 @@ def serving_measurement(jobs: int, rate: float, seed: int = 1) -> dict:
 def run_serve_mode(args) -> None:
     """serving_measurement for every rate in --rates (or --rate)."""
     rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
-    results = [serving_measurement(args.jobs, rate) for rate in rates]
-    print(json.dumps({"mode": "serve", "jobs": args.jobs, "stream": SERVING_STREAM, "rates": results}))
+    wide = args.serve_stream == "wide"
+    results = [serving_measurement(args.jobs, rate, wide=wide) for rate in rates]
+    print(json.dumps({"mode": "serve", "jobs": args.jobs, "stream": SERVING_STREAM_WIDE if wide else SERVING_STREAM,
+                      "rates": results}))
 
 
 def run_layout_mode(args) -> None:
@@ -961,6 +970,8 @@ def main() -> None:
     ap.add_argument("--rate", type=float, default=200.0,
                     help="serving stream arrival rate (jobs/s); the default is the top of the stated 1-200 sweep")
     ap.add_argument("--rates", default="", help="serve mode: comma-separated arrival rates (jobs/s)")
+    ap.add_argument("--serve-stream", default="small", choices=["small", "wide"],
+                    help="serving job mix: degrees 3-4 at bond dims 4/8 (small) or degrees 3-5 at bond dims 4/8/16")
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     ap.add_argument("--degree", type=int, default=3, help="sweep mode: degree of the random regular graph")
     ap.add_argument("--variant", default="default",

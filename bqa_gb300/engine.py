@@ -241,11 +241,13 @@ class Annealer:
         self.torch.cuda.synchronize(self.device)
         return [(n, a.elapsed_time(b), f, by) for n, a, b, f, by in self._events]
 
-    def bp_sweep_cost(self) -> tuple[float, float]:
-        """Algorithmic (flops, bytes) of one BP sweep at the current bond dim: per node of degree
-        d, 2 d^2 chi^(d+1) complex MACs (d messages, each d-1 mode products and one closing
-        contraction), and the tensor read once plus d messages read and d written."""
-        chi, el = self.chi, (8 if self.precision == "single" else 16)
+    def bp_sweep_cost(self, chi: int | None = None) -> tuple[float, float]:
+        """Algorithmic (flops, bytes) of one BP sweep at bond dim ``chi`` (the current one by
+        default): per node of degree d, 2 d^2 chi^(d+1) complex MACs (d messages, each d-1 mode
+        products and one closing contraction), and the tensor read once plus d messages read and d
+        written."""
+        chi = self.chi if chi is None else chi
+        el = 8 if self.precision == "single" else 16
         f = b = 0.0
         for c in self.classes:
             if c.degree == 0:
@@ -486,16 +488,18 @@ class Annealer:
         return self._adopt(j, res)
 
     def run_layer_packed(self, xtime: float, ztime: float, packer) -> dict:
-        """One step whose BP run is swept together with other jobs' (``packer``, a
-        ``serve.BpPacker``): the gate layer through bqa_gate_layer on this job's stream, then
-        the BP run in the packer's shared launches.  The state afterwards is the same bits as
-        after ``run_layer``."""
+        """One step whose BP run is swept together with other jobs' (``packer``: a
+        ``serve.BpPacker``, or a function from the sweep's FLOPs at the new bond dim to one): the
+        gate layer through bqa_gate_layer on this job's stream, then the BP run in the packer's
+        shared launches.  The state afterwards is the same bits as after ``run_layer``."""
         if self.ctx.max_bp_iters_number < 1:
             raise ValueError("max_bp_iter_number must be >= 1 to run belief propagation")
         j, cls = self._job_struct()
         res = _lib.BqaLayerInfo()
         self.lib.call("bqa_gate_layer", ctypes.byref(j), xtime, ztime, ctypes.byref(res), self.stream)
         self.torch.cuda.current_stream(self.device).synchronize()
+        if not hasattr(packer, "run_bp"):
+            packer = packer(self.bp_sweep_cost(int(j.chi))[0])
         packer.run_bp(j, res)
         return self._adopt(j, res)
 

@@ -9,11 +9,13 @@ the kernels of concurrent jobs overlap on the device while every job keeps its o
 state (tensors, messages, scratch).  A job's footprint is released when it finishes.
 
 BP runs are packed (``pack_bp=True``, the default): after its gate layer a job hands its BP
-run to the server's ``BpPacker``, which sweeps the runs of all the jobs waiting at that
-moment in shared launches -- each node kernel once per sweep for the degree classes of every
-job that uses it, one combine and one decision kernel for all of them (bqa_bp_packed) --
-takes each job out when its own loop state says done and lets newly waiting jobs join
-between sweep groups.
+run to a ``BpPacker``, which sweeps the runs of all the jobs waiting at that moment in shared
+launches -- each node kernel once per sweep for the degree classes of every job that uses it,
+one combine and one decision kernel for all of them (bqa_bp_packed) -- takes each job out when
+its own loop state says done and lets newly waiting jobs join between sweep groups.  Jobs are
+packed only with jobs of about the same sweep cost (one packer, thread and stream per factor-4
+band of a sweep's FLOPs), so a small job never waits on a large job's sweeps; the bands' packs
+run concurrently.
 
 Results are the ``run_qa`` result lists; ``stats()`` reports per-job latency (arrival to
 result) percentiles and the throughput of the whole stream.  A job's result is the same
@@ -243,7 +245,9 @@ class JobServer:
         self.peak_active = 0
         self.peak_bytes = 0
         self._t0 = time.perf_counter()
-        self.packer = BpPacker(self.device) if pack_bp and self.device.type == "cuda" else None
+        self.pack_bp = bool(pack_bp) and self.device.type == "cuda"
+        self._packers: dict[int, BpPacker] = {}
+        self._packers_lock = threading.Lock()
 
     # ---- submission --------------------------------------------------------------------
     def now(self) -> float:
@@ -272,8 +276,8 @@ class JobServer:
                 out = []
                 for ins in job.ctx.instructions:
                     if isinstance(ins, dict):
-                        if self.packer is not None:
-                            annealer.run_layer_packed(ins["xtime"], ins["ztime"], self.packer)
+                        if self.pack_bp:
+                            annealer.run_layer_packed(ins["xtime"], ins["ztime"], self.packer_for)
                         else:
                             annealer.run_layer(ins["xtime"], ins["ztime"])
                     elif ins == cfg.MEASURE:
@@ -337,12 +341,29 @@ class JobServer:
                "mean_s": float(lat.mean()), "jobs_per_s": len(jobs) / span if span > 0 else None,
                "steps": int(sum(sum(isinstance(i, dict) for i in j.ctx.instructions) for j in jobs)),
                "peak_active": self.peak_active, "peak_bytes": self.peak_bytes}
-        if self.packer is not None:
-            out["bp_packing"] = self.packer.stats()
+        if self._packers:
+            per = {band: p.stats() for band, p in sorted(self._packers.items())}
+            calls = sum(v["packed_calls"] for v in per.values())
+            runs = sum(v["mean_runs_per_call"] * v["packed_calls"] for v in per.values())
+            out["bp_packing"] = {"packed_calls": calls,
+                                 "sweeps_per_call": next(iter(per.values()))["sweeps_per_call"],
+                                 "mean_runs_per_call": runs / calls if calls else 0.0,
+                                 "max_runs_per_call": max(v["max_runs_per_call"] for v in per.values()),
+                                 "bands": len(per)}
         return out
 
     def close(self) -> None:
-        """Stop the BP packer's thread (the server takes no jobs afterwards)."""
-        if self.packer is not None:
-            self.packer.close()
-            self.packer = None
+        """Stop the BP packers' threads (the server takes no jobs afterwards)."""
+        with self._packers_lock:
+            packers, self._packers = list(self._packers.values()), {}
+        for p in packers:
+            p.close()
+
+    def packer_for(self, sweep_flops: float) -> "BpPacker":
+        """The packer of the factor-4 band of a sweep's FLOPs (created on first use)."""
+        band = int(np.log2(max(sweep_flops, 1.0)) // 2)
+        with self._packers_lock:
+            p = self._packers.get(band)
+            if p is None:
+                p = self._packers[band] = BpPacker(self.device)
+            return p
