@@ -362,17 +362,22 @@ __global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>
     if constexpr (QR) qr_apply_q<W, R>(sV, sH, sTau, lane);
     const bool keep = sig > eps;
     const R sq = sqrt(sig);
-    if (!live || lane >= n) return;
-    // row `lane` of lu = sqrt(sigma) conj(v)^T ; column `lane` of ul = v / sqrt(sigma)
     const R sqk = keep ? sq : R(0);
     const R inv = keep ? R(1) / sq : R(0);
+    // row k of lu = sqrt(sigma_k) conj(v_k)^T, v_k = column k of V: written a row at a time, the
+    // lanes along the row (coalesced); column `lane` of ul = v / sqrt(sigma)
 #pragma unroll
     for (int k = 0; k < W; ++k) {
-        if (k < n) {
-            lu[base + (size_t)lane * n + k] = c_make(sqk * v[k].x, -sqk * v[k].y);
-            ul[base + (size_t)k * n + lane] = c_scale(v[k], inv);
+        const R sk = __shfl_sync(BQA_FULL_MASK, sqk, k, W);
+        if (live && k < n && lane < n) {
+            const C vk = sV[k * VS + lane];
+            lu[base + (size_t)k * n + lane] = c_make(sk * vk.x, -sk * vk.y);
         }
     }
+    if (!live || lane >= n) return;
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+        if (k < n) ul[base + (size_t)k * n + lane] = c_scale(v[k], inv);
 }
 
 // Per undirected edge p: ker = lu[p] lu[p+h]^T = us s vhs; lambdas; canonicalisers
