@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(128, 4) env_factor_kernel(const typename Cx<R>
     using C = typename Cx<R>::T;
     constexpr int VS = VStride<W>::VS;
     constexpr int BLOCK = QR ? QrStride<W>::BLOCK : VStride<W>::BLOCK;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     const int lane = threadIdx.x & (W - 1);
     C* sV = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / W) * BLOCK;
     C* sH = sV + VStride<W>::BLOCK;
@@ -395,7 +395,7 @@ __global__ void __launch_bounds__(128, 4) bond_canon_kernel(const typename Cx<R>
                                                          int32_t* status) {
     static_assert(!QR || QrStride<W>::H + W <= W * W, "Householder vectors fit the staging block");
     using C = typename Cx<R>::T;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     constexpr int VS = VStride<W>::VS;
     const int lane = threadIdx.x & (W - 1);
     const int seg = threadIdx.x / W;
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(32) env_factor_wide_kernel(const typename Cx<R
                                                              typename Cx<R>::T* __restrict__ ul, int32_t* status) {
     using C = typename Cx<R>::T;
     constexpr int NS = kWideNS;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     C* A = reinterpret_cast<C*>(smem_raw);
     C* V = A + kWide * NS;
     R* nrm = reinterpret_cast<R*>(V + kWide * NS);
@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(32) bond_canon_wide_kernel(const typename Cx<R
                                                              int32_t* status) {
     using C = typename Cx<R>::T;
     constexpr int NS = kWideNS;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     C* A = reinterpret_cast<C*>(smem_raw);
     C* V = A + kWide * NS;
     R* nrm = reinterpret_cast<R*>(V + kWide * NS);

@@ -283,7 +283,7 @@ __device__ __forceinline__ void write_outputs(const NodeArgs<R>& a, int node, in
 template <int CM, int MODE, typename R>
 __device__ __forceinline__ void node_body(const NodeArgs<R>& a, int node) {
     using C = typename Cx<R>::T;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     const int d = a.d, chi = a.chi, n2 = chi * chi;
     const int per_s = ipow(chi, d);
@@ -586,7 +586,7 @@ __device__ __forceinline__ void apply_messages(const C* __restrict__ T, C* W, co
 template <int CM, int MODE, typename R>
 __global__ void __launch_bounds__(256) node_kernel_global(NodeArgs<R> a, int count, typename Cx<R>::T* scratch) {
     using C = typename Cx<R>::T;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     const int d = a.d, chi = a.chi, n2 = chi * chi;
     const int per_s = ipow(chi, d);
@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(tiled::Shape<D, CHI>::THREADS) tiled_node_kern
     static_assert(D >= 2 && D <= 4, "tiled kernel schedules cover degrees 2..4");
     static_assert(S::CLOSE_TILES <= S::THREADS, "close tiles exceed the block");
     constexpr int NT = S::NT, N2 = S::N2, PER_S = S::PER_S, TH = S::THREADS, SW = S::SW;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     float2* sT = reinterpret_cast<float2*>(smem_raw);
     float2* sA = sT + NT;
     float2* sB = sA + NT;
@@ -862,7 +862,7 @@ __device__ __forceinline__ void tiled_half_body(const NodeArgs<float>& a, int no
                   "specialised half kernel is built for degree 3, bond dim 16");
     static_assert(S::CLOSE_TILES <= S::THREADS, "close tiles exceed the block");
     constexpr int PS = S::PER_S, N2 = S::N2, TH = S::THREADS, SW = S::SW;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     float2* sT = reinterpret_cast<float2*>(smem_raw);
     float2* sA = sT + PS;
     float2* sB = sA + PS;
@@ -1028,7 +1028,7 @@ static int launch_half_packed(const PackEntry* e, int n, cudaStream_t st) {
 // diagonal applies them as bond scalings on the CUDA cores, as the other half-node kernels do.
 __global__ void __launch_bounds__(tcd3::TH, 2) tc_half_kernel_d3c16(NodeArgs<float> a) {
     constexpr int CHI = 16, D = 3, N2 = CHI * CHI, PS = CHI * CHI * CHI, TH = tcd3::TH;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     float2* region = reinterpret_cast<float2*>(smem_raw);
     float2* sMt = region + tcd3::REGION / 8;
     float2* sP = sMt + D * N2;
@@ -1161,7 +1161,7 @@ __global__ void __launch_bounds__(tcd3::TH, 2) tc_half_kernel_d3c16(NodeArgs<flo
 template <bool MIXED>
 __global__ void __launch_bounds__(tcb::TH, 2) tcb_half_kernel_d3c16(NodeArgs<float> a, float switch_dist, int halves) {
     constexpr int CHI = 16, D = 3, N2 = CHI * CHI, PS = CHI * CHI * CHI, TH = tcb::TH;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     unsigned char* reg = reinterpret_cast<unsigned char*>(smem_raw);
     float2* const V1 = reinterpret_cast<float2*>(reg);   // FP32 buffers of the bond-scaling path
     float2* const V2 = V1 + PS;

@@ -89,7 +89,7 @@ __device__ __forceinline__ void node_coefficients(const ApplyArgs<R>& a, int nod
 template <int CM, typename R>
 __global__ void __launch_bounds__(256) apply_kernel(ApplyArgs<R> a) {
     using C = typename Cx<R>::T;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     C* sm = reinterpret_cast<C*>(smem_raw);
     const int d = a.d, chi = a.chi, dim = a.dim, n = 2 * chi;
     const int m = chi > dim ? chi : dim;
@@ -161,7 +161,7 @@ size_t apply_smem_bytes(int d, int chi, size_t elem_bytes) { return apply_smem_e
 template <int CM, typename R>
 __global__ void __launch_bounds__(256) apply_kernel_global(ApplyArgs<R> a, int count, typename Cx<R>::T* scratch) {
     using C = typename Cx<R>::T;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     C* sW = reinterpret_cast<C*>(smem_raw);
     const int d = a.d, chi = a.chi, dim = a.dim, n = 2 * chi;
     const int m = chi > dim ? chi : dim;
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(tiled::HalfShape<D, CHI>::THREADS) tiled_apply
     using S = tiled::HalfShape<D, CHI>;
     constexpr bool SPEC = SPEC_IN && D == 3 && CHI == 16;
     constexpr int PS = S::PER_S, N2 = S::N2, TH = S::THREADS, SW = S::SW, n = 2 * CHI;
-    extern __shared__ double4 smem_raw[];
+    extern __shared__ double4_32a smem_raw[];
     float2* sX = reinterpret_cast<float2*>(smem_raw);
     float2* sY = sX + PS;
     float2* sW = sY + PS;           // D blocks of [j][c], CHI x CHI
