@@ -21,6 +21,7 @@
 #include "tiled_d3c16.cuh"
 #include "tc_d3c16.cuh"
 #include "tc_bf16_d3c16.cuh"
+#include "tc_f16x2_d3c16.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -1294,6 +1295,151 @@ __global__ void __launch_bounds__(tcb::TH, 2) tcb_half_kernel_d3c16(NodeArgs<flo
     }
 }
 
+// Half-node kernel of degree 3, bond dim 16 with 2xFP16 tensor-core bond products (FP32
+// accuracy, tc_f16x2_d3c16.cuh) and the closing contractions on the CUDA cores (warps 0-4, the
+// previous block copied out by warps 5-7).  Diagonal incoming messages take the FP32
+// bond-scaling path.  Same outputs as the other half-node kernels (blocks P_s into pm).
+//
+// Grid-stride: at most two CTAs per SM walk the `halves` half-nodes; tensor memory is
+// allocated once per CTA and the mbarrier runs one phase per half-node with MMAs.
+__global__ void __launch_bounds__(tch::TH, 2) tch_half_kernel_d3c16(NodeArgs<float> a, int halves) {
+    constexpr int CHI = 16, D = 3, N2 = CHI * CHI, PS = CHI * CHI * CHI, TH = tch::TH;
+    extern __shared__ double4_32a smem_raw[];
+    unsigned char* reg = reinterpret_cast<unsigned char*>(smem_raw);
+    float2* const region = reinterpret_cast<float2*>(smem_raw);
+    float2* const V1 = region + tcd3::X_V1;
+    float2* const V2 = region + tcd3::X_V2;
+    float2* const V0 = region + tcd3::X_V0;
+    float2* const sP = region + tch::SP;
+    float2* const sMt = region + tch::SMT;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reg + tch::REGION);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+    uint32_t* wmax = slot + 1;   // [warp][|T|, |M_0|, |M_1|, |M_2|]
+    const float2* msgs_in = a.msgs_a;
+    if (a.loop_state != nullptr) {
+        if (a.loop_state[0]) return;
+        if (a.loop_state[2]) msgs_in = a.msgs_b;
+    }
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    if (t == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_mbar_init();
+    }
+    const uint32_t rb = tc::smem_u32(reg);
+    uint32_t tmem = 0, parity = 0;
+    bool tmem_held = false;
+    namespace q = tiled::d3c16;
+    constexpr int CT = 160;
+    for (int h = blockIdx.x; h < halves; h += gridDim.x) {
+        const int node = h >> 1, s = h & 1;
+        float4 tv[8];
+        tcd3::load_share(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS, tv);
+        // thread t holds entry (y, x) = (t >> 4, t & 15) of each incoming message
+        float2 mv[3];
+        int offdiag = 0;
+        uint32_t mm[3];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            mv[k] = msgs_in[(size_t)a.in_pos[node * D + k] * N2 + t];
+            offdiag |= ((t >> 4) != (t & 15)) && (mv[k].x != 0.f || mv[k].y != 0.f);
+            mm[k] = __reduce_max_sync(0xffffffffu, max(tch::mag(mv[k].x), tch::mag(mv[k].y)));
+        }
+        uint32_t mt = 0;
+#pragma unroll
+        for (int m = 0; m < 8; ++m)
+            mt = max(mt, max(max(tch::mag(tv[m].x), tch::mag(tv[m].y)), max(tch::mag(tv[m].z), tch::mag(tv[m].w))));
+        mt = __reduce_max_sync(0xffffffffu, mt);
+        if (lane == 0) {
+            wmax[4 * warp] = mt;
+#pragma unroll
+            for (int k = 0; k < D; ++k) wmax[4 * warp + 1 + k] = mm[k];
+        }
+        const bool diag = !__syncthreads_or(offdiag);
+        if (!diag) {
+            uint32_t gm[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (int w = 0; w < TH / 32; ++w)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) gm[i] = max(gm[i], wmax[4 * w + i]);
+            const int kt = tch::scale_exp(gm[0]);
+            const int km[3] = {tch::scale_exp(gm[1]), tch::scale_exp(gm[2]), tch::scale_exp(gm[3])};
+            if (!tmem_held) {
+                if (warp == 0) {
+                    tc::alloc(slot, tch::TMEM_COLS);
+                    tc::relinquish();
+                }
+                tc::fence_before();
+                __syncthreads();
+                tc::fence_after();
+                tmem = *slot;
+                tmem_held = true;
+            }
+            const float sm[3] = {tch::pow2(km[0]), tch::pow2(km[1]), tch::pow2(km[2])};
+            tch::store_b(mv, sm, reg);
+            tch::store_a(tv, tch::pow2(kt), reg);
+            tc::fence_proxy_async();
+            tc::fence_before();
+            __syncthreads();
+            tc::fence_after();
+            if (t == 0) {
+                tch::issue_products(tmem, rb);
+                tc::commit(bar);
+            }
+            const bool ok = tc::mbar_wait(bar, parity, tch::WAIT_CYCLES);
+            parity ^= 1;
+            if (__syncthreads_or(!ok)) {
+                // the MMAs did not complete in time: count the fault, give them one more bounded
+                // wait and stop this CTA (its remaining blocks stay unwritten)
+                if (t == 0) atomicAdd(&g_tc_faults, 1);
+                tc::mbar_wait(bar, parity ^ 1, tch::WAIT_CYCLES);
+                break;
+            }
+            tc::fence_after();
+            // V_2, V_1, V_0 carry 2^(kt + km[2]), 2^(kt + km[1]), 2^(kt + km[0])
+            const float sc[3][2] = {{tch::pow2(-kt), tch::pow2(-km[2])},
+                                    {tch::pow2(-kt), tch::pow2(-km[1])},
+                                    {tch::pow2(-kt), tch::pow2(-km[0])}};
+            tcd3::epilogue<true>(tmem, region, sc);
+            tc::fence_before();
+            __syncthreads();
+        } else {
+            // all incoming messages diagonal: bond scalings in FP32 (sMt[k][16 x + y] = M_k[y][x])
+#pragma unroll
+            for (int k = 0; k < D; ++k) sMt[k * N2 + 16 * (t & 15) + (t >> 4)] = mv[k];
+            tcd3::store_share_swizzled(tv, V0);
+            __syncthreads();
+            tiled::diag_scale3<CHI, TH, 7>(V0, V1, sMt + N2, 1);
+            tiled::diag_scale3<CHI, TH, 7>(V0, V2, sMt + 2 * N2, 2);
+            __syncthreads();
+            tiled::diag_scale3<CHI, TH, 7>(V0, V0, sMt, 0);
+            __syncthreads();
+        }
+        float2* const sPb[2] = {sP, sP + N2};
+        int pend = -1, cur = 0;
+        auto out_block = [&](int idx) {
+            return reinterpret_cast<float4*>(a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2);
+        };
+        auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
+            constexpr int IDX = decltype(idx_tag)::value;
+            if (t < CT) q::close<IDX>(X, R, sPb[cur]);
+            else if (pend >= 0) tiled::write_half_block<CHI>(sPb[cur ^ 1], out_block(pend), t - CT, TH - CT);
+            __syncthreads();
+            pend = IDX;
+            cur ^= 1;
+        };
+        emit_s(std::integral_constant<int, 0>{}, V1, V2);
+        emit_s(std::integral_constant<int, 2>{}, V0, V1);
+        emit_s(std::integral_constant<int, 1>{}, V0, V2);
+        tiled::write_half_block<CHI>(sPb[cur ^ 1], out_block(pend), t, TH);
+        __syncthreads();
+    }
+    if (tmem_held) {
+        tc::fence_before();
+        __syncthreads();
+        if (warp == 0) tc::dealloc(tmem, tch::TMEM_COLS);
+    }
+}
+
 // BP distance above which the mixed-precision (3, 16) kernel takes its BF16 path; the
 // environment variable BQA_GB300_MIXED_SWITCH overrides it when the library loads.
 static const float g_mixed_switch = [] {
@@ -1326,8 +1472,25 @@ static int launch_tcb_half(const NodeArgs<float>& args, int count, cudaStream_t 
     return check_launch("bf16 tensor-core half kernel");
 }
 
+static int launch_tch_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    const size_t smem = (size_t)tch::REGION + tch::SCRATCH;
+    int rc = ensure_smem((const void*)tch_half_kernel_d3c16, smem, "2xFP16 tensor-core half kernel");
+    if (rc) return rc;
+    const int halves = 2 * count;
+    tch_half_kernel_d3c16<<<std::min(halves, 2 * sm_count()), tch::TH, smem, st>>>(args, halves);
+    return check_launch("2xFP16 tensor-core half kernel");
+}
+
+// The FP32-accurate tensor-core kernel: 2xFP16 products (one tensor-core round trip per
+// half-node), or 3xTF32 products when BQA_GB300_TC_TF32=1 is set when the library loads.
+static const bool g_tc_tf32 = [] {
+    const char* v = getenv("BQA_GB300_TC_TF32");
+    return v && v[0] == '1';
+}();
+
 static int launch_tc_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
     if (pack_record(launch_solo_f32<launch_tc_half>, 0, 0, count, args)) return BQA_OK;
+    if (!g_tc_tf32) return launch_tch_half(args, count, st);
     const size_t smem = (size_t)tcd3::REGION + (3 + 2) * 256 * sizeof(float2) + 16;
     int rc = ensure_smem((const void*)tc_half_kernel_d3c16, smem, "tensor-core half kernel");
     if (rc) return rc;

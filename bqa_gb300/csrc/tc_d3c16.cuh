@@ -165,9 +165,19 @@ __device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint3
     }
 }
 
+// f *= s[0] * s[1] on 32 accumulator words (each factor applied in turn)
+__device__ __forceinline__ void scale32(uint32_t (&f)[32], const float (&s)[2]) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) f[i] = __float_as_uint(__uint_as_float(f[i]) * s[0] * s[1]);
+}
+
 // Epilogue of one warp: its 32 rows (quarter w % 4 of row tile w / 4) of the three products,
-// from tensor memory into the swizzled close buffers of the region.
-__device__ __forceinline__ void epilogue(uint32_t tmem, float2* __restrict__ region) {
+// from tensor memory into the swizzled close buffers of the region.  SCALED: the accumulators
+// of V_2, V_1, V_0 are multiplied by sc[0][0] sc[0][1], sc[1][0] sc[1][1], sc[2][0] sc[2][1]
+// (powers of two that undo the operand scaling of the FP16 products; two factors so that the
+// product may leave the float exponent range while each factor stays in it).
+template <bool SCALED = false>
+__device__ __forceinline__ void epilogue(uint32_t tmem, float2* __restrict__ region, const float (&sc)[3][2] = {}) {
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int j = w >> 2, qd = w & 3;
     const int r = 128 * j + 32 * qd + lane;
@@ -176,6 +186,7 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, float2* __restrict__ reg
     {   // V_2: r = 16 a + b, columns y -> V_2[a][b][y]
         tc::ld_32x32b_x32(tl + COL_V2, f);
         tc::wait_ld();
+        if (SCALED) scale32(f, sc[0]);
         const int a = r >> 4, b = r & 15;
         float2* row = region + X_V2 + a * 256 + b * 16;
 #pragma unroll
@@ -187,6 +198,7 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, float2* __restrict__ reg
     {   // V_1: r = 16 a + c, columns y (new b) -> V_1[a][y][c]
         tc::ld_32x32b_x32(tl + COL_V1, f);
         tc::wait_ld();
+        if (SCALED) scale32(f, sc[1]);
         const int a = r >> 4, c = r & 15;
         float2* base = region + X_V1 + a * 256;
 #pragma unroll
@@ -196,6 +208,7 @@ __device__ __forceinline__ void epilogue(uint32_t tmem, float2* __restrict__ reg
     {   // V_0: r = 16 b + c, columns y (new a) -> V_0[y][b][c]
         tc::ld_32x32b_x32(tl + COL_V0, f);
         tc::wait_ld();
+        if (SCALED) scale32(f, sc[2]);
         const int b = r >> 4, c = r & 15;
         float2* base = region + X_V0 + b * 16 + (c ^ ((b & 7) << 1));
 #pragma unroll
