@@ -51,9 +51,13 @@ SAMPLE_N = 200
 # only the NG (NG + 1) / 2 upper 4x4 tiles of its NG x NG tile grid (NG = chi / 4).
 EXECUTED_FRACTION = {c: (3 + 3 * ((c // 4) * (c // 4 + 1) / 2) / (c // 4) ** 2) / 9 for c in (4, 8, 12, 16)}
 
-# DRAM bytes one chi-16 degree-3 BP sweep moves per node: ncu capture of a 10k-node sweep,
-# tiled_half_kernel<3,16> 829.2 MB + bp_combine_kernel 224.9 MB (the work is per node).
-SWEEP_DRAM_BYTES_PER_NODE = (829.23e6 + 224.94e6) / 10000
+# DRAM bytes one chi-16 degree-3 BP sweep moves per node: ncu captures of a 10k-node sweep,
+# half-node kernel + bp_combine_kernel 224.9 MB (the work is per node): the tensor-core kernel
+# tcx_half_kernel_d3c16 830.1 MB, the CUDA-core kernel tiled_half_kernel<3,16> 829.2 MB.
+SWEEP_DRAM_BYTES_PER_NODE = {"tensor": (830.11e6 + 224.94e6) / 10000, "cuda-core": (829.23e6 + 224.94e6) / 10000}
+# FLOPs the tensor cores execute per degree-3 bond-dim-16 node in the 2xFP16 kernel: per half-node
+# 36 product MMAs of 128 x 32 x 16 and 96 closing MMAs of 64 x 32 x 16 (2 FLOP per MAC)
+TC_EXECUTED_FLOPS_PER_NODE = 2 * (36 * 128 * 32 * 16 + 96 * 64 * 32 * 16) * 2
 
 
 def peaks() -> tuple[dict, str]:
@@ -468,6 +472,41 @@ def run_gpu_arm(args) -> None:
     # the other configurations' shapes, short: the mixed-degree job at bond dim 4 (every node in
     # shared memory) and the degree-4 bond-dim-32 sweep (global-memory kernels)
     tuned = [job.plans[c].describe() for c in sorted(job.plans)] if job.autotune else "off"
+    # the (3, 16) message kernel the timed sweeps ran: the tuner's choice, else the library default
+    if job.autotune and 16 in job.plans:
+        tensor_sweep = "tensor" in job.plans[16].describe()["variants"]
+    else:
+        tensor_sweep = os.environ.get("BQA_GB300_TC", "1") != "0"
+    kind = "tensor" if tensor_sweep else "cuda-core"
+    roofline = {"kernel": "bp sweep (" + ("tcx_half_kernel_d3c16" if tensor_sweep else "tiled_half_kernel<3,16>") +
+                          " + bp_combine_kernel)", "bound": "tensor",
+                "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "peak_source": f"{pk_kind} bf16 burst",
+                "traffic": (SWEEP_DRAM_BYTES_PER_NODE[kind] * n_el if args.chi == 16 else None),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 10k-node sweep "
+                                  f"(half-node kernel {SWEEP_DRAM_BYTES_PER_NODE[kind] * 1e4 / 1e6 - 224.94:.1f} MB "
+                                  "+ combine 224.9 MB), scaled by node count",
+                "algorithmic_bytes_per_launch": bp_bytes / max(len(sweep_ev), 1),
+                "algorithmic_flops_per_launch": bp_flops / max(len(sweep_ev), 1),
+                "legacy_mma_peaks_measured": {"bf16_m16n8k16": mma_peak_tflops(dev, 0),
+                                              "tf32_m16n8k8": mma_peak_tflops(dev, 1),
+                                              "unit": "TFLOP/s", "probe": "bqa_mma_probe"}}
+    if tensor_sweep and args.chi == 16:
+        executed = achieved * TC_EXECUTED_FLOPS_PER_NODE / (16 * 9 * 16 ** 4)
+        roofline["note"] = ("complex64 contraction on the tensor cores in 2xFP16 (every operand split into two "
+                            "FP16 terms, FP32 accumulation): 16 d^2 chi^(d+1) FLOP per node per sweep in the "
+                            "reference order; the tensor cores execute 2.33x that (3 product terms, 4 closing "
+                            "terms, K-split closing stages); FP16 and BF16 dense rates are the same")
+        roofline["tensor_executed"] = {"tflops": executed, "frac": executed / pk["bf16_tflops"],
+                                       "flops_per_node": TC_EXECUTED_FLOPS_PER_NODE}
+    else:
+        roofline["note"] = ("complex64 SIMT contraction: 16 d^2 chi^(d+1) FLOP per node per sweep (reference "
+                            "order; the kernel executes 54% of them at degree 3, chi 16); the FP32 CUDA-core "
+                            "peak, measured below, is the ceiling of this kernel")
+        roofline["fp32_simt"] = {"peak_measured": fp32_peak, "unit": "TFLOP/s",
+                                 "achieved_executed": achieved * EXECUTED_FRACTION.get(args.chi, 1.0),
+                                 "frac": achieved * EXECUTED_FRACTION.get(args.chi, 1.0) / fp32_peak,
+                                 "probe": "bqa_fp32_fma_probe, 16 independent FMA chains per thread"}
     secondary = None
     if args.secondary:
         del job
@@ -503,24 +542,7 @@ def run_gpu_arm(args) -> None:
         "bp_msg_updates_per_s": ctx.edges_number * sum(sweeps) / (bp_ms / 1000.0) if bp_ms else None,
         "sweeps_per_step": float(np.mean(sweeps)), "bond_dim": window[-1]["bond_dim"],
         "time_split_ms": {k: round(v, 2) for k, v in sorted(by_name.items(), key=lambda kv: -kv[1])},
-        "roofline": {"kernel": "bp sweep (tiled_half_kernel<3,16> + bp_combine_kernel)", "bound": "tensor",
-                     "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                     "frac": achieved / pk["bf16_tflops"], "peak_source": f"{pk_kind} bf16 burst",
-                     "traffic": (SWEEP_DRAM_BYTES_PER_NODE * n_el if args.chi == 16 else None),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 10k-node sweep "
-                                       "(half-node kernel 829.2 MB + combine 224.9 MB), scaled by node count",
-                     "algorithmic_bytes_per_launch": bp_bytes / max(len(sweep_ev), 1),
-                     "algorithmic_flops_per_launch": bp_flops / max(len(sweep_ev), 1),
-                     "note": "complex64 SIMT contraction: 16 d^2 chi^(d+1) FLOP per node per sweep "
-                             "(reference order; the kernel executes 54% of them at degree 3, chi 16); the FP32 "
-                             "CUDA-core peak, measured below, is the ceiling of this kernel",
-                     "fp32_simt": {"peak_measured": fp32_peak, "unit": "TFLOP/s",
-                                   "achieved_executed": achieved * EXECUTED_FRACTION.get(args.chi, 1.0),
-                                   "frac": achieved * EXECUTED_FRACTION.get(args.chi, 1.0) / fp32_peak,
-                                   "probe": "bqa_fp32_fma_probe, 16 independent FMA chains per thread"},
-                     "legacy_mma_peaks_measured": {"bf16_m16n8k16": mma_peak_tflops(dev, 0),
-                                                   "tf32_m16n8k8": mma_peak_tflops(dev, 1),
-                                                   "unit": "TFLOP/s", "probe": "bqa_mma_probe"}},
+        "roofline": roofline,
         "e2e": {"value": replica_value(world, args.steps, 1000.0 * e2e_s), "unit": "steps/s", "h2d_bytes_per_step": 16,
                 "d2h_bytes_per_step": int(n_el * 4 * 8 + 2 * args.chi * 4 + 64),
                 "what": "Annealer.run_layer + bloch_vectors per step (host scalars in, all marginals out), "

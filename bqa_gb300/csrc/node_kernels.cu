@@ -44,11 +44,12 @@ static const bool g_use_specialized = [] {
     const char* v = getenv("BQA_GB300_SPECIALIZED");
     return !(v && v[0] == '0');
 }();
-// The (3, 16) half-node kernel runs its bond products on the tensor cores (tc_d3c16.cuh)
-// when BQA_GB300_TC=1 is set when the library loads (the CUDA-core kernel otherwise).
+// The default (3, 16) half-node kernel is the FP32-accurate tensor-core kernel (2xFP16 bond
+// products and closing contractions, tc_f16x2_d3c16.cuh); BQA_GB300_TC=0 set when the library
+// loads makes it the CUDA-core kernel.
 static const bool g_use_tc = [] {
     const char* v = getenv("BQA_GB300_TC");
-    return v && v[0] == '1';
+    return !(v && v[0] == '0');
 }();
 
 // CTAs of the tensor-core kernels whose wait for their MMAs timed out (bqa_tc_faults).
@@ -1440,6 +1441,208 @@ __global__ void __launch_bounds__(tch::TH, 2) tch_half_kernel_d3c16(NodeArgs<flo
     }
 }
 
+// Half-node kernel of degree 3, bond dim 16 with the bond products AND the closing
+// contractions on the tensor cores, both in 2xFP16 (FP32-accurate; tc_f16x2_d3c16.cuh): one
+// product round trip, then six closing stages (three blocks x two halves of the contraction)
+// through three shared-memory buffers, each stage's operands written while the MMAs of the two
+// stages before it run.  Diagonal incoming messages take the FP32 bond-scaling path with the
+// closing contractions on the CUDA cores.  Same outputs as the other half-node kernels.
+//
+// Grid-stride: at most two CTAs per SM walk the `halves` half-nodes; tensor memory is allocated
+// once per CTA.  Four mbarriers (products, stage buffers 0-2); every commit is waited for
+// exactly once, in order, by every thread, so each wait's parity is its commit count's.  A wait
+// that runs out sets the CTA's fault word and the thread carries on (every access stays inside
+// its buffers); the CTA stops at the next half-node, after one more bounded wait for its last
+// commit, and counts itself in bqa_tc_faults.
+__global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<float> a, int halves) {
+    constexpr int CHI = 16, D = 3, N2 = CHI * CHI, PS = CHI * CHI * CHI, TH = tch::TH;
+    extern __shared__ double4_32a smem_raw[];
+    unsigned char* reg = reinterpret_cast<unsigned char*>(smem_raw);
+    float2* const region = reinterpret_cast<float2*>(smem_raw);
+    float2* const V1 = region + tcd3::X_V1;
+    float2* const V2 = region + tcd3::X_V2;
+    float2* const V0 = region + tcd3::X_V0;
+    float2* const sP = region + tch::SP;
+    float2* const sMt = region + tch::SMT;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reg + tch::REGION);   // products, buffers 0-2
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 4);
+    volatile uint32_t* fault = slot + 1;
+    uint32_t* wmax = slot + 2;   // [warp][|T|, |M_0|, |M_1|, |M_2|]
+    const float2* msgs_in = a.msgs_a;
+    if (a.loop_state != nullptr) {
+        if (a.loop_state[0]) return;
+        if (a.loop_state[2]) msgs_in = a.msgs_b;
+    }
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    if (t == 0) {
+        for (int i = 0; i < 4; ++i) tc::mbar_init(bars + i, 1);
+        tc::fence_mbar_init();
+        *fault = 0;
+    }
+    const uint32_t rb = tc::smem_u32(reg);
+    uint32_t tmem = 0;
+    uint32_t commits[4] = {0, 0, 0, 0};
+    int last = -1;   // barrier of the latest commit
+    bool tmem_held = false;
+    namespace q = tiled::d3c16;
+    constexpr int CT = 160;
+    // this thread's row of the products' accumulators
+    const int prow = 128 * (warp >> 2) + 32 * (warp & 3) + lane, phi = prow >> 4, plo = prow & 15;
+    auto wait = [&](int i) {
+        if (!tc::mbar_wait(bars + i, (commits[i] - 1) & 1, tch::WAIT_CYCLES)) *fault = 1;
+    };
+    for (int h = blockIdx.x; h < halves; h += gridDim.x) {
+        const int node = h >> 1, s = h & 1;
+        float4 tv[8];
+        tcd3::load_share(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS, tv);
+        // thread t holds entry (y, x) = (t >> 4, t & 15) of each incoming message
+        float2 mv[3];
+        int offdiag = 0;
+        uint32_t mm[3];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            mv[k] = msgs_in[(size_t)a.in_pos[node * D + k] * N2 + t];
+            offdiag |= ((t >> 4) != (t & 15)) && (mv[k].x != 0.f || mv[k].y != 0.f);
+            mm[k] = __reduce_max_sync(0xffffffffu, max(tch::mag(mv[k].x), tch::mag(mv[k].y)));
+        }
+        uint32_t mt = 0;
+#pragma unroll
+        for (int m = 0; m < 8; ++m)
+            mt = max(mt, max(max(tch::mag(tv[m].x), tch::mag(tv[m].y)), max(tch::mag(tv[m].z), tch::mag(tv[m].w))));
+        mt = __reduce_max_sync(0xffffffffu, mt);
+        if (lane == 0) {
+            wmax[4 * warp] = mt;
+#pragma unroll
+            for (int k = 0; k < D; ++k) wmax[4 * warp + 1 + k] = mm[k];
+        }
+        auto out_block = [&](int idx) { return a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2; };
+        const bool diag = !__syncthreads_or(offdiag);
+        if (*fault) break;
+        if (!diag) {
+            uint32_t gm[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (int w = 0; w < TH / 32; ++w)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) gm[i] = max(gm[i], wmax[4 * w + i]);
+            const int kt = tch::scale_exp(gm[0]);
+            const int km[3] = {tch::scale_exp(gm[1]), tch::scale_exp(gm[2]), tch::scale_exp(gm[3])};
+            if (!tmem_held) {
+                if (warp == 0) {
+                    tc::alloc(slot, tch::TMEM_COLS);
+                    tc::relinquish();
+                }
+                tc::fence_before();
+                __syncthreads();
+                tc::fence_after();
+                tmem = *slot;
+                tmem_held = true;
+            }
+            const float sm[3] = {tch::pow2(km[0]), tch::pow2(km[1]), tch::pow2(km[2])};
+            tch::store_b(mv, sm, reg);
+            tch::store_a(tv, tch::pow2(kt), reg);
+            tc::fence_proxy_async();
+            tc::fence_before();
+            __syncthreads();
+            tc::fence_after();
+            if (t == 0) {
+                tch::issue_products(tmem, rb);
+                tc::commit(bars);
+            }
+            ++commits[0];
+            last = 0;
+            wait(0);
+            tc::fence_after();
+            const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32 * (warp >> 2);
+            // P = D 2^(42 - 2 kt - km_x - km_r), as two normal factors
+            auto unscale = [&](int kx, int kr, float (&sc)[2]) {
+                const int e = 42 - 2 * kt - kx - kr, e1 = max(-126, min(126, e));
+                sc[0] = tch::pow2(e1);
+                sc[1] = tch::pow2(e - e1);
+            };
+            // block 0: P_0 = <V_1|V_2> (columns C0); 1: P_2 = <V_0|V_1> (C1); 2: P_1 = <V_0|V_2> (C0)
+            auto block_epilogue = [&](int blk) {
+                float sc[2];
+                if (blk == 0) unscale(km[1], km[2], sc);
+                else if (blk == 1) unscale(km[0], km[1], sc);
+                else unscale(km[0], km[2], sc);
+                tch::epilogue_block(tmem + (blk == 1 ? tch::COL_C1 : tch::COL_C0), sc,
+                                    reinterpret_cast<float*>(out_block(blk == 0 ? 0 : (blk == 1 ? 2 : 1))));
+            };
+            auto stage = [&](auto st_tag) {
+                constexpr int ST = decltype(st_tag)::value, BLK = ST >> 1, RHO = ST & 1, B = ST % 3;
+                if (ST >= 3) {   // the MMAs of stage ST - 3 (same buffer) have completed
+                    wait(1 + B);
+                    tc::fence_after();
+                    if (ST == 4 && warp < 4) block_epilogue(0);   // stage 1 is done too
+                }
+                tch::write_stage<BLK>(tl, RHO, phi, plo, reg + B * tch::STAGE);
+                tc::fence_proxy_async();
+                tc::fence_before();
+                __syncthreads();
+                if (t == 0) {
+                    tc::fence_after();
+                    tch::issue_stage(tmem + ((BLK & 1) ? tch::COL_C1 : tch::COL_C0), rb + B * tch::STAGE, RHO);
+                    tc::commit(bars + 1 + B);
+                }
+                ++commits[1 + B];
+                last = 1 + B;
+            };
+            stage(std::integral_constant<int, 0>{});
+            stage(std::integral_constant<int, 1>{});
+            stage(std::integral_constant<int, 2>{});
+            stage(std::integral_constant<int, 3>{});
+            stage(std::integral_constant<int, 4>{});
+            stage(std::integral_constant<int, 5>{});
+            wait(1);   // stage 3
+            wait(2);   // stage 4
+            wait(3);   // stage 5
+            tc::fence_after();
+            block_epilogue(warp < 4 ? 1 : 2);
+            tc::fence_before();   // these tensor-memory reads precede the next half-node's MMAs
+            continue;
+        }
+        // all incoming messages diagonal: bond scalings in FP32 (sMt[k][16 x + y] = M_k[y][x]),
+        // closing contractions on warps 0-4, the previous block copied out by warps 5-7
+#pragma unroll
+        for (int k = 0; k < D; ++k) sMt[k * N2 + 16 * (t & 15) + (t >> 4)] = mv[k];
+        tcd3::store_share_swizzled(tv, V0);
+        __syncthreads();
+        tiled::diag_scale3<CHI, TH, 7>(V0, V1, sMt + N2, 1);
+        tiled::diag_scale3<CHI, TH, 7>(V0, V2, sMt + 2 * N2, 2);
+        __syncthreads();
+        tiled::diag_scale3<CHI, TH, 7>(V0, V0, sMt, 0);
+        __syncthreads();
+        float2* const sPb[2] = {sP, sP + N2};
+        int pend = -1, cur = 0;
+        auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
+            constexpr int IDX = decltype(idx_tag)::value;
+            if (t < CT) q::close<IDX>(X, R, sPb[cur]);
+            else if (pend >= 0)
+                tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t - CT,
+                                             TH - CT);
+            __syncthreads();
+            pend = IDX;
+            cur ^= 1;
+        };
+        emit_s(std::integral_constant<int, 0>{}, V1, V2);
+        emit_s(std::integral_constant<int, 2>{}, V0, V1);
+        emit_s(std::integral_constant<int, 1>{}, V0, V2);
+        tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t, TH);
+        __syncthreads();
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (*fault) {
+        // an MMA wait ran out: give the latest commit one more bounded wait, count the CTA
+        if (last >= 0) tc::mbar_wait(bars + last, (commits[last] - 1) & 1, tch::WAIT_CYCLES);
+        if (t == 0) atomicAdd(&g_tc_faults, 1);
+    }
+    if (tmem_held && warp == 0) {
+        tc::fence_after();
+        tc::dealloc(tmem, tch::TMEM_COLS);
+    }
+}
+
 // BP distance above which the mixed-precision (3, 16) kernel takes its BF16 path; the
 // environment variable BQA_GB300_MIXED_SWITCH overrides it when the library loads.
 static const float g_mixed_switch = [] {
@@ -1472,6 +1675,15 @@ static int launch_tcb_half(const NodeArgs<float>& args, int count, cudaStream_t 
     return check_launch("bf16 tensor-core half kernel");
 }
 
+static int launch_tcx_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
+    const size_t smem = (size_t)tch::REGION + tch::SCRATCH_X;
+    int rc = ensure_smem((const void*)tcx_half_kernel_d3c16, smem, "2xFP16 tensor-core half kernel");
+    if (rc) return rc;
+    const int halves = 2 * count;
+    tcx_half_kernel_d3c16<<<std::min(halves, 2 * sm_count()), tch::TH, smem, st>>>(args, halves);
+    return check_launch("2xFP16 tensor-core half kernel");
+}
+
 static int launch_tch_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
     const size_t smem = (size_t)tch::REGION + tch::SCRATCH;
     int rc = ensure_smem((const void*)tch_half_kernel_d3c16, smem, "2xFP16 tensor-core half kernel");
@@ -1481,16 +1693,20 @@ static int launch_tch_half(const NodeArgs<float>& args, int count, cudaStream_t 
     return check_launch("2xFP16 tensor-core half kernel");
 }
 
-// The FP32-accurate tensor-core kernel: 2xFP16 products (one tensor-core round trip per
-// half-node), or 3xTF32 products when BQA_GB300_TC_TF32=1 is set when the library loads.
-static const bool g_tc_tf32 = [] {
-    const char* v = getenv("BQA_GB300_TC_TF32");
-    return v && v[0] == '1';
+// The FP32-accurate tensor-core kernel, chosen by BQA_GB300_TC_KIND when the library loads:
+// products and closing contractions in 2xFP16 (default), "products" for 2xFP16 products with
+// the closing contractions on the CUDA cores, "tf32" for 3xTF32 products.
+static const int g_tc_kind = [] {
+    const char* v = getenv("BQA_GB300_TC_KIND");
+    if (v && !strcmp(v, "products")) return 1;
+    if (v && !strcmp(v, "tf32")) return 2;
+    return 0;
 }();
 
 static int launch_tc_half(const NodeArgs<float>& args, int count, cudaStream_t st) {
     if (pack_record(launch_solo_f32<launch_tc_half>, 0, 0, count, args)) return BQA_OK;
-    if (!g_tc_tf32) return launch_tch_half(args, count, st);
+    if (g_tc_kind == 0) return launch_tcx_half(args, count, st);
+    if (g_tc_kind == 1) return launch_tch_half(args, count, st);
     const size_t smem = (size_t)tcd3::REGION + (3 + 2) * 256 * sizeof(float2) + 16;
     int rc = ensure_smem((const void*)tc_half_kernel_d3c16, smem, "tensor-core half kernel");
     if (rc) return rc;

@@ -46,6 +46,8 @@ static_assert(8 * (SMT + 3 * 256) <= (int)REGION, "close buffers exceed the regi
 static_assert(tcd3::X_V1 == 0 && tcd3::X_V2 == 4096 && tcd3::X_V0 == 8192, "close buffer offsets");
 // mbarrier (8 B), tensor-memory slot (4 B), maxima [8 warps][4] (128 B)
 constexpr uint32_t SCRATCH = 8 + 4 + 4 * 32;
+// the all-tensor-core kernel: four mbarriers, the slot, the fault word and the maxima
+constexpr uint32_t SCRATCH_X = 4 * 8 + 4 + 4 + 4 * 32;
 constexpr uint32_t TMEM_COLS = 256;
 constexpr uint32_t IDESC = tc::idesc(tc::FMT_F16, 128, 32);
 constexpr uint32_t COL_V2 = tcd3::COL_V2, COL_V1 = tcd3::COL_V1, COL_V0 = tcd3::COL_V0;
@@ -54,12 +56,13 @@ constexpr long long WAIT_CYCLES = 2000000000LL;
 // bits of |x| (ordered like the magnitudes for finite x)
 __device__ __forceinline__ uint32_t mag(float x) { return __float_as_uint(x) & 0x7fffffffu; }
 
-// Exponent k with 2^14 <= m 2^k < 2^15 for the largest magnitude m (bits of m), clamped so that
-// 2^k and 2^-k are normal floats; 0 for m = 0.
+// Exponent k with 2^14 <= m 2^k < 2^15 for the largest magnitude m (bits of m), clamped to
+// [-50, 50] so that the scales of a product of up to four operands stay normal floats (a block
+// beyond 2^36 or below 2^-36 just sits outside [2^14, 2^15)); 0 for m = 0.
 __device__ __forceinline__ int scale_exp(uint32_t mbits) {
     if (mbits == 0) return 0;
     const int e = (int)(mbits >> 23) - 127;   // floor(log2 m) for normal m, -127 below
-    return max(-126, min(126, 14 - e));
+    return max(-50, min(50, 14 - e));
 }
 __device__ __forceinline__ float pow2(int k) { return __uint_as_float((uint32_t)(k + 127) << 23); }
 
@@ -141,6 +144,132 @@ __device__ __forceinline__ void issue_products(uint32_t tmem, uint32_t rb) {
                 tc::mma_f16(d, ahi, bhi, IDESC, 1u);
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Closing contractions on the tensor cores too (2xFP16, FP32-accurate).  P[o][o'] =
+// sum_kappa conj(X[o, kappa]) R[o', kappa] over the two other bonds kappa is, as in
+// tc_bf16_d3c16.cuh, the real GEMM D[(o, p)][(o', q)] = sum_kappa X_p[o, kappa] R_q[o', kappa]
+// with Re P = D00 + D11 and Im P = D01 - D10.  Both sides are the products' accumulators times
+// 2^-21 (their scaled magnitudes are below 32 x 2^15 x 2^15 = 2^35, so the operands stay below
+// 2^14) split into FP16 hi + lo:
+//   * X (MN-major, M = 64): rows 16 Q + i hold X_hi of P row 8 Q + i and rows 16 Q + 8 + i its
+//     X_lo (P row = 2 o + p), so both halves of a P row land in the same warp's lanes of the
+//     M = 64 accumulator (row m in lane 32 (m / 16) + m % 16) and one shuffle adds them;
+//   * R_hi and R_lo (K-major, N = 32): two MMAs per K step into the same accumulator,
+// so each K step accumulates all four products X_hi R_hi + X_hi R_lo + X_lo R_hi + X_lo R_lo.
+// K (= 256 pairs kappa = (u, v) of the two contracted bonds) is split into two stages by
+// parity: stage rho takes the kappa with (u + v) % 2 = rho, at K index 8 u + v / 2, so a thread
+// holding a row of the R side (u fixed, v along its registers) writes 16-byte chunks.  The six
+// stages (three blocks x two halves) alternate between two 36 KB buffers: a stage's operands
+// are written while the previous stage's MMAs run.  Block accumulators alternate between tensor
+// memory columns 192 and 224 (the products keep [0, 192) until the last stage is written).
+//
+//   block  X side (rows: hi, lo; registers)    R side (rows: hi, lo; registers)   (u, v)
+//   P_0    V_1 (o = a, c; b)                   V_2 (o' = a, b; c)                  (b, c)
+//   P_2    V_0 (b, o = c; a)                   V_1 (a, o' = c; b)                  (a, b)
+//   P_1    V_0 (o = b, c; a)                   V_2 (a, o' = b; c)                  (a, c)
+constexpr uint32_t X_LBO = 1152, X_SBO = 144;   // K-chunk and M-group strides (8 groups, padded)
+constexpr uint32_t R_LBO = 144, R_SBO = 2304;   // K-chunk (padded) and N-group strides
+constexpr uint32_t X_BYTES = 16 * X_LBO;        // 18,432: K = 128
+constexpr uint32_t R_BYTES = 4 * R_SBO;         // 9,216
+constexpr uint32_t STAGE = X_BYTES + 2 * R_BYTES;
+static_assert(3 * STAGE <= REGION, "close stages exceed the region");
+constexpr uint32_t COL_C0 = 192, COL_C1 = 224;
+constexpr uint32_t ID_CLOSE = tc::idesc(tc::FMT_F16, 64, 32, true, false);
+constexpr float OPERAND_SCALE = 1.0f / 2097152.0f;   // 2^-21
+
+__device__ __forceinline__ uint32_t x_off(int m, int k) {   // MN-major
+    return (k >> 3) * X_LBO + (m >> 3) * X_SBO + (k & 7) * 16 + (m & 7) * 2;
+}
+__device__ __forceinline__ uint32_t r_off(int n, int k) {   // K-major
+    return (n >> 3) * R_SBO + (k >> 3) * R_LBO + (n & 7) * 16 + (k & 7) * 2;
+}
+
+// Operands of stage (block BLK, half rho) into buffer `buf`, from the products' accumulators:
+// the thread's row r = 16 hi + lo (32 rows a warp, quarter w % 4 of row tile w / 4).
+template <int BLK>
+__device__ __forceinline__ void write_stage(uint32_t tl, int rho, int hi, int lo, unsigned char* __restrict__ buf) {
+    uint32_t f[32];
+    {   // X side: the thread holds open index o and contracted index V; u along the registers
+        tc::ld_32x32b_x32(tl + (BLK == 0 ? COL_V1 : COL_V0), f);
+        tc::wait_ld();
+        const int O = BLK == 1 ? lo : hi, V = BLK == 1 ? hi : lo;
+        const int mh = 16 * (O >> 2) + 2 * (O & 3);
+        const bool odd = ((V + rho) & 1) != 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {   // u = 2 i + odd
+            const float x0 = __uint_as_float(odd ? f[4 * i + 2] : f[4 * i]);
+            const float x1 = __uint_as_float(odd ? f[4 * i + 3] : f[4 * i + 1]);
+            const Pair e = split2(x0, x1, OPERAND_SCALE);
+            const int k = 8 * (2 * i + (odd ? 1 : 0)) + (V >> 1);
+            *reinterpret_cast<uint32_t*>(buf + x_off(mh, k)) = e.hi;
+            *reinterpret_cast<uint32_t*>(buf + x_off(mh + 8, k)) = e.lo;
+        }
+    }
+    {   // R side: the thread holds contracted index U and open index o'; v along the registers
+        tc::ld_32x32b_x32(tl + (BLK == 1 ? COL_V1 : COL_V2), f);
+        tc::wait_ld();
+        const int U = BLK == 0 ? lo : hi, Op = BLK == 0 ? hi : lo;
+        const bool odd = ((U + rho) & 1) != 0;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            uint32_t wh[4], wl[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {   // v = 2 j + odd for j = 2 i, 2 i + 1
+                const float y0 = __uint_as_float(odd ? f[8 * i + 2 + q] : f[8 * i + q]);
+                const float y1 = __uint_as_float(odd ? f[8 * i + 6 + q] : f[8 * i + 4 + q]);
+                const Pair e = split2(y0, y1, OPERAND_SCALE);
+                wh[i] = e.hi;
+                wl[i] = e.lo;
+            }
+            const uint32_t o = r_off(2 * Op + q, 8 * U);
+            *reinterpret_cast<uint4*>(buf + X_BYTES + o) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+            *reinterpret_cast<uint4*>(buf + X_BYTES + R_BYTES + o) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+        }
+    }
+}
+
+// One thread: the 16 MMAs of a stage (8 K steps x (R_lo, R_hi)) into accumulator d; `acc` 0
+// starts the block.
+__device__ __forceinline__ void issue_stage(uint32_t d, uint32_t buf, uint32_t acc) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const uint64_t x = tc::desc_noswz(buf + s * 2 * X_LBO, X_LBO, X_SBO);
+        const uint64_t rh = tc::desc_noswz(buf + X_BYTES + s * 2 * R_LBO, R_LBO, R_SBO);
+        const uint64_t rl = tc::desc_noswz(buf + X_BYTES + R_BYTES + s * 2 * R_LBO, R_LBO, R_SBO);
+        tc::mma_f16(d, x, rl, ID_CLOSE, (s > 0 || acc) ? 1u : 0u);
+        tc::mma_f16(d, x, rh, ID_CLOSE, 1u);
+    }
+}
+
+// Epilogue of one block by four warps (warp w reading lane quarter w % 4): lanes 0-7 hold the hi
+// rows m = 16 w + i of P rows 8 w + i, lanes 8-15 the lo rows; the two are added, lane pairs
+// combine the real and imaginary parts, and lanes 0-7 write P row 8 w + lane (16 values of part
+// p), scaled by s[0] s[1], to P (global, row-major 16 x 16 complex).
+__device__ __forceinline__ void epilogue_block(uint32_t tmem_col, const float (&sc)[2], float* __restrict__ P) {
+    const int w = (threadIdx.x >> 5) & 3, lane = threadIdx.x & 31;
+    uint32_t f[32];
+    tc::ld_32x32b_x32(tmem_col + ((uint32_t)(32 * w) << 16), f);
+    tc::wait_ld();
+    float g[32];
+#pragma unroll
+    for (int n = 0; n < 32; ++n) {
+        const float v = __uint_as_float(f[n]);
+        g[n] = v + __shfl_xor_sync(0xffffffffu, v, 8);
+    }
+    const int pr = 8 * w + (lane & 7), o = pr >> 1, p = pr & 1;
+    float out[16];
+#pragma unroll
+    for (int y = 0; y < 16; ++y) {
+        const float h = __shfl_xor_sync(0xffffffffu, g[2 * y + 1], 1);
+        const float own = g[2 * y];
+        out[y] = (p ? h - own : own + h) * sc[0] * sc[1];
+    }
+    if (lane < 8) {
+#pragma unroll
+        for (int y = 0; y < 16; ++y) P[2 * (o * 16 + y) + p] = out[y];
     }
 }
 

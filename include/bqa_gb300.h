@@ -49,8 +49,11 @@ enum {
     BQA_VARIANT_DEFAULT = 0,  /* the kernel bqa_bp_sweep / bqa_bp_sweep_split launch */
     BQA_VARIANT_TILED = 1,    /* register-tiled: half-node (two-stage sweep) or whole-node (one stage) */
     BQA_VARIANT_GENERIC = 2,  /* generic shared-memory kernel (global-memory form beyond shared memory) */
-    BQA_VARIANT_TENSOR = 3,   /* half-node kernel with tensor-core (tcgen05, 3xTF32) bond products:
-                                 two-stage complex64 sweeps of degree 3 at bond dim 16 */
+    BQA_VARIANT_TENSOR = 3,   /* FP32-accurate tensor-core (tcgen05) half-node kernel: bond products
+                                 and closing contractions in 2xFP16 (BQA_GB300_TC_KIND=products or
+                                 tf32 at library load: 2xFP16 or 3xTF32 products with the closing
+                                 contractions on the CUDA cores); two-stage complex64 sweeps of
+                                 degree 3 at bond dim 16 */
     BQA_VARIANT_TENSOR_BF16 = 4, /* half-node kernel with BF16 tensor-core products AND closing
                                     contractions (FP32 accumulation; messages ~1e-3 relative),
                                     same shapes as TENSOR */
@@ -260,7 +263,7 @@ int32_t bqa_bp_sweep_split(const bqa_class* classes /* host array */, int32_t n_
  * (complex64, degree 2-4, chi in {4, 8, 12, 16} minus (2, 4) and (4, 12+)); at degree 3, bond dim
  * 16 it is the CUDA-core half-node kernel.  TENSOR is the tensor-core half-node kernel (two-stage,
  * complex64, degree 3, bond dim 16 only; BQA_ERR_UNSUPPORTED elsewhere), which is also what
- * DEFAULT launches there when BQA_GB300_TC=1 was set when the library loaded.  GENERIC may carry
+ * DEFAULT launches there unless BQA_GB300_TC=0 was set when the library loaded.  GENERIC may carry
  * the CTA size of the shared-memory generic kernel as warps per node in bits 8-15
  * (GENERIC | (w << 8), 1 <= w <= 32; 0 keeps the kernel's own choice: one thread per fibre, at
  * most 8 warps, or 32 for nodes whose shared memory leaves room for at most two CTAs per SM at

@@ -1,13 +1,16 @@
-"""The tensor-core (tcgen05, 3xTF32) half-node message kernel of degree 3 at bond dim 16.
+"""The FP32-accurate tensor-core (tcgen05) half-node message kernels of degree 3 at bond dim 16.
 
-It computes the bond products T x_k M_k on the tensor cores and keeps the closing
-contractions on the CUDA cores.  Checked through the C ABI (bqa_bp_sweep_plan with
+BQA_VARIANT_TENSOR runs the bond products T x_k M_k and the closing contractions on the tensor
+cores in 2xFP16 (BQA_GB300_TC_KIND at load selects 2xFP16 products with CUDA-core closing
+contractions, or 3xTF32 products).  Checked through the C ABI (bqa_bp_sweep_plan with
 BQA_VARIANT_TENSOR, and the default two-stage entry points that launch it):
   * one BP sweep equals one oracle sweep to the complex64 kernel tolerance (2e-5 relative);
   * it agrees with the CUDA-core half-node kernel (BQA_VARIANT_TILED) to 2e-6 relative on a
     few hundred nodes with dense random Hermitian messages;
   * diagonal incoming messages take the bond-scaling path and match the oracle;
   * the extended messages of the two-stage pass match the oracle;
+  * the per-half-node FP16 operand scaling leaves normalised messages unchanged for tensors
+    and messages far from unit scale;
   * no CTA ever hits the bounded wait for its MMAs (bqa_tc_faults stays 0);
   * other shapes are refused with BQA_ERR_UNSUPPORTED.
 """
@@ -107,7 +110,8 @@ sys.exit(0 if np.array_equal(got, tc) else 3)
 
 
 def test_tensor_core_kernel_as_the_default_two_stage_sweep():
-    """With BQA_GB300_TC=1 at load, bqa_bp_sweep_split at (3, 16) gives the TENSOR variant's bits."""
+    """With BQA_GB300_TC=1 at load (the default), bqa_bp_sweep_split at (3, 16) gives the TENSOR
+    variant's bits."""
     import os
     import subprocess
     import sys
@@ -145,6 +149,52 @@ def test_tensor_core_extended_messages_match_oracle():
     want = orc.get_extended_msgs(octx, zt, st)
     got = job.ext[: want.size].cpu().numpy().reshape(want.shape)
     assert rel_err(got, want) < RTOL
+
+
+_KIND_SCRIPT = """
+import sys, numpy as np
+from tests.test_gpu_tensor_core import dense_state, plan_sweep
+from tests.test_gpu_kernels import rel_err
+from bqa_gb300 import _lib
+from tests.test_gpu_tensor_core import oracle_sweep
+ctx, tens, m, job = dense_state(128, 3)
+tc = plan_sweep(job, _lib.BQA_VARIANT_TENSOR)
+cc = plan_sweep(job, _lib.BQA_VARIANT_TILED)
+err, err_o = rel_err(tc, cc), rel_err(tc, oracle_sweep(ctx, m, tens))
+print(f"tensor-core kernel {sys.argv[1]!r}: vs CUDA-core sweep {err:.2e}, vs oracle {err_o:.2e}")
+sys.exit(0 if err < 2e-6 and err_o < 2e-6 and job.lib.tc_faults(job.stream) == 0 else 3)
+"""
+
+
+@pytest.mark.parametrize("kind", ["products", "tf32"])
+def test_other_tensor_core_kernels_match_cuda_core_kernel(kind):
+    """BQA_GB300_TC_KIND at load selects 2xFP16 products with CUDA-core closing contractions
+    ("products") or 3xTF32 products ("tf32") for BQA_VARIANT_TENSOR; both are FP32-accurate."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, BQA_GB300_TC_KIND=kind, PYTHONPATH=str(root))
+    r = subprocess.run([sys.executable, "-c", _KIND_SCRIPT, kind], cwd=root, env=env, timeout=600)
+    assert r.returncode == 0
+
+
+def _normalised(m):
+    return m / np.trace(m, axis1=1, axis2=2)[:, None, None]
+
+
+def test_tensor_core_sweep_scaling_of_operands():
+    """The FP16 operands are scaled per half-node: tensors scaled by 2^-40 (beyond the scale
+    exponent's clamp) and messages by 2^20 give the same normalised messages."""
+    ctx, tens, m, job = dense_state(64, 6)
+    base = _normalised(plan_sweep(job, _lib.BQA_VARIANT_TENSOR))
+    job.set_state({d: t * 2.0 ** -40 for d, t in tens.items()}, m * 2.0 ** 20)
+    scaled = _normalised(plan_sweep(job, _lib.BQA_VARIANT_TENSOR))
+    err = rel_err(scaled, base)
+    print(f"scaled operands: {err:.2e}")
+    assert err < 2e-6
+    assert job.lib.tc_faults(job.stream) == 0
 
 
 def test_tensor_variant_refuses_other_shapes():
