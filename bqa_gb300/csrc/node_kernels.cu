@@ -1547,6 +1547,15 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
             if (t == 0) {
                 tch::issue_products(tmem, rb);
                 tc::commit(bars);
+                // the CTA's next half-node: its tensor and incoming messages into L2 meanwhile
+                const int hn = h + gridDim.x;
+                if (hn < halves) {
+                    const int nn = hn >> 1;
+                    tc::prefetch_l2(a.tensors + (size_t)nn * 2 * PS + (size_t)(hn & 1) * PS, PS * sizeof(float2));
+#pragma unroll
+                    for (int k = 0; k < D; ++k)
+                        tc::prefetch_l2(msgs_in + (size_t)a.in_pos[nn * D + k] * N2, N2 * sizeof(float2));
+                }
             }
             ++commits[0];
             last = 0;

@@ -154,9 +154,10 @@ __device__ __forceinline__ void issue_products(uint32_t tmem, uint32_t rb) {
 // with Re P = D00 + D11 and Im P = D01 - D10.  Both sides are the products' accumulators times
 // 2^-21 (their scaled magnitudes are below 32 x 2^15 x 2^15 = 2^35, so the operands stay below
 // 2^14) split into FP16 hi + lo:
-//   * X (MN-major, M = 64): rows 16 Q + i hold X_hi of P row 8 Q + i and rows 16 Q + 8 + i its
-//     X_lo (P row = 2 o + p), so both halves of a P row land in the same warp's lanes of the
-//     M = 64 accumulator (row m in lane 32 (m / 16) + m % 16) and one shuffle adds them;
+//   * X (MN-major, M = 64): row 16 Q + 2 i + l holds X_hi (l = 0) or X_lo (l = 1) of P row
+//     8 Q + i (P row = 2 o + p), so both halves of a P row land in neighbouring lanes of the
+//     M = 64 accumulator (row m in lane 32 (m / 16) + m % 16) and one shuffle adds them, and the
+//     four rows of an open index o (p, l) are 8 contiguous bytes of a core matrix;
 //   * R_hi and R_lo (K-major, N = 32): two MMAs per K step into the same accumulator,
 // so each K step accumulates all four products X_hi R_hi + X_hi R_lo + X_lo R_hi + X_lo R_lo.
 // K (= 256 pairs kappa = (u, v) of the two contracted bonds) is split into two stages by
@@ -196,7 +197,7 @@ __device__ __forceinline__ void write_stage(uint32_t tl, int rho, int hi, int lo
         tc::ld_32x32b_x32(tl + (BLK == 0 ? COL_V1 : COL_V0), f);
         tc::wait_ld();
         const int O = BLK == 1 ? lo : hi, V = BLK == 1 ? hi : lo;
-        const int mh = 16 * (O >> 2) + 2 * (O & 3);
+        const int m0 = 16 * (O >> 2) + 4 * (O & 3);   // rows (p, l) = m0 + 2 p + l
         const bool odd = ((V + rho) & 1) != 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {   // u = 2 i + odd
@@ -204,8 +205,8 @@ __device__ __forceinline__ void write_stage(uint32_t tl, int rho, int hi, int lo
             const float x1 = __uint_as_float(odd ? f[4 * i + 3] : f[4 * i + 1]);
             const Pair e = split2(x0, x1, OPERAND_SCALE);
             const int k = 8 * (2 * i + (odd ? 1 : 0)) + (V >> 1);
-            *reinterpret_cast<uint32_t*>(buf + x_off(mh, k)) = e.hi;
-            *reinterpret_cast<uint32_t*>(buf + x_off(mh + 8, k)) = e.lo;
+            *reinterpret_cast<uint2*>(buf + x_off(m0, k)) =
+                make_uint2(__byte_perm(e.hi, e.lo, 0x5410), __byte_perm(e.hi, e.lo, 0x7632));
         }
     }
     {   // R side: the thread holds contracted index U and open index o'; v along the registers
@@ -244,10 +245,10 @@ __device__ __forceinline__ void issue_stage(uint32_t d, uint32_t buf, uint32_t a
     }
 }
 
-// Epilogue of one block by four warps (warp w reading lane quarter w % 4): lanes 0-7 hold the hi
-// rows m = 16 w + i of P rows 8 w + i, lanes 8-15 the lo rows; the two are added, lane pairs
-// combine the real and imaginary parts, and lanes 0-7 write P row 8 w + lane (16 values of part
-// p), scaled by s[0] s[1], to P (global, row-major 16 x 16 complex).
+// Epilogue of one block by four warps (warp w reading lane quarter w % 4): lanes 2 i and 2 i + 1
+// (i < 8) hold the hi and lo rows m = 16 w + 2 i + l of P row 8 w + i; the two are added, lanes
+// 2 apart combine the real and imaginary parts, and the even lanes write P row 8 w + lane / 2
+// (16 values of part p), scaled by s[0] s[1], to P (global, row-major 16 x 16 complex).
 __device__ __forceinline__ void epilogue_block(uint32_t tmem_col, const float (&sc)[2], float* __restrict__ P) {
     const int w = (threadIdx.x >> 5) & 3, lane = threadIdx.x & 31;
     uint32_t f[32];
@@ -257,17 +258,17 @@ __device__ __forceinline__ void epilogue_block(uint32_t tmem_col, const float (&
 #pragma unroll
     for (int n = 0; n < 32; ++n) {
         const float v = __uint_as_float(f[n]);
-        g[n] = v + __shfl_xor_sync(0xffffffffu, v, 8);
+        g[n] = v + __shfl_xor_sync(0xffffffffu, v, 1);
     }
-    const int pr = 8 * w + (lane & 7), o = pr >> 1, p = pr & 1;
+    const int pr = 8 * w + ((lane >> 1) & 7), o = pr >> 1, p = pr & 1;
     float out[16];
 #pragma unroll
     for (int y = 0; y < 16; ++y) {
-        const float h = __shfl_xor_sync(0xffffffffu, g[2 * y + 1], 1);
+        const float h = __shfl_xor_sync(0xffffffffu, g[2 * y + 1], 2);
         const float own = g[2 * y];
         out[y] = (p ? h - own : own + h) * sc[0] * sc[1];
     }
-    if (lane < 8) {
+    if (lane < 16 && !(lane & 1)) {
 #pragma unroll
         for (int y = 0; y < 16; ++y) P[2 * (o * 16 + y) + p] = out[y];
     }

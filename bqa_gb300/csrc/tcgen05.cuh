@@ -146,6 +146,11 @@ __device__ __forceinline__ void ld_32x32b_x16(uint32_t taddr, uint32_t (&r)[16])
         : "r"(taddr));
 }
 
+// Bulk prefetch of `bytes` (a multiple of 16) at global address p (16-byte aligned) into L2.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // x rounded to TF32 (round to nearest, ties away; low 13 mantissa bits zero)
 __device__ __forceinline__ float to_tf32(float x) {
     uint32_t r;
