@@ -529,7 +529,8 @@ def run_gpu_arm(args) -> None:
                  "vs_plain": t_max / mms, **mixed, "accuracy": measured_accuracy(mixed=True),
                  "what": "Annealer(mixed=True): at bond dim 16 the degree-3 sweeps run the mixed kernel "
                          "(BF16 tensor-core products and closing contractions while the last BP distance is "
-                         "above 2^-5, FP32 CUDA-core sweeps after that), same schedule window, device-timed"}
+                         "above 2^-5, FP32-accurate 2xFP16 tensor-core sweeps after that), same schedule window, "
+                         "device-timed"}
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,

@@ -1152,8 +1152,8 @@ __global__ void __launch_bounds__(tcd3::TH, 2) tc_half_kernel_d3c16(NodeArgs<flo
 
 // Half-node kernel of degree 3, bond dim 16 with BF16 tensor-core products and closing
 // contractions (tc_bf16_d3c16.cuh).  MIXED: the kernel does the low-precision sweeps of a mixed
-// BP run (low_precision_sweep) and returns at once on the others, which the specialised
-// CUDA-core half-node kernel, launched next with mixed_role 2, does in FP32.  Diagonal
+// BP run (low_precision_sweep) and returns at once on the others, which the default
+// FP32-accurate half-node kernel, launched next with mixed_role 2, does.  Diagonal
 // incoming messages take the FP32 bond-scaling path.  Same outputs as the other half-node
 // kernels (blocks P_s into pm).
 //
@@ -1473,6 +1473,7 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
         if (a.loop_state[0]) return;
         if (a.loop_state[2]) msgs_in = a.msgs_b;
     }
+    if (a.mixed_role == 2 && low_precision_sweep(a.loop_state, a.mixed_switch)) return;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     if (t == 0) {
         for (int i = 0; i < 4; ++i) tc::mbar_init(bars + i, 1);
@@ -2438,14 +2439,16 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes, int32_t n_classes, int32_t c
             } else if (v == BQA_VARIANT_TENSOR_BF16) {
                 rc = launch_tcb_half<false>(ca, k.count, st);
             } else {
-                // the BF16 kernel takes the low-precision sweeps, the CUDA-core kernel the others
+                // the BF16 kernel takes the low-precision sweeps, the default FP32-accurate kernel
+                // (2xFP16 tensor cores, or the CUDA cores with BQA_GB300_TC=0) the others
                 rc = launch_tcb_half<true>(ca, k.count, st);
                 if (!rc) {
                     NodeArgs<float> cb = ca;
                     cb.mixed_role = 2;
                     cb.mixed_switch = g_mixed_switch;
-                    rc = g_use_specialized ? launch_half_k<3, 16, true>(cb, k.count, st)
-                                           : launch_half_k<3, 16, false>(cb, k.count, st);
+                    rc = g_use_tc ? launch_tcx_half(cb, k.count, st)
+                                  : (g_use_specialized ? launch_half_k<3, 16, true>(cb, k.count, st)
+                                                       : launch_half_k<3, 16, false>(cb, k.count, st));
                 }
             }
         } else if (v == BQA_VARIANT_TILED && pm && dtype == BQA_C64 && k.degree == 3 && chi == 16) {

@@ -60,7 +60,8 @@ enum {
     BQA_VARIANT_MIXED = 5     /* precision follows the BP loop: with a loop state, a sweep after the
                                  first whose last distance (loop_state[5]) exceeds the switch
                                  (2^-5, or BQA_GB300_MIXED_SWITCH at library load) runs the BF16
-                                 kernel, every other sweep the FP32 CUDA-core half-node kernel;
+                                 kernel, every other sweep the default FP32-accurate half-node
+                                 kernel (2xFP16 tensor cores unless BQA_GB300_TC=0);
                                  same shapes as TENSOR */
 };
 

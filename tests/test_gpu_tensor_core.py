@@ -270,9 +270,12 @@ def test_bf16_kernel_with_diagonal_messages_is_exact():
 
 def test_mixed_kernel_follows_the_loop_state():
     """BF16 path after the first sweep while the last distance is above the switch (2^-5), the
-    FP32 CUDA-core kernel otherwise (bit-identical to it), FP32 without a loop state."""
+    default FP32-accurate kernel otherwise (bit-identical to it: the 2xFP16 tensor-core kernel,
+    or the CUDA-core kernel with BQA_GB300_TC=0), FP32 without a loop state."""
+    import os
     ctx, tens, m, job = dense_state(128, 7)
-    fp32 = plan_sweep(job, _lib.BQA_VARIANT_TILED)
+    tc_default = os.environ.get("BQA_GB300_TC", "1") != "0"
+    fp32 = plan_sweep(job, _lib.BQA_VARIANT_TENSOR if tc_default else _lib.BQA_VARIANT_TILED)
     bf16 = plan_sweep(job, _lib.BQA_VARIANT_TENSOR_BF16)
     assert not np.array_equal(fp32, bf16)
     assert np.array_equal(plan_sweep(job, _lib.BQA_VARIANT_MIXED), fp32)                     # no loop state
