@@ -1444,9 +1444,10 @@ __global__ void __launch_bounds__(tch::TH, 2) tch_half_kernel_d3c16(NodeArgs<flo
 // Half-node kernel of degree 3, bond dim 16 with the bond products AND the closing
 // contractions on the tensor cores, both in 2xFP16 (FP32-accurate; tc_f16x2_d3c16.cuh): one
 // product round trip, then six closing stages (three blocks x two halves of the contraction)
-// through three shared-memory buffers, each stage's operands written while the MMAs of the two
-// stages before it run.  Diagonal incoming messages take the FP32 bond-scaling path with the
-// closing contractions on the CUDA cores.  Same outputs as the other half-node kernels.
+// through three shared-memory buffers, a block's two stages written from one read of the
+// accumulators while the previous block's MMAs run.  Diagonal incoming messages take the FP32
+// bond-scaling path with the closing contractions on the CUDA cores.  Same outputs as the other
+// half-node kernels.
 //
 // Grid-stride: at most two CTAs per SM walk the `halves` half-nodes; tensor memory is allocated
 // once per CTA.  Four mbarriers (products, stage buffers 0-2); every commit is waited for
@@ -1578,31 +1579,39 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
                 tch::epilogue_block(tmem + (blk == 1 ? tch::COL_C1 : tch::COL_C0), sc,
                                     reinterpret_cast<float*>(out_block(blk == 0 ? 0 : (blk == 1 ? 2 : 1))));
             };
-            auto stage = [&](auto st_tag) {
-                constexpr int ST = decltype(st_tag)::value, BLK = ST >> 1, RHO = ST & 1, B = ST % 3;
-                if (ST >= 3) {   // the MMAs of stage ST - 3 (same buffer) have completed
-                    wait(1 + B);
+            // block b's two stages go to buffers (2 b) % 3 and (2 b + 1) % 3: block 1 waits for
+            // stage 0 (its buffer 0), block 2 for stages 1 and 2 (buffers 1, 2; block 0's
+            // accumulator, which block 2 reuses, is complete then and read first)
+            auto block = [&](auto blk_tag) {
+                constexpr int BLK = decltype(blk_tag)::value, B0 = (2 * BLK) % 3, B1 = (2 * BLK + 1) % 3;
+                if (BLK == 1) {
+                    wait(1);
                     tc::fence_after();
-                    if (ST == 4 && warp < 4) block_epilogue(0);   // stage 1 is done too
+                } else if (BLK == 2) {
+                    wait(2);
+                    wait(3);
+                    tc::fence_after();
+                    if (warp < 4) block_epilogue(0);
                 }
-                tch::write_stage<BLK>(tl, RHO, phi, plo, reg + B * tch::STAGE);
+                tch::write_block<BLK>(tl, phi, plo, reg + B0 * tch::STAGE, reg + B1 * tch::STAGE);
                 tc::fence_proxy_async();
                 tc::fence_before();
                 __syncthreads();
                 if (t == 0) {
                     tc::fence_after();
-                    tch::issue_stage(tmem + ((BLK & 1) ? tch::COL_C1 : tch::COL_C0), rb + B * tch::STAGE, RHO);
-                    tc::commit(bars + 1 + B);
+                    const uint32_t d = tmem + ((BLK & 1) ? tch::COL_C1 : tch::COL_C0);
+                    tch::issue_stage(d, rb + B0 * tch::STAGE, 0);
+                    tc::commit(bars + 1 + B0);
+                    tch::issue_stage(d, rb + B1 * tch::STAGE, 1);
+                    tc::commit(bars + 1 + B1);
                 }
-                ++commits[1 + B];
-                last = 1 + B;
+                ++commits[1 + B0];
+                ++commits[1 + B1];
+                last = 1 + B1;
             };
-            stage(std::integral_constant<int, 0>{});
-            stage(std::integral_constant<int, 1>{});
-            stage(std::integral_constant<int, 2>{});
-            stage(std::integral_constant<int, 3>{});
-            stage(std::integral_constant<int, 4>{});
-            stage(std::integral_constant<int, 5>{});
+            block(std::integral_constant<int, 0>{});
+            block(std::integral_constant<int, 1>{});
+            block(std::integral_constant<int, 2>{});
             wait(1);   // stage 3
             wait(2);   // stage 4
             wait(3);   // stage 5

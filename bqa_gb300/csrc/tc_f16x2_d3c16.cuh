@@ -163,9 +163,10 @@ __device__ __forceinline__ void issue_products(uint32_t tmem, uint32_t rb) {
 // K (= 256 pairs kappa = (u, v) of the two contracted bonds) is split into two stages by
 // parity: stage rho takes the kappa with (u + v) % 2 = rho, at K index 8 u + v / 2, so a thread
 // holding a row of the R side (u fixed, v along its registers) writes 16-byte chunks.  The six
-// stages (three blocks x two halves) alternate between two 36 KB buffers: a stage's operands
-// are written while the previous stage's MMAs run.  Block accumulators alternate between tensor
-// memory columns 192 and 224 (the products keep [0, 192) until the last stage is written).
+// stages (three blocks x two halves) rotate through three 36 KB buffers; both stages of a block
+// are written from one read of the accumulators, while the previous block's second stage runs.
+// Block accumulators alternate between tensor-memory columns 192 and 224 (the products keep
+// [0, 192) until the last block is written).
 //
 //   block  X side (rows: hi, lo; registers)    R side (rows: hi, lo; registers)   (u, v)
 //   P_0    V_1 (o = a, c; b)                   V_2 (o' = a, b; c)                  (b, c)
@@ -188,46 +189,55 @@ __device__ __forceinline__ uint32_t r_off(int n, int k) {   // K-major
     return (n >> 3) * R_SBO + (k >> 3) * R_LBO + (n & 7) * 16 + (k & 7) * 2;
 }
 
-// Operands of stage (block BLK, half rho) into buffer `buf`, from the products' accumulators:
-// the thread's row r = 16 hi + lo (32 rows a warp, quarter w % 4 of row tile w / 4).
+// Operands of both stages of block BLK (half rho into buf[rho]) from the products'
+// accumulators: the thread's row r = 16 hi + lo (32 rows a warp, quarter w % 4 of row tile w / 4).
 template <int BLK>
-__device__ __forceinline__ void write_stage(uint32_t tl, int rho, int hi, int lo, unsigned char* __restrict__ buf) {
+__device__ __forceinline__ void write_block(uint32_t tl, int hi, int lo, unsigned char* __restrict__ buf0,
+                                            unsigned char* __restrict__ buf1) {
     uint32_t f[32];
     {   // X side: the thread holds open index o and contracted index V; u along the registers
         tc::ld_32x32b_x32(tl + (BLK == 0 ? COL_V1 : COL_V0), f);
         tc::wait_ld();
         const int O = BLK == 1 ? lo : hi, V = BLK == 1 ? hi : lo;
         const int m0 = 16 * (O >> 2) + 4 * (O & 3);   // rows (p, l) = m0 + 2 p + l
-        const bool odd = ((V + rho) & 1) != 0;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {   // u = 2 i + odd
-            const float x0 = __uint_as_float(odd ? f[4 * i + 2] : f[4 * i]);
-            const float x1 = __uint_as_float(odd ? f[4 * i + 3] : f[4 * i + 1]);
-            const Pair e = split2(x0, x1, OPERAND_SCALE);
-            const int k = 8 * (2 * i + (odd ? 1 : 0)) + (V >> 1);
-            *reinterpret_cast<uint2*>(buf + x_off(m0, k)) =
-                make_uint2(__byte_perm(e.hi, e.lo, 0x5410), __byte_perm(e.hi, e.lo, 0x7632));
+        for (int rho = 0; rho < 2; ++rho) {
+            unsigned char* buf = rho ? buf1 : buf0;
+            const bool odd = ((V + rho) & 1) != 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {   // u = 2 i + odd
+                const float x0 = __uint_as_float(odd ? f[4 * i + 2] : f[4 * i]);
+                const float x1 = __uint_as_float(odd ? f[4 * i + 3] : f[4 * i + 1]);
+                const Pair e = split2(x0, x1, OPERAND_SCALE);
+                const int k = 8 * (2 * i + (odd ? 1 : 0)) + (V >> 1);
+                *reinterpret_cast<uint2*>(buf + x_off(m0, k)) =
+                    make_uint2(__byte_perm(e.hi, e.lo, 0x5410), __byte_perm(e.hi, e.lo, 0x7632));
+            }
         }
     }
     {   // R side: the thread holds contracted index U and open index o'; v along the registers
         tc::ld_32x32b_x32(tl + (BLK == 1 ? COL_V1 : COL_V2), f);
         tc::wait_ld();
         const int U = BLK == 0 ? lo : hi, Op = BLK == 0 ? hi : lo;
-        const bool odd = ((U + rho) & 1) != 0;
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            uint32_t wh[4], wl[4];
+        for (int rho = 0; rho < 2; ++rho) {
+            unsigned char* buf = rho ? buf1 : buf0;
+            const bool odd = ((U + rho) & 1) != 0;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {   // v = 2 j + odd for j = 2 i, 2 i + 1
-                const float y0 = __uint_as_float(odd ? f[8 * i + 2 + q] : f[8 * i + q]);
-                const float y1 = __uint_as_float(odd ? f[8 * i + 6 + q] : f[8 * i + 4 + q]);
-                const Pair e = split2(y0, y1, OPERAND_SCALE);
-                wh[i] = e.hi;
-                wl[i] = e.lo;
+            for (int q = 0; q < 2; ++q) {
+                uint32_t wh[4], wl[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {   // v = 2 j + odd for j = 2 i, 2 i + 1
+                    const float y0 = __uint_as_float(odd ? f[8 * i + 2 + q] : f[8 * i + q]);
+                    const float y1 = __uint_as_float(odd ? f[8 * i + 6 + q] : f[8 * i + 4 + q]);
+                    const Pair e = split2(y0, y1, OPERAND_SCALE);
+                    wh[i] = e.hi;
+                    wl[i] = e.lo;
+                }
+                const uint32_t o = r_off(2 * Op + q, 8 * U);
+                *reinterpret_cast<uint4*>(buf + X_BYTES + o) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+                *reinterpret_cast<uint4*>(buf + X_BYTES + R_BYTES + o) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
             }
-            const uint32_t o = r_off(2 * Op + q, 8 * U);
-            *reinterpret_cast<uint4*>(buf + X_BYTES + o) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-            *reinterpret_cast<uint4*>(buf + X_BYTES + R_BYTES + o) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
         }
     }
 }

@@ -59,3 +59,27 @@ def test_complex64_mixed_precision_within_bar(case, monkeypatch):
     print(f"complex64 mixed vs reference: max Bloch error {err:.3e}, mean |<Z> error| "
           f"{np.abs(got[:, 2] - want[:, 2]).mean():.3e}")
     assert err < 1e-3, err
+
+
+_CUDA_CORE_SCRIPT = """
+import sys, numpy as np, bqa_gb300
+from tests.test_gpu_c2_parity import FIXTURE
+from tests.golden.make_golden_c2 import config_from_fixture
+conf, want = config_from_fixture(FIXTURE), np.load(FIXTURE)["bloch"]
+got = bqa_gb300.run_qa(dict(conf), as_arrays=True)[0][1]
+err = float(np.abs(got - want).max())
+print(f"complex64 on the CUDA-core message kernel vs reference: max Bloch error {err:.3e}")
+sys.exit(0 if err < 1.8e-4 else 3)
+"""
+
+
+def test_complex64_cuda_core_kernel_within_bar(case):
+    """BQA_GB300_TC=0 at load: the degree-3 bond-dim-16 sweeps on the CUDA-core kernel instead of
+    the 2xFP16 tensor-core default, held to the same bar."""
+    import os
+    import subprocess
+    import sys
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, BQA_GB300_TC="0", BQA_PRECISION="single", PYTHONPATH=str(root))
+    r = subprocess.run([sys.executable, "-c", _CUDA_CORE_SCRIPT], cwd=root, env=env, timeout=900)
+    assert r.returncode == 0
