@@ -1547,12 +1547,8 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
             __syncthreads();
             tc::fence_after();
             if (t == 0) {
-                // V_2 and V_1 (all that block 0 reads) are committed first; V_0 completes before
-                // the MMAs of block 0, which block 1 waits for
-                tch::issue_product(tmem, rb, 2);
-                tch::issue_product(tmem, rb, 1);
+                tch::issue_products(tmem, rb);
                 tc::commit(bars);
-                tch::issue_product(tmem, rb, 0);
                 // the CTA's next half-node: its tensor and incoming messages into L2 meanwhile
                 const int hn = h + gridDim.x;
                 if (hn < halves) {

@@ -118,36 +118,33 @@ __device__ __forceinline__ void store_b(const float2 (&m)[3], const float (&s)[3
     }
 }
 
-// One thread: the 12 MMAs of the product on `bond` (2 row tiles x 2 K steps x 3 terms).
-__device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t rb, int bond) {
+// One thread: the 36 product MMAs (3 products x 2 row tiles x 2 K steps x 3 terms).
+__device__ __forceinline__ void issue_products(uint32_t tmem, uint32_t rb) {
     using tcb::PA_LBO;
     using tcb::PA_SBO;
     using tcb::PB_LBO;
     using tcb::PB_SBO;
-    const uint32_t aslot = (2 - bond) * A_BYTES;   // bond 2 at 0, bond 1 at 16 K, bond 0 at 32 K
-    const uint32_t col = bond == 2 ? COL_V2 : (bond == 1 ? COL_V1 : COL_V0);
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        const uint32_t d = tmem + col + 32 * j;
+    for (int bond = 0; bond < 3; ++bond) {
+        const uint32_t aslot = (2 - bond) * A_BYTES;   // bond 2 at 0, bond 1 at 16 K, bond 0 at 32 K
+        const uint32_t col = bond == 2 ? COL_V2 : (bond == 1 ? COL_V1 : COL_V0);
 #pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const uint32_t ao = rb + aslot + j * 16 * PA_SBO + s * 2 * PA_LBO;
-            const uint32_t bo = rb + bond * B_BYTES + s * 2 * PB_LBO;
-            const uint64_t ahi = tc::desc_noswz(ao + A_HI, PA_LBO, PA_SBO);
-            const uint64_t alo = tc::desc_noswz(ao + A_LO, PA_LBO, PA_SBO);
-            const uint64_t bhi = tc::desc_noswz(bo + B_HI, PB_LBO, PB_SBO);
-            const uint64_t blo = tc::desc_noswz(bo + B_LO, PB_LBO, PB_SBO);
-            tc::mma_f16(d, alo, bhi, IDESC, s ? 1u : 0u);
-            tc::mma_f16(d, ahi, blo, IDESC, 1u);
-            tc::mma_f16(d, ahi, bhi, IDESC, 1u);
+        for (int j = 0; j < 2; ++j) {
+            const uint32_t d = tmem + col + 32 * j;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                const uint32_t ao = rb + aslot + j * 16 * PA_SBO + s * 2 * PA_LBO;
+                const uint32_t bo = rb + bond * B_BYTES + s * 2 * PB_LBO;
+                const uint64_t ahi = tc::desc_noswz(ao + A_HI, PA_LBO, PA_SBO);
+                const uint64_t alo = tc::desc_noswz(ao + A_LO, PA_LBO, PA_SBO);
+                const uint64_t bhi = tc::desc_noswz(bo + B_HI, PB_LBO, PB_SBO);
+                const uint64_t blo = tc::desc_noswz(bo + B_LO, PB_LBO, PB_SBO);
+                tc::mma_f16(d, alo, bhi, IDESC, s ? 1u : 0u);
+                tc::mma_f16(d, ahi, blo, IDESC, 1u);
+                tc::mma_f16(d, ahi, bhi, IDESC, 1u);
+            }
         }
     }
-}
-
-// One thread: the 36 product MMAs.
-__device__ __forceinline__ void issue_products(uint32_t tmem, uint32_t rb) {
-#pragma unroll
-    for (int bond = 0; bond < 3; ++bond) issue_product(tmem, rb, bond);
 }
 
 // ---------------------------------------------------------------------------------------------
