@@ -10,8 +10,8 @@ bond dim and the number of nodes:
 * per class, within a form: the register-tiled kernel (half-node CTAs in the two-stage form,
   whole-node CTAs in the one-stage form; complex64, degree 2-4, bond dims 4/8/12/16), the
   generic shared-memory kernel (global-memory form for nodes beyond shared memory), or, in the
-  two-stage form at degree 3, bond dim 16, the half-node kernel whose bond products run on the
-  tensor cores (tcgen05, 3xTF32);
+  two-stage form at degree 3, bond dim 16, the FP32-accurate tensor-core half-node kernel
+  (tcgen05, bond products and closing contractions in 2xFP16; the library's default there);
 * for the generic kernel, the warps per node (CTA size): its own choice (one thread per fibre,
   up to 8 warps, or up to 32 for nodes whose shared memory leaves room for at most two CTAs
   per SM) or 16 or 32 warps at bond dims <= 8.
