@@ -1445,9 +1445,10 @@ __global__ void __launch_bounds__(tch::TH, 2) tch_half_kernel_d3c16(NodeArgs<flo
 // contractions on the tensor cores, both in 2xFP16 (FP32-accurate; tc_f16x2_d3c16.cuh): one
 // product round trip, then six closing stages (three blocks x two halves of the contraction)
 // through three shared-memory buffers, a block's two stages written from one read of the
-// accumulators while the previous block's MMAs run.  Diagonal incoming messages take the FP32
-// bond-scaling path with the closing contractions on the CUDA cores.  Same outputs as the other
-// half-node kernels.
+// accumulators while the previous block's MMAs run.  Diagonal incoming messages (the first sweep
+// after a truncation) take the same path: a diagonal message is just a sparse B operand, and
+// the bond-scaling path with CUDA-core closing contractions measured 13.4 ms against 10.4 ms
+// per 100k-node sweep.  Same outputs as the other half-node kernels.
 //
 // Grid-stride: at most two CTAs per SM walk the `halves` half-nodes; tensor memory is allocated
 // once per CTA.  Four mbarriers (products, stage buffers 0-2); every commit is waited for
@@ -1459,12 +1460,6 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
     constexpr int CHI = 16, D = 3, N2 = CHI * CHI, PS = CHI * CHI * CHI, TH = tch::TH;
     extern __shared__ double4_32a smem_raw[];
     unsigned char* reg = reinterpret_cast<unsigned char*>(smem_raw);
-    float2* const region = reinterpret_cast<float2*>(smem_raw);
-    float2* const V1 = region + tcd3::X_V1;
-    float2* const V2 = region + tcd3::X_V2;
-    float2* const V0 = region + tcd3::X_V0;
-    float2* const sP = region + tch::SP;
-    float2* const sMt = region + tch::SMT;
     uint64_t* bars = reinterpret_cast<uint64_t*>(reg + tch::REGION);   // products, buffers 0-2
     uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 4);
     volatile uint32_t* fault = slot + 1;
@@ -1484,27 +1479,25 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
     const uint32_t rb = tc::smem_u32(reg);
     uint32_t tmem = 0;
     uint32_t commits[4] = {0, 0, 0, 0};
-    int last = -1;   // barrier of the latest commit
+    int last = -1;          // barrier of the latest commit
+    uint32_t last_par = 0;  // and the parity of its phase
     bool tmem_held = false;
-    namespace q = tiled::d3c16;
-    constexpr int CT = 160;
     // this thread's row of the products' accumulators
     const int prow = 128 * (warp >> 2) + 32 * (warp & 3) + lane, phi = prow >> 4, plo = prow & 15;
     auto wait = [&](int i) {
         if (!tc::mbar_wait(bars + i, (commits[i] - 1) & 1, tch::WAIT_CYCLES)) *fault = 1;
     };
+#pragma unroll 1
     for (int h = blockIdx.x; h < halves; h += gridDim.x) {
         const int node = h >> 1, s = h & 1;
         float4 tv[8];
         tcd3::load_share(a.tensors + (size_t)node * 2 * PS + (size_t)s * PS, tv);
         // thread t holds entry (y, x) = (t >> 4, t & 15) of each incoming message
         float2 mv[3];
-        int offdiag = 0;
         uint32_t mm[3];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             mv[k] = msgs_in[(size_t)a.in_pos[node * D + k] * N2 + t];
-            offdiag |= ((t >> 4) != (t & 15)) && (mv[k].x != 0.f || mv[k].y != 0.f);
             mm[k] = __reduce_max_sync(0xffffffffu, max(tch::mag(mv[k].x), tch::mag(mv[k].y)));
         }
         uint32_t mt = 0;
@@ -1518,9 +1511,9 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
             for (int k = 0; k < D; ++k) wmax[4 * warp + 1 + k] = mm[k];
         }
         auto out_block = [&](int idx) { return a.out + ((size_t)a.out_pos[node * D + idx] * 2 + s) * N2; };
-        const bool diag = !__syncthreads_or(offdiag);
+        __syncthreads();
         if (*fault) break;
-        if (!diag) {
+        {
             uint32_t gm[4] = {0, 0, 0, 0};
 #pragma unroll
             for (int w = 0; w < TH / 32; ++w)
@@ -1561,6 +1554,7 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
             }
             ++commits[0];
             last = 0;
+            last_par = (commits[0] - 1) & 1;
             wait(0);
             tc::fence_after();
             const uint32_t tl = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32 * (warp >> 2);
@@ -1608,6 +1602,7 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
                 ++commits[1 + B0];
                 ++commits[1 + B1];
                 last = 1 + B1;
+                last_par = (commits[1 + B1] - 1) & 1;
             };
             block(std::integral_constant<int, 0>{});
             block(std::integral_constant<int, 1>{});
@@ -1618,42 +1613,13 @@ __global__ void __launch_bounds__(tch::TH, 2) tcx_half_kernel_d3c16(NodeArgs<flo
             tc::fence_after();
             block_epilogue(warp < 4 ? 1 : 2);
             tc::fence_before();   // these tensor-memory reads precede the next half-node's MMAs
-            continue;
         }
-        // all incoming messages diagonal: bond scalings in FP32 (sMt[k][16 x + y] = M_k[y][x]),
-        // closing contractions on warps 0-4, the previous block copied out by warps 5-7
-#pragma unroll
-        for (int k = 0; k < D; ++k) sMt[k * N2 + 16 * (t & 15) + (t >> 4)] = mv[k];
-        tcd3::store_share_swizzled(tv, V0);
-        __syncthreads();
-        tiled::diag_scale3<CHI, TH, 7>(V0, V1, sMt + N2, 1);
-        tiled::diag_scale3<CHI, TH, 7>(V0, V2, sMt + 2 * N2, 2);
-        __syncthreads();
-        tiled::diag_scale3<CHI, TH, 7>(V0, V0, sMt, 0);
-        __syncthreads();
-        float2* const sPb[2] = {sP, sP + N2};
-        int pend = -1, cur = 0;
-        auto emit_s = [&](auto idx_tag, const float2* X, const float2* R) {
-            constexpr int IDX = decltype(idx_tag)::value;
-            if (t < CT) q::close<IDX>(X, R, sPb[cur]);
-            else if (pend >= 0)
-                tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t - CT,
-                                             TH - CT);
-            __syncthreads();
-            pend = IDX;
-            cur ^= 1;
-        };
-        emit_s(std::integral_constant<int, 0>{}, V1, V2);
-        emit_s(std::integral_constant<int, 2>{}, V0, V1);
-        emit_s(std::integral_constant<int, 1>{}, V0, V2);
-        tiled::write_half_block<CHI>(sPb[cur ^ 1], reinterpret_cast<float4*>(out_block(pend)), t, TH);
-        __syncthreads();
     }
     tc::fence_before();
     __syncthreads();
     if (*fault) {
         // an MMA wait ran out: give the latest commit one more bounded wait, count the CTA
-        if (last >= 0) tc::mbar_wait(bars + last, (commits[last] - 1) & 1, tch::WAIT_CYCLES);
+        if (last >= 0) tc::mbar_wait(bars + last, last_par, tch::WAIT_CYCLES);
         if (t == 0) atomicAdd(&g_tc_faults, 1);
     }
     if (tmem_held && warp == 0) {

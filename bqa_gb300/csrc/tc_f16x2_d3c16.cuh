@@ -261,26 +261,21 @@ __device__ __forceinline__ void issue_stage(uint32_t d, uint32_t buf, uint32_t a
 // (16 values of part p), scaled by s[0] s[1], to P (global, row-major 16 x 16 complex).
 __device__ __forceinline__ void epilogue_block(uint32_t tmem_col, const float (&sc)[2], float* __restrict__ P) {
     const int w = (threadIdx.x >> 5) & 3, lane = threadIdx.x & 31;
-    uint32_t f[32];
-    tc::ld_32x32b_x32(tmem_col + ((uint32_t)(32 * w) << 16), f);
-    tc::wait_ld();
-    float g[32];
-#pragma unroll
-    for (int n = 0; n < 32; ++n) {
-        const float v = __uint_as_float(f[n]);
-        g[n] = v + __shfl_xor_sync(0xffffffffu, v, 1);
-    }
     const int pr = 8 * w + ((lane >> 1) & 7), o = pr >> 1, p = pr & 1;
-    float out[16];
 #pragma unroll
-    for (int y = 0; y < 16; ++y) {
-        const float h = __shfl_xor_sync(0xffffffffu, g[2 * y + 1], 2);
-        const float own = g[2 * y];
-        out[y] = (p ? h - own : own + h) * sc[0] * sc[1];
-    }
-    if (lane < 16 && !(lane & 1)) {
+    for (int half = 0; half < 2; ++half) {   // columns 2 y + q for y in [8 half, 8 half + 8)
+        uint32_t f[16];
+        tc::ld_32x32b_x16(tmem_col + ((uint32_t)(32 * w) << 16) + 16 * half, f);
+        tc::wait_ld();
 #pragma unroll
-        for (int y = 0; y < 16; ++y) P[2 * (o * 16 + y) + p] = out[y];
+        for (int y = 0; y < 8; ++y) {
+            const float re = __uint_as_float(f[2 * y]), im = __uint_as_float(f[2 * y + 1]);
+            const float g0 = re + __shfl_xor_sync(0xffffffffu, re, 1);
+            const float g1 = im + __shfl_xor_sync(0xffffffffu, im, 1);
+            const float h = __shfl_xor_sync(0xffffffffu, g1, 2);
+            const float out = (p ? h - g0 : g0 + h) * sc[0] * sc[1];
+            if (lane < 16 && !(lane & 1)) P[2 * (o * 16 + 8 * half + y) + p] = out;
+        }
     }
 }
 

@@ -7,7 +7,7 @@ BQA_VARIANT_TENSOR, and the default two-stage entry points that launch it):
   * one BP sweep equals one oracle sweep to the complex64 kernel tolerance (2e-5 relative);
   * it agrees with the CUDA-core half-node kernel (BQA_VARIANT_TILED) to 2e-6 relative on a
     few hundred nodes with dense random Hermitian messages;
-  * diagonal incoming messages take the bond-scaling path and match the oracle;
+  * diagonal incoming messages (the first sweep after a truncation) match the oracle;
   * the extended messages of the two-stage pass match the oracle;
   * the per-half-node FP16 operand scaling leaves normalised messages unchanged for tensors
     and messages far from unit scale;
