@@ -1,5 +1,8 @@
-// Tensor-core (tcgen05) bond products of the degree-3, bond-dim-16 half-node message kernel in
-// two FP16 terms (2xFP16), FP32-accurate; closing contractions on the CUDA cores (d3c16::close).
+// FP32-accurate tensor-core (tcgen05) parts of the degree-3, bond-dim-16 half-node message
+// kernels in two FP16 terms (2xFP16): the bond products (both kernels) and, further down, the
+// closing contractions of the all-tensor-core kernel (tcx_half_kernel_d3c16, the default); the
+// products-only kernel (tch_half_kernel_d3c16) keeps its closing contractions on the CUDA cores
+// (d3c16::close).
 //
 // The real GEMM of each product is that of tc_d3c16.cuh (rows r = the two kept bonds, K = the
 // interleaved parts of T along bond x, columns n = 2 y + q), with the operand layouts of
@@ -11,8 +14,9 @@
 // dropped A_lo B_lo and the split residuals are below 2^-21 |v| (11 + 11 significant bits), the
 // level of 3xTF32 (tc_d3c16.cuh).  Remainders of elements far below the block maximum fall into
 // FP16's subnormal range, where their absolute error stays below 2^-25 of a scaled value that
-// is at least 2^14: far below FP32 rounding of the largest element.  The epilogue multiplies
-// the accumulators by 2^-(k_T + k_M) (exact) before the closing contractions.
+// is at least 2^14: far below FP32 rounding of the largest element.  The products-only
+// kernel's epilogue multiplies the accumulators by 2^-(k_T + k_M) (exact) before the closing
+// contractions; the all-tensor-core kernel rescales them into its closing operands instead.
 //
 // Against 3xTF32 the operands take half the bytes, so the three products' A operands (hi and lo,
 // 96 KB) and the messages' B operands (12 KB) are all written at once and the 36 MMAs of a
@@ -21,10 +25,12 @@
 //
 // Shared memory (bytes, one region of 110,592): product phase -- A hi of bonds 2, 1, 0 at 0,
 // 16 K, 32 K; A lo at 48 K, 64 K, 80 K; B hi of messages 0, 1, 2 at 96 K + 2 K k; B lo at
-// 102 K + 2 K k.  Close phase -- V_1, V_2, V_0 (32 KB each, swizzled FP32, tc_d3c16.cuh
-// offsets), the two close output buffers and, on the diagonal-message path, the transposed
-// messages.  After the region: the mbarrier, the tensor-memory slot and the warps' maxima.
-// Tensor memory: V_2, V_1, V_0 at columns [0, 64), [64, 128), [128, 192) of 256.
+// 102 K + 2 K k.  Close phase of the products-only kernel -- V_1, V_2, V_0 (32 KB each,
+// swizzled FP32, tc_d3c16.cuh offsets), the two close output buffers and, on its
+// diagonal-message path, the transposed messages; of the all-tensor-core kernel -- three
+// closing-stage buffers (below).  After the region: the mbarrier(s), the tensor-memory slot
+// and the warps' maxima.  Tensor memory: V_2, V_1, V_0 at columns [0, 64), [64, 128),
+// [128, 192) of 256.
 #pragma once
 
 #include <cuda_fp16.h>
