@@ -1,6 +1,6 @@
 """CPU oracle for the bqa annealing hot path -- TEST INFRASTRUCTURE ONLY.
 
-This module is the checker, never the product: only ``tests/``, ``__graft_entry__.smoke()``
+This module is the oracle, never the product: only ``tests/``, ``__graft_entry__.smoke()``
 and the CPU-baseline leg of ``bench.py`` may import it.  The GB300 package never calls it
 and has no CPU fallback.
 
