@@ -46,4 +46,9 @@ def run_compiled(ctx, device=None, as_arrays: bool = False) -> list:
             out.append(["bloch_vectors", bloch if as_arrays else bloch.tolist()])
         else:
             raise ValueError(f"Unknown instruction {ins}")
+    # a tensor-core CTA whose bounded wait for its MMAs ran out voids the results (never in
+    # correct operation; the counter is read and reset once per job)
+    faults = job.lib.tc_faults(job.stream)
+    if faults:
+        raise RuntimeError(f"{faults} tensor-core CTA(s) timed out waiting for their MMAs; results are void")
     return out

@@ -285,7 +285,10 @@ int32_t bqa_bp_sweep_plan(const bqa_class* classes /* host array */, int32_t n_c
 /*
  * Tensor-core kernel health (no reference counterpart): *out (host) = the number of CTAs of the
  * tensor-core kernels whose bounded wait for their MMAs ran out since the library loaded (or
- * since the last reset), 0 in correct operation; such a CTA leaves its output blocks unwritten.
+ * since the last reset), 0 in correct operation; such a CTA's output blocks from that
+ * half-node on are not valid (left unwritten, or written from incomplete accumulators by the
+ * 2xFP16 kernel, which finishes the half-node before it stops), so a non-zero count voids the
+ * sweep.
  * reset != 0 zeroes the counter after reading it.  Blocks the calling thread until `stream`
  * has drained.
  */
